@@ -1,0 +1,181 @@
+/*
+ * dips.h -- C ABI of the GB300 (sm_103a) NBM jump-condition finite-volume residual.
+ *
+ * Every pointer argument is a device pointer owned by the caller (torch tensors, XLA
+ * buffers, cudaMalloc'd memory) unless the comment says "host".  Work runs on the
+ * cudaStream_t passed in; no entry point synchronises the device.  Each function
+ * returns 0 on success or a nonzero DIPS_E_* code; dips_last_error() gives the text
+ * of the last failure on the calling thread.  No C++ exception crosses this ABI.
+ *
+ * Layouts
+ *   points      float32 [n][3], row-major (x, y, z)               (domain/mesh.py:125-129)
+ *   level set   ghosted float32 cube [(nx+2)][(ny+2)][(nz+2)], C order, built by
+ *               dips_phi_ghost_layer from the [nx][ny][nz] samples  (domain/interpolate.py:762-816)
+ *   params      float32 flat vector: net u- then net u+; per net and hidden layer
+ *               W[in][out] row-major then b[out]; output layer W[width] then b[1].
+ *               This is the haiku tree order of double_mlp/~mlp_{m,p}_fn/linear{,_1,..}
+ *               (nn/mlp/MLP.py:101-139) with w before b.
+ *   job code    uint16: stencil point j (0..6: ijk, i-1, i+1, j-1, j+1, k-1, k+1) times 27
+ *               plus regression-cube vertex k (0..26, x fastest), bit 15 set when the
+ *               u+ network evaluates the point (phi >= 0, nn/mlp/MLP.py:98).
+ */
+#ifndef DIPS_H_
+#define DIPS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  DIPS_OK = 0,
+  DIPS_E_ARG = 1,        /* invalid argument (null pointer, bad size, unsupported shape) */
+  DIPS_E_CUDA = 2,       /* a CUDA call failed */
+  DIPS_E_WORKSPACE = 3,  /* workspace too small */
+  DIPS_E_UNSUPPORTED = 4 /* network shape without a compiled kernel */
+};
+
+/* Level-set grid: ghosted samples and ghosted coordinates (n+2 each). */
+typedef struct {
+  const float* phi_gh;
+  const float* xg;
+  const float* yg;
+  const float* zg;
+  int32_t nx, ny, nz; /* unghosted sizes */
+  /* bounds of the level-set grid, used by the box-boundary test
+     (solvers/poisson/discretization.py:60-65, :319-333) */
+  float xmin, xmax, ymin, ymax, zmin, zmax;
+} dips_levelset_t;
+
+/* Coefficient samples at the query points the geometry kernels emit (the user's
+   coefficient callables are evaluated by the host between classify/queries and assemble). */
+typedef struct {
+  const float* mu_m_face; /* [n][6] face centres imh, iph, jmh, jph, kmh, kph */
+  const float* mu_p_face; /* [n][6] */
+  const float* k_m;       /* [n] */
+  const float* k_p;       /* [n] */
+  const float* f_m;       /* [n] */
+  const float* f_p;       /* [n] */
+  const float* g;         /* [n] Dirichlet value at the point */
+  const float* beta_tri;  /* [3 * sum n_tri] beta at interface-triangle vertices */
+  const float* mu_m_s;    /* [sum n_xs] mu- at crossed stencil points */
+  const float* mu_p_s;    /* [sum n_xs] mu+ at crossed stencil points */
+  const float* alpha_r;   /* [sum n_xs] alpha at the projection r = s - phi(s) n */
+  const float* beta_r;    /* [sum n_xs] beta at r */
+  const float* mu_m_r;    /* [sum n_xs] mu- at r */
+  const float* mu_p_r;    /* [sum n_xs] mu+ at r */
+  float beta_origin;      /* beta(0,0,0): the reference also integrates its zero-padding triangles */
+} dips_coeffs_t;
+
+/* Per-point residual records of one stencil spacing h (one "level"). */
+typedef struct {
+  const float* pts;         /* [n][3] */
+  int64_t n_pts;
+  float h[3];
+  const float* lhs0;        /* [n] constant part of lhs (jump terms) */
+  const float* diag;        /* [n] diagonal coefficient (discretization.py:381-386) */
+  const float* rod;         /* [n] nan_to_num(rhs / diag) */
+  const int32_t* cnt;       /* [n] jobs of the point */
+  const int32_t* cnt_m;     /* [n] of which u- network jobs (stored first) */
+  const int64_t* job_off;   /* [n] first job of the point */
+  const uint16_t* job_code; /* [jobs] */
+  const float* job_A;       /* [jobs] lhs coefficient of the network value at the job point */
+} dips_records_t;
+
+typedef struct {
+  int32_t m_layers, m_width, p_layers, p_width; /* DoubleMLP hidden layers and widths, tanh */
+} dips_arch_t;
+
+/* optax chain: clip_by_global_norm -> scale_by_adam -> scale_by_schedule(exponential_decay)
+   -> scale(-1) (solvers/optimizers.py:33-54). */
+typedef struct {
+  float lr, decay_rate, transition_steps, max_norm, b1, b2, eps;
+} dips_adam_t;
+
+/* ---- errors ------------------------------------------------------------------------- */
+/* Text of the last failure on this thread (static storage; never NULL). */
+const char* dips_last_error(void);
+/* Library version string (host). */
+const char* dips_version(void);
+
+/* ---- level set: replaces domain/interpolate.py:762-816 and :906-1021 ------------------ */
+/* Ghost layer of linear extrapolation around the [nx][ny][nz] samples. */
+int dips_phi_ghost_layer(const float* phi, int32_t nx, int32_t ny, int32_t nz, float* phi_gh,
+                         cudaStream_t stream);
+/* Trilinear interpolation of the ghosted cube at n points (multilinear_interpolation). */
+int dips_phi_trilinear(const dips_levelset_t* ls, const float* pts, int64_t n, float* out,
+                       cudaStream_t stream);
+
+/* ---- geometry: replaces geometry/geometric_integrations_per_point.py:201-1009 and
+        solvers/poisson/discretization.py:164-519 (the parameter-independent part) ------- */
+/* Pass 1: per point, flags (bit 0 box boundary, bits 1-2 crossed(p) as 0/1/2 for -1/0/+1,
+   bits 4..17 crossed(s_j) two bits per stencil point, bits 18..24 phi(s_j) >= 0),
+   number of real interface triangles of the point's cell, number of interface-crossed
+   stencil points, and an upper bound of its jobs. */
+int dips_geometry_classify(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
+                           uint32_t* flags, int32_t* n_tri, int32_t* n_xs, int32_t* job_cap,
+                           cudaStream_t stream);
+/* Pass 2: query coordinates for the coefficient callables: interface-triangle vertices
+   (3 per triangle, at tri_off[i]*3), crossed stencil points and their projections onto
+   the interface (at xs_off[i]); offsets are exclusive prefix sums of pass-1 counts. */
+int dips_geometry_queries(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
+                          const uint32_t* flags, const int64_t* tri_off, const int64_t* xs_off,
+                          float* tri_pts, float* xs_pts, float* xr_pts, cudaStream_t stream);
+/* Pass 3: the per-point residual records.  Jobs of point i are written at job_off[i]
+   (a prefix sum of job_cap); cnt[i] <= job_cap[i] are used, u- jobs first.  coeff26
+   ([n][26], may be NULL) receives compute_face_centroids_values_plus_minus_at_point and
+   beta_int ([n], may be NULL) the interface integral of beta. */
+int dips_geometry_assemble(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
+                           const uint32_t* flags, const int64_t* tri_off, const int64_t* xs_off,
+                           const int64_t* job_off, const dips_coeffs_t* co, float* lhs0, float* diag,
+                           float* rod, int32_t* cnt, int32_t* cnt_m, uint16_t* job_code, float* job_A,
+                           float* coeff26, float* beta_int, cudaStream_t stream);
+
+/* ---- residual, loss, adjoint, optimizer: replace Trainer.loss (trainer.py:892-912),
+        value_and_grad in Trainer.update (:783-789) and the optax chain ---------------- */
+int32_t dips_num_params(const dips_arch_t* arch);
+/* 1 if a kernel is compiled for this network shape. */
+int32_t dips_arch_supported(const dips_arch_t* arch);
+/* Workspace bytes for a step over `batch` points whose jobs total at most max_jobs. */
+size_t dips_step_workspace_bytes(const dips_arch_t* arch, int64_t batch, int64_t max_jobs);
+/* Loss over a batch: point ids batch_ids[0..B) (NULL = 0..B-1).  loss_out: device double.
+   residual_out ([B], may be NULL) receives lhs/diag - rhs/diag per batch slot. */
+int dips_residual_fwd(const dips_arch_t* arch, const float* params, const dips_records_t* rec,
+                      const int32_t* batch_ids, int64_t batch, void* workspace, size_t ws_bytes,
+                      double* loss_out, float* residual_out, cudaStream_t stream);
+/* Gradient of the loss of the preceding dips_residual_fwd call (same workspace) with
+   respect to the params: grad_out [num_params]. */
+int dips_residual_bwd(const dips_arch_t* arch, const float* params, const dips_records_t* rec,
+                      const int32_t* batch_ids, int64_t batch, void* workspace, size_t ws_bytes,
+                      float* grad_out, cudaStream_t stream);
+/* One chained-Adam update of params (in place) from grad; mu, nu: [num_params];
+   count: device int64 step counter (incremented). */
+int dips_adam_step(const dips_arch_t* arch, const dips_adam_t* hp, float* params, const float* grad,
+                   float* mu, float* nu, int64_t* count, cudaStream_t stream);
+/* Fused training step = residual_fwd + residual_bwd + adam_step.  loss_out: device double. */
+int dips_train_step(const dips_arch_t* arch, const dips_adam_t* hp, float* params, float* mu, float* nu,
+                    int64_t* count, const dips_records_t* rec, const int32_t* batch_ids, int64_t batch,
+                    void* workspace, size_t ws_bytes, double* loss_out, float* grad_out,
+                    cudaStream_t stream);
+/* Batch ids of batch `index` of an epoch: a seeded bijective permutation of 0..n-1
+   (uniform minibatches without replacement), written to ids[0..B).  epoch_index and
+   seed select the permutation. */
+int dips_batch_ids(int64_t n, int64_t epoch_index, uint64_t seed, int64_t batch_index, int64_t batch,
+                   int32_t* ids, cudaStream_t stream);
+
+/* ---- network evaluation: replaces Trainer.evaluate_solution_fn (trainer.py:836-844)
+        and compute_gradient_solution_neural_network (:953-957) --------------------------- */
+/* u and grad u (grad_out [n][3], may be NULL) at n points; the network is chosen by
+   phi_at (phi >= 0 -> u+). */
+int dips_mlp_eval(const dips_arch_t* arch, const float* params, const float* pts, const float* phi_at,
+                  int64_t n, float* u_out, float* grad_out, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DIPS_H_ */

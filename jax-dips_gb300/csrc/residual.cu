@@ -1,0 +1,519 @@
+// Arch-independent part of the fused NBM residual step and the C API (sm_103a).
+//
+// Work unit: a "job" is one evaluation of a u-/u+ network at a stencil or regression-cube
+// point of a training point.  A point's residual is affine in its job values:
+//     r = nan_to_num((lhs0 + sum_j A_j u(x_j)) / diag) - rod
+// (the records come from geometry.cu).  One step:
+//   expand   batch -> job list, u- jobs first (padded to a multiple of 32), then u+ jobs
+//   forward  thread per job (residual_arch.cuh)
+//   residual thread per batch point: r, loss partials (FP64), dL/dlhs
+//   adjoint  thread per job (residual_arch.cuh): one partial gradient row per CTA
+//   reduce   partial rows -> gradient;  adam: clip -> Adam -> schedule -> apply
+//
+// Reference: Trainer.loss / update (solvers/poisson/trainer.py:783-789, :892-912),
+// chained_adam (solvers/optimizers.py:33-54).
+
+#include <math.h>
+
+#include "residual_common.cuh"
+
+namespace dips {
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static size_t carve(Workspace* w, char* base, int64_t B, int64_t max_jobs, int P) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* p = base ? base + off : nullptr;
+    off = align256(off + bytes);
+    return p;
+  };
+  Workspace W;
+  W.nblk = (B + kScanBlock - 1) / kScanBlock;
+  W.nres = (B + 255) / 256;
+  W.jcap = max_jobs + 64;
+  W.grid = kAdjGrid;
+  W.ctl = (Ctl*)take(sizeof(Ctl));
+  W.cm = (int32_t*)take(sizeof(int32_t) * B);
+  W.cp = (int32_t*)take(sizeof(int32_t) * B);
+  W.om = (int64_t*)take(sizeof(int64_t) * B);
+  W.op = (int64_t*)take(sizeof(int64_t) * B);
+  W.gs = (float*)take(sizeof(float) * B);
+  W.res = (float*)take(sizeof(float) * B);
+  W.blk = (int64_t*)take(sizeof(int64_t) * 2 * (W.nblk + 1));
+  W.lossp = (double*)take(sizeof(double) * W.nres);
+  W.jslot = (int32_t*)take(sizeof(int32_t) * W.jcap);
+  W.jcode = (uint16_t*)take(sizeof(uint16_t) * W.jcap);
+  W.jA = (float*)take(sizeof(float) * W.jcap);
+  W.ju = (float*)take(sizeof(float) * W.jcap);
+  W.partials = (float*)take(sizeof(float) * (size_t)W.grid * P);
+  W.grad = (float*)take(sizeof(float) * P);
+  if (w) *w = W;
+  return off;
+}
+
+// ----------------------------------------------------------------------------------------
+// expansion of a batch into jobs
+// ----------------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T warp_incl_scan(T v, int lane) {
+#pragma unroll
+  for (int s = 1; s < 32; s <<= 1) {
+    T t = __shfl_up_sync(0xffffffffu, v, s);
+    if (lane >= s) v += t;
+  }
+  return v;
+}
+
+// exclusive block scan of two counters; returns block totals through *tot
+__device__ __forceinline__ void block_scan2(int64_t a, int64_t b, int64_t* ea, int64_t* eb, int64_t* ta, int64_t* tb) {
+  __shared__ int64_t wa[32], wb[32], tot[2];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int64_t ia = warp_incl_scan(a, lane), ib = warp_incl_scan(b, lane);
+  if (lane == 31) {
+    wa[wid] = ia;
+    wb[wid] = ib;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    int64_t va = lane < nw ? wa[lane] : 0, vb = lane < nw ? wb[lane] : 0;
+    int64_t sa = warp_incl_scan(va, lane), sb = warp_incl_scan(vb, lane);
+    if (lane < nw) {
+      wa[lane] = sa - va;
+      wb[lane] = sb - vb;
+    }
+    if (lane == nw - 1) {
+      tot[0] = sa;
+      tot[1] = sb;
+    }
+  }
+  __syncthreads();
+  *ea = wa[wid] + ia - a;
+  *eb = wb[wid] + ib - b;
+  *ta = tot[0];
+  *tb = tot[1];
+  __syncthreads();
+}
+
+__global__ void k_count(const int32_t* __restrict__ ids, int64_t B, const int32_t* __restrict__ cnt,
+                        const int32_t* __restrict__ cnt_m, Workspace w) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t a = 0, c = 0;
+  if (b < B) {
+    const int64_t pid = batch_pid(ids, b);
+    a = cnt_m[pid];
+    c = cnt[pid] - a;
+    w.cm[b] = (int32_t)a;
+    w.cp[b] = (int32_t)c;
+  }
+  int64_t ea, eb, ta, tb;
+  block_scan2(a, c, &ea, &eb, &ta, &tb);
+  if (b < B) {
+    w.om[b] = ea;
+    w.op[b] = eb;
+  }
+  if (threadIdx.x == 0) {
+    w.blk[2 * blockIdx.x] = ta;
+    w.blk[2 * blockIdx.x + 1] = tb;
+  }
+}
+
+__global__ void k_scan_blocks(Workspace w) {
+  int64_t carry_a = 0, carry_b = 0;
+  for (int64_t base = 0; base < w.nblk; base += blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    const int64_t a = i < w.nblk ? w.blk[2 * i] : 0, b = i < w.nblk ? w.blk[2 * i + 1] : 0;
+    int64_t ea, eb, ta, tb;
+    block_scan2(a, b, &ea, &eb, &ta, &tb);
+    if (i < w.nblk) {
+      w.blk[2 * i] = ea + carry_a;
+      w.blk[2 * i + 1] = eb + carry_b;
+    }
+    carry_a += ta;
+    carry_b += tb;
+  }
+  if (threadIdx.x == 0) {
+    const int64_t jm = carry_a, jp = carry_b;
+    const int64_t jm_pad = (jm + 31) / 32 * 32;
+    const bool over = jm_pad + jp > w.jcap;
+    // on overflow no job is expanded or evaluated and every residual becomes NaN
+    w.ctl->overflow = over ? 1 : 0;
+    w.ctl->jm = over ? 0 : jm;
+    w.ctl->jp = over ? 0 : jp;
+    w.ctl->jm_pad = over ? 0 : jm_pad;
+    w.ctl->total = over ? 0 : jm_pad + jp;
+  }
+}
+
+__global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, dips_records_t rec, Workspace w) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const Ctl ctl = *w.ctl;
+  if (ctl.overflow) return;
+  if (b == 0) {  // padding jobs between the u- and u+ segments
+    for (int64_t j = ctl.jm; j < ctl.jm_pad; ++j) {
+      w.jslot[j] = -1;
+      w.jcode[j] = job_code(0, kCubeCentre, false);
+      w.jA[j] = 0.0f;
+    }
+  }
+  if (b >= B) return;
+  const int64_t pid = batch_pid(ids, b);
+  const int64_t om = w.om[b] + w.blk[2 * blockIdx.x];
+  const int64_t op = w.op[b] + w.blk[2 * blockIdx.x + 1] + ctl.jm_pad;
+  w.om[b] = om;
+  w.op[b] = op;
+  const int cm = w.cm[b], cp = w.cp[b];
+  const int64_t src_m = rec.job_off[pid];
+  const int64_t src_p = rec.job_off[pid + 1] - cp;
+  for (int q = 0; q < cm; ++q) {
+    w.jslot[om + q] = (int32_t)b;
+    w.jcode[om + q] = rec.job_code[src_m + q];
+    w.jA[om + q] = rec.job_A[src_m + q];
+  }
+  for (int q = 0; q < cp; ++q) {
+    w.jslot[op + q] = (int32_t)b;
+    w.jcode[op + q] = rec.job_code[src_p + q];
+    w.jA[op + q] = rec.job_A[src_p + q];
+  }
+}
+
+// ----------------------------------------------------------------------------------------
+// residual and loss per batch point
+// ----------------------------------------------------------------------------------------
+__device__ __forceinline__ double block_sum_d(double v) {
+  __shared__ double ws[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int s = 16; s > 0; s >>= 1) v += __shfl_down_sync(0xffffffffu, v, s);
+  if (lane == 0) ws[wid] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (wid == 0) {
+    t = lane < nw ? ws[lane] : 0.0;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) t += __shfl_down_sync(0xffffffffu, t, s);
+  }
+  __syncthreads();
+  return t;
+}
+
+__global__ void k_residual(const int32_t* __restrict__ ids, int64_t B, dips_records_t rec, Workspace w,
+                           float* __restrict__ residual_out) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool overflow = w.ctl->overflow != 0;
+  double l = 0.0;
+  if (b < B && overflow) {
+    w.res[b] = nanf("");
+    w.gs[b] = 0.0f;
+    if (residual_out) residual_out[b] = nanf("");
+    l = nan("");
+  } else if (b < B) {
+    const int64_t pid = batch_pid(ids, b);
+    float lhs = rec.lhs0[pid];
+    const int64_t om = w.om[b], op = w.op[b];
+    const int cm = w.cm[b], cp = w.cp[b];
+    for (int q = 0; q < cm; ++q) lhs = fmaf(w.jA[om + q], w.ju[om + q], lhs);
+    for (int q = 0; q < cp; ++q) lhs = fmaf(w.jA[op + q], w.ju[op + q], lhs);
+    const float diag = rec.diag[pid];
+    const float q = lhs / diag;
+    const float r = nan_to_num(q) - rec.rod[pid];
+    w.res[b] = r;
+    // d(mean 0.5 r^2)/d lhs; nan_to_num has zero derivative where lhs/diag is not finite
+    w.gs[b] = isfinite(q) ? (r / (float)B) / diag : 0.0f;
+    if (residual_out) residual_out[b] = r;
+    l = 0.5 * (double)r * (double)r;
+  }
+  const double t = block_sum_d(l);
+  if (threadIdx.x == 0) w.lossp[blockIdx.x] = t;
+}
+
+__global__ void k_loss_final(Workspace w, int64_t B, double* __restrict__ loss_out) {
+  double v = 0.0;
+  for (int64_t i = threadIdx.x; i < w.nres; i += blockDim.x) v += w.lossp[i];
+  const double t = block_sum_d(v);
+  if (threadIdx.x == 0) *loss_out = t / (double)B;
+}
+
+__global__ void k_grad_reduce(Workspace w, int P, float* __restrict__ grad_out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  float v = 0.0f;
+  for (int c = 0; c < w.grid; ++c) v += w.partials[(size_t)c * P + i];
+  grad_out[i] = v;
+}
+
+// ----------------------------------------------------------------------------------------
+// chained Adam (optax 0.1.5 semantics)
+// ----------------------------------------------------------------------------------------
+__global__ void k_adam(dips_adam_t hp, int P, float* __restrict__ params, const float* __restrict__ grad,
+                       float* __restrict__ mu, float* __restrict__ nu, int64_t* __restrict__ count) {
+  __shared__ float red[32];
+  __shared__ float s_scale;
+  __shared__ int64_t s_count;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  float ss = 0.0f;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) ss = fmaf(grad[i], grad[i], ss);
+#pragma unroll
+  for (int s = 16; s > 0; s >>= 1) ss += __shfl_down_sync(0xffffffffu, ss, s);
+  if (lane == 0) red[wid] = ss;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+    for (int q = 0; q < nw; ++q) t += red[q];
+    const float gnorm = sqrtf(t);
+    // clip_by_global_norm: keep g when gnorm < max_norm, else g / gnorm * max_norm
+    s_scale = (gnorm < hp.max_norm) ? -1.0f : gnorm;
+    s_count = *count;
+  }
+  __syncthreads();
+  const float gnorm = s_scale;
+  const int64_t cnt0 = s_count;
+  const float cnt1 = (float)(cnt0 + 1);
+  const float bc1 = 1.0f - powf(hp.b1, cnt1);
+  const float bc2 = 1.0f - powf(hp.b2, cnt1);
+  const float step = hp.lr * powf(hp.decay_rate, (float)cnt0 / hp.transition_steps);
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    float g = grad[i];
+    if (gnorm >= 0.0f) g = (g / gnorm) * hp.max_norm;
+    const float m = (1.0f - hp.b1) * g + hp.b1 * mu[i];
+    const float v = (1.0f - hp.b2) * (g * g) + hp.b2 * nu[i];
+    mu[i] = m;
+    nu[i] = v;
+    const float upd = (m / bc1) / (sqrtf(v / bc2) + hp.eps);
+    params[i] = params[i] + (upd * step) * -1.0f;
+  }
+  if (threadIdx.x == 0) *count = cnt0 + 1;
+}
+
+// ----------------------------------------------------------------------------------------
+// seeded bijective permutation (4-round Feistel network with cycle walking)
+// ----------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+
+__device__ __forceinline__ uint64_t feistel(uint64_t v, int half, uint64_t key) {
+  const uint64_t mask = (1ull << half) - 1;
+  uint64_t l = v >> half, r = v & mask;
+#pragma unroll
+  for (int round = 0; round < 4; ++round) {
+    const uint32_t f = mix32((uint32_t)r ^ (uint32_t)(key >> (round * 8)) ^ (uint32_t)(round * 0x9e3779b9u) ^
+                             (uint32_t)(key >> 32));
+    const uint64_t nl = r;
+    r = (l ^ f) & mask;
+    l = nl;
+  }
+  return (l << half) | r;
+}
+
+__global__ void k_batch_ids(int64_t n, uint64_t key, int half, int64_t start, int64_t B, int32_t* __restrict__ ids) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  uint64_t v = (uint64_t)(start + b);
+  // cycle walking: iterate the permutation of [0, 2^(2*half)) until the value lands in [0, n)
+  for (int it = 0; it < (1 << 24); ++it) {
+    v = feistel(v, half, key);
+    if (v < (uint64_t)n) break;
+  }
+  ids[b] = (int32_t)v;
+}
+
+// ----------------------------------------------------------------------------------------
+// network-shape table
+// ----------------------------------------------------------------------------------------
+const ArchOps* arch_ops_1_1_2_10();
+const ArchOps* arch_ops_2_8_2_8();
+const ArchOps* arch_ops_2_16_2_16();
+const ArchOps* arch_ops_3_32_3_32();
+
+static const ArchOps* find_arch(const dips_arch_t* a) {
+  if (!a) {
+    set_error("null arch");
+    return nullptr;
+  }
+  const ArchOps* table[] = {arch_ops_1_1_2_10(), arch_ops_2_8_2_8(), arch_ops_2_16_2_16(), arch_ops_3_32_3_32()};
+  for (const ArchOps* o : table)
+    if (o->m_layers == a->m_layers && o->m_width == a->m_width && o->p_layers == a->p_layers &&
+        o->p_width == a->p_width)
+      return o;
+  set_error("no kernel compiled for DoubleMLP m=%dx%d p=%dx%d (supported: 1x1/2x10, 2x8/2x8, 2x16/2x16, 3x32/3x32)",
+            a->m_layers, a->m_width, a->p_layers, a->p_width);
+  return nullptr;
+}
+
+static int arch_params(const dips_arch_t* a) {
+  if (!a || a->m_layers < 1 || a->p_layers < 1 || a->m_width < 1 || a->p_width < 1) return -1;
+  auto np = [](int L, int W) { return 3 * W + W + (L - 1) * (W * W + W) + W + 1; };
+  return np(a->m_layers, a->m_width) + np(a->p_layers, a->p_width);
+}
+
+static int check_rec(const dips_records_t* rec, int64_t B) {
+  DIPS_REQUIRE(rec && rec->pts && rec->lhs0 && rec->diag && rec->rod && rec->cnt && rec->cnt_m && rec->job_off &&
+                   rec->job_code && rec->job_A,
+               DIPS_E_ARG, "records: null pointer");
+  DIPS_REQUIRE(B > 0 && B <= 0x7fffffff, DIPS_E_ARG, "batch size must be in [1, 2^31)");
+  return DIPS_OK;
+}
+
+static PtsH make_ph(const dips_records_t* rec) {
+  PtsH ph;
+  ph.pts = rec->pts;
+  ph.h[0] = rec->h[0];
+  ph.h[1] = rec->h[1];
+  ph.h[2] = rec->h[2];
+  return ph;
+}
+
+static int prep_ws(const dips_arch_t* arch, int64_t B, void* ws, size_t ws_bytes, Workspace* W) {
+  const int P = arch_params(arch);
+  DIPS_REQUIRE(P > 0, DIPS_E_ARG, "invalid arch");
+  DIPS_REQUIRE(ws != nullptr, DIPS_E_ARG, "null workspace");
+  const size_t fixed = carve(nullptr, nullptr, B, 0, P);
+  DIPS_REQUIRE(ws_bytes >= fixed + 256, DIPS_E_WORKSPACE, "workspace too small: %zu < %zu", ws_bytes, fixed + 256);
+  char* base = (char*)(((uintptr_t)ws + 255) & ~(uintptr_t)255);
+  const size_t avail = ws_bytes - (size_t)(base - (char*)ws);
+  // largest job capacity whose layout fits
+  int64_t lo = 0, hi = (int64_t)(avail / 14) + 1;
+  while (lo + 1 < hi) {
+    const int64_t mid = (lo + hi) / 2;
+    if (carve(nullptr, nullptr, B, mid, P) <= avail)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  carve(W, base, B, lo, P);
+  return DIPS_OK;
+}
+
+static int run_forward(const ArchOps* ops, const float* params, const dips_records_t* rec, const int32_t* ids,
+                       int64_t B, Workspace& W, double* loss_out, float* residual_out, cudaStream_t s) {
+  int st = ops->load_params(params, s);
+  if (st) return st;
+  const int nblk = (int)W.nblk;
+  k_count<<<nblk, kScanBlock, 0, s>>>(ids, B, rec->cnt, rec->cnt_m, W);
+  k_scan_blocks<<<1, kScanBlock, 0, s>>>(W);
+  k_emit<<<nblk, kScanBlock, 0, s>>>(ids, B, *rec, W);
+  DIPS_CHECK_LAUNCH("job expansion");
+  st = ops->job_forward(make_ph(rec), ids, W, s);
+  if (st) return st;
+  k_residual<<<(int)W.nres, 256, 0, s>>>(ids, B, *rec, W, residual_out);
+  if (loss_out) k_loss_final<<<1, 256, 0, s>>>(W, B, loss_out);
+  DIPS_CHECK_LAUNCH("residual");
+  return DIPS_OK;
+}
+
+static int run_backward(const ArchOps* ops, const dips_records_t* rec, const int32_t* ids, Workspace& W,
+                        float* grad_out, cudaStream_t s) {
+  int st = ops->job_adjoint(make_ph(rec), ids, W, s);
+  if (st) return st;
+  k_grad_reduce<<<div_up(ops->n_params, 256), 256, 0, s>>>(W, ops->n_params, grad_out);
+  DIPS_CHECK_LAUNCH("gradient reduction");
+  return DIPS_OK;
+}
+
+}  // namespace dips
+
+using namespace dips;
+
+extern "C" int32_t dips_num_params(const dips_arch_t* arch) { return arch_params(arch); }
+
+extern "C" int32_t dips_arch_supported(const dips_arch_t* arch) { return find_arch(arch) ? 1 : 0; }
+
+extern "C" size_t dips_step_workspace_bytes(const dips_arch_t* arch, int64_t batch, int64_t max_jobs) {
+  const int P = arch_params(arch);
+  if (P <= 0 || batch <= 0 || max_jobs < 0) return 0;
+  return carve(nullptr, nullptr, batch, max_jobs, P) + 256;
+}
+
+extern "C" int dips_residual_fwd(const dips_arch_t* arch, const float* params, const dips_records_t* rec,
+                                 const int32_t* batch_ids, int64_t batch, void* workspace, size_t ws_bytes,
+                                 double* loss_out, float* residual_out, cudaStream_t stream) {
+  int st = check_rec(rec, batch);
+  if (st) return st;
+  DIPS_REQUIRE(params, DIPS_E_ARG, "null params");
+  const ArchOps* ops = find_arch(arch);
+  if (!ops) return DIPS_E_UNSUPPORTED;
+  Workspace W;
+  st = prep_ws(arch, batch, workspace, ws_bytes, &W);
+  if (st) return st;
+  return run_forward(ops, params, rec, batch_ids, batch, W, loss_out, residual_out, stream);
+}
+
+extern "C" int dips_residual_bwd(const dips_arch_t* arch, const float* params, const dips_records_t* rec,
+                                 const int32_t* batch_ids, int64_t batch, void* workspace, size_t ws_bytes,
+                                 float* grad_out, cudaStream_t stream) {
+  int st = check_rec(rec, batch);
+  if (st) return st;
+  DIPS_REQUIRE(params && grad_out, DIPS_E_ARG, "null params or grad_out");
+  const ArchOps* ops = find_arch(arch);
+  if (!ops) return DIPS_E_UNSUPPORTED;
+  Workspace W;
+  st = prep_ws(arch, batch, workspace, ws_bytes, &W);
+  if (st) return st;
+  st = ops->load_params(params, stream);
+  if (st) return st;
+  return run_backward(ops, rec, batch_ids, W, grad_out, stream);
+}
+
+extern "C" int dips_adam_step(const dips_arch_t* arch, const dips_adam_t* hp, float* params, const float* grad,
+                              float* mu, float* nu, int64_t* count, cudaStream_t stream) {
+  const int P = arch_params(arch);
+  DIPS_REQUIRE(P > 0 && hp && params && grad && mu && nu && count, DIPS_E_ARG, "dips_adam_step: bad argument");
+  k_adam<<<1, 1024, 0, stream>>>(*hp, P, params, grad, mu, nu, count);
+  DIPS_CHECK_LAUNCH("dips_adam_step");
+  return DIPS_OK;
+}
+
+extern "C" int dips_train_step(const dips_arch_t* arch, const dips_adam_t* hp, float* params, float* mu, float* nu,
+                               int64_t* count, const dips_records_t* rec, const int32_t* batch_ids, int64_t batch,
+                               void* workspace, size_t ws_bytes, double* loss_out, float* grad_out,
+                               cudaStream_t stream) {
+  int st = check_rec(rec, batch);
+  if (st) return st;
+  DIPS_REQUIRE(hp && params && mu && nu && count, DIPS_E_ARG, "dips_train_step: null pointer");
+  const ArchOps* ops = find_arch(arch);
+  if (!ops) return DIPS_E_UNSUPPORTED;
+  Workspace W;
+  st = prep_ws(arch, batch, workspace, ws_bytes, &W);
+  if (st) return st;
+  st = run_forward(ops, params, rec, batch_ids, batch, W, loss_out, nullptr, stream);
+  if (st) return st;
+  float* g = grad_out ? grad_out : W.grad;
+  st = run_backward(ops, rec, batch_ids, W, g, stream);
+  if (st) return st;
+  k_adam<<<1, 1024, 0, stream>>>(*hp, ops->n_params, params, g, mu, nu, count);
+  DIPS_CHECK_LAUNCH("dips_train_step adam");
+  return DIPS_OK;
+}
+
+extern "C" int dips_batch_ids(int64_t n, int64_t epoch_index, uint64_t seed, int64_t batch_index, int64_t batch,
+                              int32_t* ids, cudaStream_t stream) {
+  DIPS_REQUIRE(n > 0 && n <= 0x7fffffff && batch > 0 && ids && batch_index >= 0, DIPS_E_ARG,
+               "dips_batch_ids: bad argument");
+  DIPS_REQUIRE((batch_index + 1) * batch <= n, DIPS_E_ARG, "dips_batch_ids: batch %lld of size %lld exceeds n=%lld",
+               (long long)batch_index, (long long)batch, (long long)n);
+  int bits = 1;
+  while ((1ll << bits) < n) ++bits;
+  const int half = (bits + 1) / 2;
+  const uint64_t key = seed * 0x9E3779B97F4A7C15ull ^ (uint64_t)(epoch_index + 1) * 0xD1B54A32D192ED03ull;
+  k_batch_ids<<<div_up(batch, 256), 256, 0, stream>>>(n, key, half, batch_index * batch, batch, ids);
+  DIPS_CHECK_LAUNCH("dips_batch_ids");
+  return DIPS_OK;
+}
+
+extern "C" int dips_mlp_eval(const dips_arch_t* arch, const float* params, const float* pts, const float* phi_at,
+                             int64_t n, float* u_out, float* grad_out, cudaStream_t stream) {
+  DIPS_REQUIRE(n >= 0, DIPS_E_ARG, "dips_mlp_eval: negative n");
+  if (n == 0) return DIPS_OK;
+  DIPS_REQUIRE(params && pts && phi_at && u_out, DIPS_E_ARG, "dips_mlp_eval: null pointer");
+  const ArchOps* ops = find_arch(arch);
+  if (!ops) return DIPS_E_UNSUPPORTED;
+  int st = ops->load_params(params, stream);
+  if (st) return st;
+  return ops->mlp_eval(pts, phi_at, n, u_out, grad_out, stream);
+}

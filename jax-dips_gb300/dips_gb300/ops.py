@@ -1,0 +1,114 @@
+"""Residual, loss, adjoint and optimizer entry points over the C ABI, and the
+``torch.autograd.Function`` that replaces ``value_and_grad(Trainer.loss)``
+(solvers/poisson/trainer.py:783-789, :892-912)."""
+
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+from .nn import Arch, n_params
+from .records import FVLevel
+
+
+class StepWorkspace:
+    """Scratch memory for one batch size and job bound (caller-owned, library-carved)."""
+
+    def __init__(self, arch: Arch, batch: int, max_jobs: int, device="cuda"):
+        lib = _lib.load()
+        nbytes = int(lib.dips_step_workspace_bytes(arch.ctype(), batch, max_jobs))
+        if nbytes == 0:
+            raise ValueError("invalid workspace request")
+        self.arch, self.batch, self.max_jobs, self.nbytes = arch, batch, max_jobs, nbytes
+        self.buf = torch.empty(nbytes, dtype=torch.uint8, device=device)
+
+    def fits(self, arch, batch, max_jobs):
+        return arch == self.arch and batch == self.batch and max_jobs <= self.max_jobs
+
+
+def _ids_ptr(batch_ids):
+    return _lib.ptr(batch_ids) if batch_ids is not None else _lib.c_void_p(0)
+
+
+def residual_forward(arch: Arch, params: torch.Tensor, level: FVLevel, batch_ids=None, ws: StepWorkspace = None,
+                     want_residual=False):
+    """Loss (device float64 scalar) and optionally the per-point residuals of a batch."""
+    lib = _lib.load()
+    B = level.n if batch_ids is None else int(batch_ids.numel())
+    if ws is None or not ws.fits(arch, B, level.max_jobs(B)):
+        ws = StepWorkspace(arch, B, level.max_jobs(B), params.device)
+    loss = torch.empty((), dtype=torch.float64, device=params.device)
+    res = torch.empty(B, dtype=torch.float32, device=params.device) if want_residual else None
+    _lib.check(lib.dips_residual_fwd(arch.ctype(), _lib.ptr(params), level.desc, _ids_ptr(batch_ids), B,
+                                     _lib.ptr(ws.buf), ws.nbytes, _lib.ptr(loss), _lib.ptr(res),
+                                     _lib.stream_handle()), "dips_residual_fwd")
+    return loss, res, ws
+
+
+def residual_backward(arch: Arch, params: torch.Tensor, level: FVLevel, batch_ids, ws: StepWorkspace):
+    lib = _lib.load()
+    B = level.n if batch_ids is None else int(batch_ids.numel())
+    grad = torch.empty(n_params(arch), dtype=torch.float32, device=params.device)
+    _lib.check(lib.dips_residual_bwd(arch.ctype(), _lib.ptr(params), level.desc, _ids_ptr(batch_ids), B,
+                                     _lib.ptr(ws.buf), ws.nbytes, _lib.ptr(grad), _lib.stream_handle()),
+               "dips_residual_bwd")
+    return grad
+
+
+class ResidualLoss(torch.autograd.Function):
+    """loss = mean(0.5 * (lhs/diag - rhs/diag)^2) over a batch, differentiable in params."""
+
+    @staticmethod
+    def forward(ctx, params, arch, level, batch_ids):
+        loss, _, ws = residual_forward(arch, params.detach().contiguous(), level, batch_ids)
+        ctx.arch, ctx.level, ctx.batch_ids, ctx.ws = arch, level, batch_ids, ws
+        ctx.save_for_backward(params)
+        return loss.to(torch.float32)
+
+    @staticmethod
+    def backward(ctx, g):
+        (params,) = ctx.saved_tensors
+        grad = residual_backward(ctx.arch, params.detach().contiguous(), ctx.level, ctx.batch_ids, ctx.ws)
+        return grad * g.to(grad.dtype), None, None, None
+
+
+def residual_loss(params, arch: Arch, level: FVLevel, batch_ids=None):
+    return ResidualLoss.apply(params, arch, level, batch_ids)
+
+
+class AdamState:
+    """clip_by_global_norm -> scale_by_adam -> scale_by_schedule(exponential_decay) -> scale(-1)
+    (solvers/optimizers.py:33-54); moments and step count live on the device."""
+
+    def __init__(self, n: int, lr=1e-3, decay_rate=0.9, transition_steps=1000, max_norm=1.0,
+                 b1=0.9, b2=0.999, eps=1e-8, device="cuda"):
+        self.mu = torch.zeros(n, dtype=torch.float32, device=device)
+        self.nu = torch.zeros(n, dtype=torch.float32, device=device)
+        self.count = torch.zeros(1, dtype=torch.int64, device=device)
+        self.hp = _lib.AdamT(lr, decay_rate, float(transition_steps), max_norm, b1, b2, eps)
+
+    def step(self, arch: Arch, params: torch.Tensor, grad: torch.Tensor):
+        lib = _lib.load()
+        _lib.check(lib.dips_adam_step(arch.ctype(), self.hp, _lib.ptr(params), _lib.ptr(grad), _lib.ptr(self.mu),
+                                      _lib.ptr(self.nu), _lib.ptr(self.count), _lib.stream_handle()),
+                   "dips_adam_step")
+
+
+def train_step(arch: Arch, params: torch.Tensor, opt: AdamState, level: FVLevel, batch_ids, ws: StepWorkspace,
+               loss_out: torch.Tensor, grad_out=None):
+    """One fused step: residual forward, adjoint, gradient reduction and Adam (params in place)."""
+    lib = _lib.load()
+    B = level.n if batch_ids is None else int(batch_ids.numel())
+    _lib.check(lib.dips_train_step(arch.ctype(), opt.hp, _lib.ptr(params), _lib.ptr(opt.mu), _lib.ptr(opt.nu),
+                                   _lib.ptr(opt.count), level.desc, _ids_ptr(batch_ids), B, _lib.ptr(ws.buf),
+                                   ws.nbytes, _lib.ptr(loss_out), _lib.ptr(grad_out), _lib.stream_handle()),
+               "dips_train_step")
+
+
+def batch_ids(n: int, batch: int, epoch: int, batch_index: int, seed: int = 0, out=None, device="cuda"):
+    """Ids of minibatch ``batch_index`` of ``epoch``: a seeded permutation of 0..n-1."""
+    lib = _lib.load()
+    out = out if out is not None else torch.empty(batch, dtype=torch.int32, device=device)
+    _lib.check(lib.dips_batch_ids(n, epoch, seed, batch_index, batch, _lib.ptr(out), _lib.stream_handle()),
+               "dips_batch_ids")
+    return out

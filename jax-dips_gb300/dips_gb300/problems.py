@@ -1,0 +1,291 @@
+"""Manufactured interface problems used by the tests and the benchmark.
+
+Each problem is a dict of coefficient callables in the shape the reference's
+``trainer.setup`` takes (solvers/poisson/trainer.py:980-994), except that a
+callable receives a whole coordinate array ``r`` of shape (3, M) -- a numpy
+array or a torch tensor -- and returns shape (M,).  ``x, y, z = r`` and
+``r[0]`` work as in the reference's per-point callables
+(tests/confs/experiment_configs.py).
+
+Sign conventions follow the reference's FV residual
+(solvers/poisson/discretization.py:403-408): the PDE is
+``-div(mu grad u) + k u = f`` and the flux jump enters the right-hand side as
+``+ int_Gamma beta dA`` with ``beta = -(mu+ d_n u+ - mu- d_n u-)``, n the unit
+normal pointing from Omega^- (phi < 0) into Omega^+ (see
+tests/confs/experiment_configs.py:84-96).  ``alpha = u+ - u-``.
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+try:  # torch is optional for the numpy-only users of this module
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+
+# ----------------------------------------------------------------------------------------
+# array-namespace helpers: the same callable runs on numpy (CPU) or torch (GPU) arrays
+# ----------------------------------------------------------------------------------------
+def _is_torch(a):
+    return torch is not None and isinstance(a, torch.Tensor)
+
+
+class _NS:
+    def __init__(self, like):
+        self.t = _is_torch(like)
+        self.like = like
+
+    def __getattr__(self, name):
+        mod = torch if self.t else np
+        alias = {"arccos": "acos", "arctan2": "atan2"} if self.t else {}
+        return getattr(mod, alias.get(name, name))
+
+    def full(self, value):
+        if self.t:
+            return torch.full_like(self.like, float(value))
+        return np.full_like(self.like, value)
+
+    def maximum(self, a, b):
+        if self.t:
+            return torch.clamp(a, min=b) if not _is_torch(b) else torch.maximum(a, b)
+        return np.maximum(a, b)
+
+    def safe_div(self, a, b):
+        """a / b with b == 0 replaced by 1 (so 0/0 -> 0)."""
+        if self.t:
+            return a / torch.where(b == 0, torch.ones_like(b), b)
+        return a / np.where(b == 0, np.ones_like(b), b)
+
+
+def _xyz(r):
+    return r[0], r[1], r[2], _NS(r[0])
+
+
+# ----------------------------------------------------------------------------------------
+# sphere (configs 1 and 2): phi = |x| - 0.5
+# ----------------------------------------------------------------------------------------
+def sphere_problem(mu_m=1.0, mu_p=10.0):
+    """Sphere interface, u- = sin x cos y e^z, u+ = x^2+y^2+z^2, mu-=1, mu+=10, k=0."""
+
+    def phi(r):
+        x, y, z, xp = _xyz(r)
+        return xp.sqrt(x * x + y * y + z * z) - 0.5
+
+    def u_m(r):
+        x, y, z, xp = _xyz(r)
+        return xp.sin(x) * xp.cos(y) * xp.exp(z)
+
+    def u_p(r):
+        x, y, z, xp = _xyz(r)
+        return x * x + y * y + z * z
+
+    def grad_u_m(r):
+        x, y, z, xp = _xyz(r)
+        e = xp.exp(z)
+        return (xp.cos(x) * xp.cos(y) * e, -xp.sin(x) * xp.sin(y) * e, xp.sin(x) * xp.cos(y) * e)
+
+    def normal(r):
+        x, y, z, xp = _xyz(r)
+        n = xp.sqrt(x * x + y * y + z * z)
+        return xp.safe_div(x, n), xp.safe_div(y, n), xp.safe_div(z, n)
+
+    def beta(r):
+        x, y, z, xp = _xyz(r)
+        nx, ny, nz = normal(r)
+        gm = grad_u_m(r)
+        dn_up = 2.0 * x * nx + 2.0 * y * ny + 2.0 * z * nz
+        dn_um = gm[0] * nx + gm[1] * ny + gm[2] * nz
+        return -(mu_p * dn_up - mu_m * dn_um)
+
+    def f_m(r):  # -mu- lap(u-) ; lap(sin x cos y e^z) = -sin x cos y e^z
+        return mu_m * u_m(r)
+
+    def f_p(r):
+        x, y, z, xp = _xyz(r)
+        return xp.full(-6.0 * mu_p)
+
+    return _assemble(phi, u_m, u_p, lambda r: _xyz(r)[3].full(mu_m), lambda r: _xyz(r)[3].full(mu_p),
+                     lambda r: _xyz(r)[3].full(0.0), lambda r: _xyz(r)[3].full(0.0), f_m, f_p, beta)
+
+
+# ----------------------------------------------------------------------------------------
+# star (config 3): phi = r - 0.5 - 0.15 sin(5 theta) cos(3 varphi)
+# ----------------------------------------------------------------------------------------
+def star_problem():
+    """Star interface, variable mu, k+ = 1; u- = exp(-|x|^2), u+ = cos(x+y+z)."""
+
+    def _angles(r):
+        x, y, z, xp = _xyz(r)
+        rr = xp.sqrt(x * x + y * y + z * z)
+        cz = xp.clip(xp.safe_div(z, rr), -1.0, 1.0)
+        theta = xp.arccos(cz)
+        vphi = xp.arctan2(y, x)
+        return rr, theta, vphi
+
+    def phi(r):
+        rr, th, vp = _angles(r)
+        xp = _xyz(r)[3]
+        return rr - 0.5 - 0.15 * xp.sin(5.0 * th) * xp.cos(3.0 * vp)
+
+    def grad_phi(r):
+        x, y, z, xp = _xyz(r)
+        rr, th, vp = _angles(r)
+        rho2 = x * x + y * y
+        rho = xp.sqrt(rho2)
+        r2 = rr * rr
+        A = -0.15 * 5.0 * xp.cos(5.0 * th) * xp.cos(3.0 * vp)  # d phi / d theta
+        B = 0.15 * 3.0 * xp.sin(5.0 * th) * xp.sin(3.0 * vp)  # d phi / d varphi
+        dth_dx = xp.safe_div(x * z, r2 * rho)
+        dth_dy = xp.safe_div(y * z, r2 * rho)
+        dth_dz = xp.safe_div(-rho, r2)
+        dvp_dx = xp.safe_div(-y, rho2)
+        dvp_dy = xp.safe_div(x, rho2)
+        gx = xp.safe_div(x, rr) + A * dth_dx + B * dvp_dx
+        gy = xp.safe_div(y, rr) + A * dth_dy + B * dvp_dy
+        gz = xp.safe_div(z, rr) + A * dth_dz
+        return gx, gy, gz
+
+    def mu_m(r):
+        x, y, z, xp = _xyz(r)
+        return 1.0 + 0.5 * xp.sin(x * y)
+
+    def mu_p(r):
+        x, y, z, xp = _xyz(r)
+        return 20.0 + 5.0 * xp.cos(z)
+
+    def u_m(r):
+        x, y, z, xp = _xyz(r)
+        return xp.exp(-(x * x + y * y + z * z))
+
+    def u_p(r):
+        x, y, z, xp = _xyz(r)
+        return xp.cos(x + y + z)
+
+    def f_m(r):
+        x, y, z, xp = _xyz(r)
+        rr2 = x * x + y * y + z * z
+        e = xp.exp(-rr2)
+        return 2.0 * x * y * xp.cos(x * y) * e - (1.0 + 0.5 * xp.sin(x * y)) * (4.0 * rr2 - 6.0) * e
+
+    def f_p(r):
+        x, y, z, xp = _xyz(r)
+        s = x + y + z
+        return -5.0 * xp.sin(z) * xp.sin(s) + 3.0 * (20.0 + 5.0 * xp.cos(z)) * xp.cos(s) + xp.cos(s)
+
+    def beta(r):
+        x, y, z, xp = _xyz(r)
+        gx, gy, gz = grad_phi(r)
+        gn = xp.sqrt(gx * gx + gy * gy + gz * gz)
+        nx, ny, nz = xp.safe_div(gx, gn), xp.safe_div(gy, gn), xp.safe_div(gz, gn)
+        e = xp.exp(-(x * x + y * y + z * z))
+        gum = (-2.0 * x * e, -2.0 * y * e, -2.0 * z * e)
+        sn = -xp.sin(x + y + z)
+        dn_up = sn * (nx + ny + nz)
+        dn_um = gum[0] * nx + gum[1] * ny + gum[2] * nz
+        return -(mu_p(r) * dn_up - mu_m(r) * dn_um)
+
+    return _assemble(phi, u_m, u_p, mu_m, mu_p, lambda r: _xyz(r)[3].full(0.0),
+                     lambda r: _xyz(r)[3].full(1.0), f_m, f_p, beta)
+
+
+def _assemble(phi, u_m, u_p, mu_m, mu_p, k_m, k_p, f_m, f_p, beta):
+    def alpha(r):
+        return u_p(r) - u_m(r)
+
+    def exact(r):
+        x, y, z, xp = _xyz(r)
+        return xp.where(phi(r) >= 0, u_p(r), u_m(r))
+
+    return {
+        "phi": phi,
+        "mu_m": mu_m,
+        "mu_p": mu_p,
+        "k_m": k_m,
+        "k_p": k_p,
+        "f_m": f_m,
+        "f_p": f_p,
+        "alpha": alpha,
+        "beta": beta,
+        "g": u_p,
+        "u_m": u_m,
+        "u_p": u_p,
+        "exact": exact,
+    }
+
+
+# ----------------------------------------------------------------------------------------
+# linearised Poisson-Boltzmann instances (config 4)
+# ----------------------------------------------------------------------------------------
+def lpbe_problem(centres, radii, charges, sigma=0.02, mu_m=1.0, mu_p=80.0, k_p=0.1):
+    """phi = min_i(|x - c_i| - r_i); f- = sum_i q_i N(c_i, sigma); zero Dirichlet BC, no jumps.
+
+    The form follows examples/benchmark_LPBE/geometry.py:20-37 and coefficients.py:266-291.
+    """
+    C = np.asarray(centres, np.float32)
+    R = np.asarray(radii, np.float32)
+    Q = np.asarray(charges, np.float32)
+    norm = 1.0 / ((2.0 * math.pi) ** 1.5 * sigma ** 3)
+
+    def _cols(r):
+        if _is_torch(r):
+            dev = r.device
+            return (torch.as_tensor(C, device=dev), torch.as_tensor(R, device=dev), torch.as_tensor(Q, device=dev))
+        return C, R, Q
+
+    def phi(r):
+        c, rad, _ = _cols(r)
+        xp = _NS(r[0])
+        out = None
+        for i in range(c.shape[0]):
+            d = xp.sqrt((r[0] - c[i, 0]) ** 2 + (r[1] - c[i, 1]) ** 2 + (r[2] - c[i, 2]) ** 2) - rad[i]
+            out = d if out is None else xp.minimum(out, d)
+        return out
+
+    def f_m(r):
+        c, _, q = _cols(r)
+        xp = _NS(r[0])
+        out = xp.full(0.0)
+        for i in range(c.shape[0]):
+            if float(q[i]) == 0.0:
+                continue
+            d2 = (r[0] - c[i, 0]) ** 2 + (r[1] - c[i, 1]) ** 2 + (r[2] - c[i, 2]) ** 2
+            out = out + q[i] * norm * xp.exp(-d2 / (2.0 * sigma * sigma))
+        return out
+
+    zero = lambda r: _NS(r[0]).full(0.0)  # noqa: E731
+    return {
+        "phi": phi,
+        "mu_m": lambda r: _NS(r[0]).full(mu_m),
+        "mu_p": lambda r: _NS(r[0]).full(mu_p),
+        "k_m": zero,
+        "k_p": lambda r: _NS(r[0]).full(k_p),
+        "f_m": f_m,
+        "f_p": zero,
+        "alpha": zero,
+        "beta": zero,
+        "g": zero,
+    }
+
+
+def lpbe_instances(n_instances=64, seed=0):
+    """Seeded synthetic stand-ins for the 64 uneven LPBE instances (sides 48..160 step 16)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    sides = np.arange(48, 161, 16)
+    for _ in range(n_instances):
+        side = int(rng.choice(sides))
+        ns = int(rng.integers(50, 2001))
+        c = rng.uniform(-0.6, 0.6, (ns, 3)).astype(np.float32)
+        r = rng.uniform(0.05, 0.12, ns).astype(np.float32)
+        q = rng.integers(-1, 2, ns).astype(np.float32)
+        out.append((side, c, r, q))
+    return out
+
+
+def exact_solution(prob, pts):
+    """u_exact at points (N,3) (numpy)."""
+    return np.asarray(prob["exact"](np.asarray(pts, np.float32).T), np.float32)

@@ -1,0 +1,143 @@
+"""Per-point residual records of one stencil spacing (one "level").
+
+The reference recomputes the whole parameter-independent part of the residual --
+cell decomposition, face areas, interface quadrature, regression extrapolation --
+for every point at every step (solvers/poisson/discretization.py:299-519).  Here it
+is computed once per (point, h) by three HBM-streaming kernels:
+
+1. ``dips_geometry_classify``  flags and counts per point
+2. ``dips_geometry_queries``   the points where coefficient callables are needed
+   (interface-triangle vertices, crossed stencil points, their projections r = s - phi n)
+3. the host evaluates the user's coefficient callables at those points (torch, on the GPU)
+4. ``dips_geometry_assemble``  the residual of each point as an affine function of the
+   network values at its jobs: r = nan_to_num((lhs0 + sum_j A_j u(x_j)) / diag) - rod
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from .levelset import LevelSetGrid
+
+F32 = np.float32
+
+
+def eval_callable(fn, pts: torch.Tensor) -> torch.Tensor:
+    """Evaluate a coefficient callable on points (M, 3); the callable sees r of shape (3, M)."""
+    M = pts.shape[0]
+    if M == 0:
+        return torch.empty(0, dtype=torch.float32, device=pts.device)
+    v = fn(pts.T)
+    v = torch.as_tensor(v, dtype=torch.float32, device=pts.device)
+    return torch.broadcast_to(v, (M,)).contiguous()
+
+
+def _excl_scan(counts: torch.Tensor) -> torch.Tensor:
+    c = counts.to(torch.int64)
+    out = torch.zeros(c.numel() + 1, dtype=torch.int64, device=c.device)
+    torch.cumsum(c, 0, out=out[1:])
+    return out
+
+
+class FVLevel:
+    """Residual records of the points ``pts`` at stencil spacing ``h`` (device tensors)."""
+
+    def __init__(self, ls: LevelSetGrid, coeff_fns: dict, pts: torch.Tensor, h, keep_geometry=False):
+        lib = _lib.load()
+        dev = pts.device
+        self.ls = ls
+        self.pts = pts.to(torch.float32).contiguous()
+        n = self.pts.shape[0]
+        self.n = n
+        self.h = np.asarray(h, F32).reshape(3)
+        hc = (_lib.c_f32 * 3)(*[float(v) for v in self.h])
+        st = _lib.stream_handle()
+        i32 = dict(dtype=torch.int32, device=dev)
+        flags = torch.empty(n, **i32)
+        n_tri = torch.empty(n, **i32)
+        n_xs = torch.empty(n, **i32)
+        cap = torch.empty(n, **i32)
+        P = _lib.ptr
+        _lib.check(
+            lib.dips_geometry_classify(ls.desc, P(self.pts), n, hc, P(flags), P(n_tri), P(n_xs), P(cap), st),
+            "dips_geometry_classify",
+        )
+        tri_off = _excl_scan(n_tri)
+        xs_off = _excl_scan(n_xs)
+        self.job_off = _excl_scan(cap)
+        n_tri_tot = int(tri_off[-1])
+        n_xs_tot = int(xs_off[-1])
+        self.n_jobs_cap = int(self.job_off[-1])
+        f32 = dict(dtype=torch.float32, device=dev)
+        tri_pts = torch.empty(max(3 * n_tri_tot, 1), 3, **f32)
+        xs_pts = torch.empty(max(n_xs_tot, 1), 3, **f32)
+        xr_pts = torch.empty(max(n_xs_tot, 1), 3, **f32)
+        _lib.check(
+            lib.dips_geometry_queries(ls.desc, P(self.pts), n, hc, P(flags), P(tri_off), P(xs_off), P(tri_pts),
+                                      P(xs_pts), P(xr_pts), st),
+            "dips_geometry_queries",
+        )
+        tri_pts = tri_pts[: 3 * n_tri_tot]
+        xs_pts = xs_pts[:n_xs_tot]
+        xr_pts = xr_pts[:n_xs_tot]
+
+        # ---- coefficient callables (reference semantics: evaluated at exactly these points)
+        fn = coeff_fns
+        half = torch.tensor(0.5, dtype=torch.float32, device=dev)
+        hv = torch.as_tensor(self.h, device=dev)
+        offs = torch.zeros(6, 3, **f32)
+        for a in range(3):
+            offs[2 * a, a] = -hv[a]
+            offs[2 * a + 1, a] = hv[a]
+        offs = half * offs
+        faces = (self.pts[:, None, :] + offs[None]).reshape(-1, 3)
+        vals = {}
+        vals["mu_m_face"] = eval_callable(fn["mu_m"], faces)
+        vals["mu_p_face"] = eval_callable(fn["mu_p"], faces)
+        del faces
+        for name in ("k_m", "k_p", "f_m", "f_p", "g"):
+            vals[name] = eval_callable(fn[name], self.pts)
+        vals["beta_tri"] = eval_callable(fn["beta"], tri_pts)
+        vals["mu_m_s"] = eval_callable(fn["mu_m"], xs_pts)
+        vals["mu_p_s"] = eval_callable(fn["mu_p"], xs_pts)
+        vals["alpha_r"] = eval_callable(fn["alpha"], xr_pts)
+        vals["beta_r"] = eval_callable(fn["beta"], xr_pts)
+        vals["mu_m_r"] = eval_callable(fn["mu_m"], xr_pts)
+        vals["mu_p_r"] = eval_callable(fn["mu_p"], xr_pts)
+        beta0 = float(eval_callable(fn["beta"], torch.zeros(1, 3, **f32))[0])
+        for k, v in vals.items():
+            if v.numel() == 0:
+                vals[k] = torch.zeros(1, **f32)
+        co = _lib.CoeffsT(*[P(vals[k]) for k, _ in _lib.CoeffsT._fields_[:-1]], beta0)
+
+        self.lhs0 = torch.empty(n, **f32)
+        self.diag = torch.empty(n, **f32)
+        self.rod = torch.empty(n, **f32)
+        self.cnt = torch.empty(n, **i32)
+        self.cnt_m = torch.empty(n, **i32)
+        self.job_code = torch.empty(max(self.n_jobs_cap, 1), dtype=torch.int16, device=dev)
+        self.job_A = torch.zeros(max(self.n_jobs_cap, 1), **f32)
+        self.coeff26 = torch.empty(n, 26, **f32) if keep_geometry else None
+        self.beta_int = torch.empty(n, **f32) if keep_geometry else None
+        _lib.check(
+            lib.dips_geometry_assemble(ls.desc, P(self.pts), n, hc, P(flags), P(tri_off), P(xs_off), P(self.job_off),
+                                       co, P(self.lhs0), P(self.diag), P(self.rod), P(self.cnt), P(self.cnt_m),
+                                       P(self.job_code), P(self.job_A), P(self.coeff26), P(self.beta_int), st),
+            "dips_geometry_assemble",
+        )
+        self.flags = flags if keep_geometry else None
+        self.n_tri, self.n_xs = (n_tri, n_xs) if keep_geometry else (None, None)
+        self._vals = vals if keep_geometry else None
+        self.n_jobs = int(self.cnt.sum())
+        self.max_cnt = int(self.cnt.max()) if n else 0
+        self.desc = _lib.RecordsT(
+            P(self.pts), n, (_lib.c_f32 * 3)(*[float(v) for v in self.h]), P(self.lhs0), P(self.diag), P(self.rod),
+            P(self.cnt), P(self.cnt_m), P(self.job_off), P(self.job_code), P(self.job_A),
+        )
+
+    def max_jobs(self, batch: int, distinct: bool = True) -> int:
+        """Upper bound of the jobs of a batch of ``batch`` points (distinct points: <= all jobs)."""
+        bound = batch * self.max_cnt
+        return min(bound, self.n_jobs) if distinct else bound

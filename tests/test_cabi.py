@@ -1,0 +1,64 @@
+"""The C ABI library builds for sm_103a, loads on a host without a GPU, and exports every
+entry point include/dips.h declares (no compute calls here)."""
+
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for fname in os.listdir(os.path.join(ROOT, "include")):
+        if not fname.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", fname)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*[A-Za-z_][\w\s\*]*?\b(dips_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for required in ("dips_last_error", "dips_phi_trilinear", "dips_geometry_assemble", "dips_residual_fwd",
+                     "dips_residual_bwd", "dips_train_step", "dips_adam_step"):
+        assert required in names
+
+
+def test_library_loads_and_exports_all_declared_symbols():
+    from dips_gb300 import _lib
+
+    lib = _lib.load()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, f"symbols declared in include/ but not exported: {missing}"
+    assert lib.dips_version().startswith(b"dips_gb300")
+
+
+def test_arch_table_and_workspace_query():
+    from dips_gb300 import _lib
+    from dips_gb300.nn import Arch, n_params
+
+    lib = _lib.load()
+    for a in (Arch(1, 1, 2, 10), Arch(3, 32, 3, 32), Arch(2, 16, 2, 16), Arch(2, 8, 2, 8)):
+        assert lib.dips_arch_supported(a.ctype()) == 1
+        assert lib.dips_num_params(a.ctype()) == n_params(a)
+    assert lib.dips_arch_supported(Arch(4, 64, 4, 64).ctype()) == 0
+    small = lib.dips_step_workspace_bytes(Arch().ctype(), 1000, 7000)
+    big = lib.dips_step_workspace_bytes(Arch().ctype(), 1000, 70000)
+    assert 0 < small < big
+
+
+def test_argument_errors_are_reported_without_a_gpu():
+    from dips_gb300 import _lib
+
+    lib = _lib.load()
+    # null pointers are rejected on the host before any CUDA call
+    st = lib.dips_phi_ghost_layer(None, 4, 4, 4, None, None)
+    assert st == 1
+    assert b"null" in lib.dips_last_error()
+    a = _lib.ArchT(5, 5, 5, 5)
+    st = lib.dips_mlp_eval(a, _lib.c_void_p(8), _lib.c_void_p(8), _lib.c_void_p(8), 4, _lib.c_void_p(8), None, None)
+    assert st == 4 and b"no kernel compiled" in lib.dips_last_error()
