@@ -571,8 +571,8 @@ __global__ void k_classify(LevelSet L0, const float* __restrict__ pts, int64_t n
       if (j == 0) f |= enc_crossed(c) << kFlagCrossedP;
       nx += (c == 0);
     }
-    int ntri = 0;
-    if (!bnd && dec_crossed(f, kFlagCrossedP) == 0) {
+    int ntri = 0;  // counted for box-boundary points too: assemble integrates beta on every crossed cell
+    if (dec_crossed(f, kFlagCrossedP) == 0) {
       Cell cell;
       cell_eval(L, p, h, cell);
       for (int t = 0; t < 5; ++t) {
@@ -597,7 +597,6 @@ __global__ void k_queries(LevelSet L0, const float* __restrict__ pts, int64_t n,
   const float* h = hh.v;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t f = flags[i];
-    if (f & 1u) continue;
     float p[3];
     load_point(pts, i, p);
     if (dec_crossed(f, kFlagCrossedP) == 0) {
@@ -612,6 +611,7 @@ __global__ void k_queries(LevelSet L0, const float* __restrict__ pts, int64_t n,
             for (int a = 0; a < 3; ++a) tri_pts[3 * o + a] = tri[q][v][a];
       }
     }
+    if (f & 1u) continue;  // box-boundary points have no stencil queries
     int64_t ox = xs_off[i];
     for (int j = 0; j < kStencil; ++j) {
       if (dec_crossed(f, kFlagCrossedS + 2 * j) != 0) continue;

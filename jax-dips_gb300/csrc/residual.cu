@@ -95,14 +95,16 @@ __device__ __forceinline__ void block_scan2(int64_t a, int64_t b, int64_t* ea, i
   __syncthreads();
 }
 
-__global__ void k_count(const int32_t* __restrict__ ids, int64_t B, const int32_t* __restrict__ cnt,
+__global__ void k_count(const int32_t* __restrict__ ids, int64_t B, int64_t n_pts, const int32_t* __restrict__ cnt,
                         const int32_t* __restrict__ cnt_m, Workspace w) {
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   int64_t a = 0, c = 0;
   if (b < B) {
     const int64_t pid = batch_pid(ids, b);
-    a = cnt_m[pid];
-    c = cnt[pid] - a;
+    if (pid >= 0 && pid < n_pts) {  // an out-of-range id gets no jobs and a NaN residual
+      a = cnt_m[pid];
+      c = cnt[pid] - a;
+    }
     w.cm[b] = (int32_t)a;
     w.cp[b] = (int32_t)c;
   }
@@ -163,6 +165,7 @@ __global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, dips_records_
   w.om[b] = om;
   w.op[b] = op;
   const int cm = w.cm[b], cp = w.cp[b];
+  if (cm == 0 && cp == 0) return;
   const int64_t src_m = rec.job_off[pid];
   const int64_t src_p = rec.job_off[pid + 1] - cp;
   for (int q = 0; q < cm; ++q) {
@@ -203,6 +206,11 @@ __global__ void k_residual(const int32_t* __restrict__ ids, int64_t B, dips_reco
   const bool overflow = w.ctl->overflow != 0;
   double l = 0.0;
   if (b < B && overflow) {
+    w.res[b] = nanf("");
+    w.gs[b] = 0.0f;
+    if (residual_out) residual_out[b] = nanf("");
+    l = nan("");
+  } else if (b < B && (batch_pid(ids, b) < 0 || batch_pid(ids, b) >= rec.n_pts)) {
     w.res[b] = nanf("");
     w.gs[b] = 0.0f;
     if (residual_out) residual_out[b] = nanf("");
@@ -395,7 +403,7 @@ static int run_forward(const ArchOps* ops, const float* params, const dips_recor
   int st = ops->load_params(params, s);
   if (st) return st;
   const int nblk = (int)W.nblk;
-  k_count<<<nblk, kScanBlock, 0, s>>>(ids, B, rec->cnt, rec->cnt_m, W);
+  k_count<<<nblk, kScanBlock, 0, s>>>(ids, B, rec->n_pts, rec->cnt, rec->cnt_m, W);
   k_scan_blocks<<<1, kScanBlock, 0, s>>>(W);
   k_emit<<<nblk, kScanBlock, 0, s>>>(ids, B, *rec, W);
   DIPS_CHECK_LAUNCH("job expansion");
