@@ -1,0 +1,455 @@
+#!/usr/bin/env python
+"""Benchmark of the NBM jump-condition FV residual path on GB300.
+
+Workload (one step): one NBM training step -- residual forward, adjoint to the network
+parameters, chained Adam -- over a minibatch of 2^18 points drawn uniformly (a seeded
+per-epoch permutation) from the 128^3 sphere problem (phi = |x| - 0.5, u- = sin x cos y e^z,
+u+ = |x|^2, mu- = 1, mu+ = 10), DoubleMLP 3x32 / 3x32 tanh, stencil spacing h = dx.
+
+Prints one JSON line.  `value` is residual points per second with the inputs resident in
+HBM (one CUDA graph per step); `e2e` is the same metric through the public Python API with
+the batch ids copied from pinned host memory and the loss read back every step.  The
+headline comparison of the metric -- time to a relative L-infinity error target at 128^3,
+fused NBM vs matrix-free BiCGSTAB on the same FV system -- is reported in `time_to_target`.
+
+`--impl reference` times the CPU restatement of the reference's algorithm (the oracle
+port: per-step geometry + residual + autograd gradient) on the host cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "jax-dips_gb300"))
+
+METRIC = "time to rel L-inf<=1e-2 at 128^3: fused NBM vs Krylov FD, 1 GB300; residual pts/s"
+UNIT = "residual_pts/s"
+ARCH = (3, 32, 3, 32)
+
+
+def net_flops(layers, width):
+    """Forward FLOPs of one network evaluation: sum of 2*in*out + out per layer + one per tanh."""
+    f = 2 * 3 * width + width
+    f += (layers - 1) * (2 * width * width + width)
+    f += 2 * width + 1
+    f += layers * width
+    return f
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--batch", type=int, default=1 << 18)
+    ap.add_argument("--tta-seconds", type=float, default=60.0, help="NBM time budget of the time-to-target run")
+    ap.add_argument("--no-tta", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=16384)
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------------------
+# clocks during the timed region
+# ----------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(index)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------------------
+# reference arm: the CPU restatement of the reference's per-step work
+# ----------------------------------------------------------------------------------------
+def cpu_oracle_rate(n, sample, steps, seed=0, arch=ARCH):
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import nbm_loss as L
+    import nbm_oracle as O
+    from dips_gb300 import mesh, problems
+
+    pr = problems.sphere_problem()
+    g = mesh.uniform_grid(n)
+    phi = O.perturb(np.asarray(pr["phi"](g.R.T), np.float32))
+    prob = L.Problem(phi, g.x, g.y, g.z, pr)
+    h = np.array([g.dx, g.dy, g.dz], np.float32)
+    a = L.Arch(*arch)
+    w = L.init_params(a, 0)
+    rng = np.random.default_rng(seed)
+    times = []
+    for _ in range(steps):
+        idx = rng.choice(g.R.shape[0], sample, replace=False)
+        t0 = time.perf_counter()
+        rg = L.ResidualGeometry(prob, g.R[idx], h)  # the reference recomputes this every step
+        L.loss_and_grad(w, a, rg, torch.float32)
+        times.append(time.perf_counter() - t0)
+    return sample * len(times) / sum(times), times, torch.get_num_threads()
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    steps = max(args.steps, 1)
+    sample = args.cpu_sample
+    # warm-up (imports, allocator)
+    cpu_oracle_rate(args.n, 256, max(min(args.warmup, 2), 1))
+    t0 = time.perf_counter()
+    rate, times, cores = cpu_oracle_rate(args.n, sample, steps)
+    wall = time.perf_counter() - t0
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": rate,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"sphere {args.n}^3, DoubleMLP 3x32/3x32 tanh, h=dx; each step a sample of "
+                               f"{sample} points (geometry + residual + gradient, recomputed per step as the "
+                               "reference does)", "global_batch": sample},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{steps} steps x {sample} points of the {args.n}^3 grid, {wall:.1f} s"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "JAX is not installable here; the timed CPU path is the numpy/torch restatement of the "
+                "reference's algorithm (oracle/), run on the host cores",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------------------
+# our arm
+# ----------------------------------------------------------------------------------------
+def run_ours(args, rank, world):
+    import torch
+
+    from dips_gb300 import _lib, krylov, levelset, mesh, nn, ops, problems
+    from dips_gb300.records import FVLevel
+
+    dev = f"cuda:{int(os.environ.get('LOCAL_RANK', 0))}"
+    torch.cuda.set_device(dev)
+    lib = _lib.load()
+    pr = problems.sphere_problem()
+    g = mesh.uniform_grid(args.n)
+    arch = nn.Arch(*ARCH)
+    P = nn.n_params(arch)
+
+    # ---- set-up: level set and residual records (timed, reported as set-up)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ls = levelset.LevelSetGrid.from_callable(g, lambda r: levelset.perturb(pr["phi"](r)), dev)
+    pts = torch.as_tensor(g.R, device=dev)
+    h = np.array([g.dx, g.dy, g.dz], np.float32)
+    lvl = FVLevel(ls, pr, pts, h)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+
+    B = min(args.batch, lvl.n)
+    nb = lvl.n // B
+    params = torch.as_tensor(nn.init_params(arch, 42), device=dev)
+    opt = ops.AdamState(P, lr=1e-3, decay_rate=0.9)
+    ws = ops.StepWorkspace(arch, B, lvl.max_jobs(B), dev)
+    ids = torch.empty(B, dtype=torch.int32, device=dev)
+    loss = torch.zeros((), dtype=torch.float64, device=dev)
+    grad = torch.empty(P, dtype=torch.float32, device=dev)
+
+    def step():
+        _lib.check(lib.dips_batch_ids_device(lvl.n, B, nb, 7 + rank, 1, _lib.ptr(opt.count), _lib.ptr(ids),
+                                             _lib.stream_handle()), "batch ids")
+        if world == 1:
+            ops.train_step(arch, params, opt, lvl, ids, ws, loss, grad)
+        else:  # data parallel: gradient all-reduce (the reference's psum, trainer.py:739-743)
+            l, _, _ = ops.residual_forward(arch, params, lvl, ids, ws)
+            gr = ops.residual_backward(arch, params, lvl, ids, ws)
+            torch.distributed.all_reduce(gr)
+            opt.step(arch, params, gr)
+            loss.copy_(l)
+
+    # warm-up, then capture one step in a CUDA graph
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    graph = None
+    if world == 1:
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            step()
+        run = graph.replay
+    else:
+        run = step
+    for _ in range(2):
+        run()
+    torch.cuda.synchronize()
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    wall0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.zero_()
+        starts[i].record()
+        run()
+        ends[i].record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    t_total = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([t_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_total = float(t)
+        torch.distributed.barrier()
+    value = B * world * args.steps / t_total
+
+    # ---- dominant kernel (adjoint) timed live with CUDA events on the launching stream
+    ids_m = ops.batch_ids(lvl.n, B, epoch=0, batch_index=0, seed=123)
+    cnt = lvl.cnt[ids_m.long()].long()
+    cntm = lvl.cnt_m[ids_m.long()].long()
+    jobs_m, jobs_p = int(cntm.sum()), int((cnt - cntm).sum())
+    fwd_flops = jobs_m * net_flops(ARCH[0], ARCH[1]) + jobs_p * net_flops(ARCH[2], ARCH[3])
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    t_fwd, t_adj = [], []
+    for _ in range(5):
+        flush.zero_()
+        ev[0].record()
+        l_, _, ws_ = ops.residual_forward(arch, params, lvl, ids_m, ws)
+        ev[1].record()
+        flush.zero_()
+        ev[2].record()
+        ops.residual_backward(arch, params, lvl, ids_m, ws)
+        ev[3].record()
+        torch.cuda.synchronize()
+        t_fwd.append(ev[0].elapsed_time(ev[1]) / 1e3)
+        t_adj.append(ev[2].elapsed_time(ev[3]) / 1e3)
+    t_adj_med = statistics.median(t_adj)
+    t_fwd_med = statistics.median(t_fwd)
+    # FP32 FMA peak of this GPU (measured)
+    probe = torch.empty(152 * 16 * 256, dtype=torch.float32, device=dev)
+    iters = 4096
+    _lib.check(lib.dips_fp32_fma_probe(_lib.ptr(probe), 152 * 16, iters, _lib.stream_handle()), "probe")
+    pe0, pe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pe0.record()
+    _lib.check(lib.dips_fp32_fma_probe(_lib.ptr(probe), 152 * 16, iters, _lib.stream_handle()), "probe")
+    pe1.record()
+    torch.cuda.synchronize()
+    fp32_peak = 152 * 16 * 256 * 8 * 16 * iters * 2 / (pe0.elapsed_time(pe1) / 1e3) / 1e12
+    adj_tflops = 2 * fwd_flops / t_adj_med / 1e12
+    step_tflops = 3 * fwd_flops / (t_total / args.steps) / 1e12 * (1 if world == 1 else 1)
+
+    # ---- e2e through the public API with host buffers
+    host_ids = torch.empty(B, dtype=torch.int32).pin_memory()
+    host_loss = torch.empty((), dtype=torch.float64).pin_memory()
+    perm = np.random.default_rng(5).permutation(lvl.n)[: B * 4].astype(np.int32).reshape(4, B)
+    e2e_steps = max(args.steps // 2, 5)
+    torch.cuda.synchronize()
+    te0 = time.perf_counter()
+    for i in range(e2e_steps):
+        host_ids.numpy()[:] = perm[i % 4]
+        ids.copy_(host_ids, non_blocking=True)
+        ops.train_step(arch, params, opt, lvl, ids, ws, loss, None)
+        host_loss.copy_(loss, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        _ = float(host_loss)
+    te = time.perf_counter() - te0
+    e2e = {"value": B * e2e_steps / te, "unit": UNIT, "h2d_bytes_per_step": 4 * B, "d2h_bytes_per_step": 8,
+           "api": "dips_gb300.ops.train_step (dips_train_step) per step, ids H2D from pinned memory, loss D2H"}
+
+    # ---- time to target: BiCGSTAB vs NBM on the same level-0 FV system
+    tta = None
+    if not args.no_tta and rank == 0:
+        tta = time_to_target(args, lvl, g, pr, arch, dev)
+
+    # ---- CPU baseline (oracle port, bounded sample)
+    cpu = None
+    if rank == 0:
+        rate, times, cores = cpu_oracle_rate(args.n, args.cpu_sample, 3)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"3 steps x {args.cpu_sample} points of the {args.n}^3 grid (geometry + residual + "
+                         f"gradient per step), {sum(times):.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_total / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"NBM training step, sphere {args.n}^3 (phi grid {args.n}^3), DoubleMLP "
+                                   "3x32/3x32 tanh, h=dx, minibatch drawn uniformly",
+                       "global_batch": B * world, "points": int(lvl.n), "jobs_per_step": jobs_m + jobs_p,
+                       "l2": "flushed (256 MB write) between timed steps", "cuda_graph": world == 1,
+                       "setup_s": setup_s, "wall_s_timed": wall},
+            "roofline": {"bound": "fp32", "kernel": "k_job_adjoint (recompute + backpropagation + dW)",
+                         "achieved": adj_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": adj_tflops / fp32_peak, "traffic": None,
+                         "algorithmic": "2 x forward FLOPs per job (sum 2*in*out+out per layer + tanh count)",
+                         "peak_source": "measured FFMA probe (dips_fp32_fma_probe), not in MEASURED_PEAKS.json",
+                         "adjoint_ms": 1e3 * t_adj_med, "forward_ms": 1e3 * t_fwd_med,
+                         "step_tflops": step_tflops, "step_frac": step_tflops / fp32_peak},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": 10 * args.steps,
+            "clocks": clk,
+            "time_to_target": tta,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def time_to_target(args, lvl, g, pr, arch, dev):
+    import torch
+
+    from dips_gb300 import _lib, krylov, nn, ops, problems
+
+    lib = _lib.load()
+    shape = (g.x.shape[0], g.y.shape[0], g.z.shape[0])
+    ex = torch.as_tensor(problems.exact_solution(pr, g.R), device=dev)
+    # discretisation floor: the converged discrete solution's error against the exact solution
+    res = krylov.bicgstab(lvl, shape, u_exact=ex, max_iter=3000, rtol=1e-6, check_every=25)
+    floor = res.rel_linf
+    target = max(1e-2, 1.1 * floor)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    kr = krylov.bicgstab(lvl, shape, u_exact=ex, max_iter=3000, rtol=1e-9, check_every=5, target_rel_linf=target)
+    torch.cuda.synchronize()
+    t_kr = time.perf_counter() - t0
+    # NBM: graph-captured steps, error checked every epoch (checks excluded from the time)
+    B = min(args.batch, lvl.n)
+    nb = lvl.n // B
+    P = nn.n_params(arch)
+    params = torch.as_tensor(nn.init_params(arch, 42), device=dev)
+    opt = ops.AdamState(P, lr=1e-3, decay_rate=0.9)
+    ws = ops.StepWorkspace(arch, B, lvl.max_jobs(B), dev)
+    ids = torch.empty(B, dtype=torch.int32, device=dev)
+    loss = torch.zeros((), dtype=torch.float64, device=dev)
+
+    def step():
+        _lib.check(lib.dips_batch_ids_device(lvl.n, B, nb, 11, 1, _lib.ptr(opt.count), _lib.ptr(ids),
+                                             _lib.stream_handle()), "batch ids")
+        ops.train_step(arch, params, opt, lvl, ids, ws, loss)
+
+    p0 = params.clone()
+    step()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        step()
+    params.copy_(p0)
+    opt.mu.zero_()
+    opt.nu.zero_()
+    opt.count.zero_()
+    R = lvl.pts
+    phi = lvl.ls(R)
+    exmax = float(ex.abs().max())
+    t_train, steps, best, reached = 0.0, 0, float("inf"), None
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    while t_train < args.tta_seconds:
+        e0.record()
+        for _ in range(nb):
+            graph.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        t_train += e0.elapsed_time(e1) / 1e3
+        steps += nb
+        u = nn.mlp_eval(arch, params, R, phi)
+        err = float((u - ex).abs().max()) / exmax
+        best = min(best, err)
+        if err <= target:
+            reached = t_train
+            break
+    return {"target_rel_linf": target, "floor_rel_linf": floor,
+            "note": "target = max(1e-2, 1.1 x the converged discrete solution's error): 1e-2 against the exact "
+                    "solution is below this discretisation's error at this grid",
+            "krylov_s": t_kr, "krylov_iterations": kr.iterations, "krylov_rel_linf": kr.rel_linf,
+            "krylov_reached": kr.target_iteration >= 0,
+            "nbm_s": reached, "nbm_steps": steps, "nbm_best_rel_linf": best, "nbm_budget_s": args.tta_seconds,
+            "nbm_reached": reached is not None}
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        if args.impl != "reference":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group(backend)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

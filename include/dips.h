@@ -80,8 +80,9 @@ typedef struct {
   const float* diag;        /* [n] diagonal coefficient (discretization.py:381-386) */
   const float* rod;         /* [n] nan_to_num(rhs / diag) */
   const int32_t* cnt;       /* [n] jobs of the point */
-  const int32_t* cnt_m;     /* [n] of which u- network jobs (stored first) */
-  const int64_t* job_off;   /* [n] first job of the point */
+  const int32_t* cnt_m;     /* [n] of which u- network jobs */
+  const int64_t* job_off;   /* [n+1] the jobs of point i live in [job_off[i], job_off[i+1]):
+                               its cnt_m u- jobs at the start, its cnt - cnt_m u+ jobs at the end */
   const uint16_t* job_code; /* [jobs] */
   const float* job_A;       /* [jobs] lhs coefficient of the network value at the job point */
 } dips_records_t;
@@ -101,6 +102,11 @@ typedef struct {
 const char* dips_last_error(void);
 /* Library version string (host). */
 const char* dips_version(void);
+
+/* FP32 FMA throughput probe (the roofline denominator of the FP32-pipe kernels; no
+   counterpart in the reference): `blocks` blocks of 256 threads, each thread 8 independent
+   chains of 16*iters FMAs (2 FLOP each); out: [blocks*256]. */
+int dips_fp32_fma_probe(float* out, int32_t blocks, int32_t iters, cudaStream_t stream);
 
 /* ---- level set: replaces domain/interpolate.py:762-816 and :906-1021 ------------------ */
 /* Ghost layer of linear extrapolation around the [nx][ny][nz] samples. */
@@ -125,8 +131,9 @@ int dips_geometry_classify(const dips_levelset_t* ls, const float* pts, int64_t 
 int dips_geometry_queries(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
                           const uint32_t* flags, const int64_t* tri_off, const int64_t* xs_off,
                           float* tri_pts, float* xs_pts, float* xr_pts, cudaStream_t stream);
-/* Pass 3: the per-point residual records.  Jobs of point i are written at job_off[i]
-   (a prefix sum of job_cap); cnt[i] <= job_cap[i] are used, u- jobs first.  coeff26
+/* Pass 3: the per-point residual records.  job_off ([n+1]) is the exclusive prefix sum of
+   job_cap; cnt[i] <= job_cap[i] jobs are written (u- jobs from the front of the point's
+   range, u+ jobs from its back).  coeff26
    ([n][26], may be NULL) receives compute_face_centroids_values_plus_minus_at_point and
    beta_int ([n], may be NULL) the interface integral of beta. */
 int dips_geometry_assemble(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
@@ -167,12 +174,44 @@ int dips_train_step(const dips_arch_t* arch, const dips_adam_t* hp, float* param
 int dips_batch_ids(int64_t n, int64_t epoch_index, uint64_t seed, int64_t batch_index, int64_t batch,
                    int32_t* ids, cudaStream_t stream);
 
+/* Graph-replay form of dips_batch_ids: the step index is read from the device
+   (step_counter, e.g. the Adam step count), batch = step % n_batches and
+   epoch = step / n_batches.  mode 0 writes consecutive ranges batch*B + [0, B) (the
+   reference's fixed sequential batches, data/data_management.py:104-159); mode 1 the
+   seeded per-epoch permutation of dips_batch_ids. */
+int dips_batch_ids_device(int64_t n, int64_t batch, int64_t n_batches, uint64_t seed, int32_t mode,
+                          const int64_t* step_counter, int32_t* ids, cudaStream_t stream);
+
 /* ---- network evaluation: replaces Trainer.evaluate_solution_fn (trainer.py:836-844)
         and compute_gradient_solution_neural_network (:953-957) --------------------------- */
 /* u and grad u (grad_out [n][3], may be NULL) at n points; the network is chosen by
    phi_at (phi >= 0 -> u+). */
 int dips_mlp_eval(const dips_arch_t* arch, const float* params, const float* pts, const float* phi_at,
                   int64_t n, float* u_out, float* grad_out, cudaStream_t stream);
+
+/* ---- plain method: the FV system of a nodal vector (replaces Trainer.residual_vector,
+        trainer.py:883-890, over compute_Ax_and_b_discrete_fn, discretization.py:522-741)
+        and a matrix-free BiCGSTAB on it ---------------------------------------------- */
+typedef struct {
+  int32_t iterations;       /* BiCGSTAB iterations run */
+  int32_t target_iteration; /* first checked iteration with rel_linf <= target, -1 if never */
+  int32_t breakdown;        /* 1 if a recurrence scalar became 0 or non-finite */
+  double rel_residual;      /* ||b - K x|| / ||b|| at the last check */
+  float rel_linf;           /* max|x - u_exact| / max|u_exact| (-1 without u_exact) */
+} dips_krylov_stats_t;
+
+/* Residual of a nodal vector u on the grid whose nodes (C order, nx*ny*nz == n_pts) are the
+   records' points: out = K u - b, or K u when linear_only is nonzero. */
+int dips_fv_residual(const dips_records_t* rec, int32_t nx, int32_t ny, int32_t nz, const float* u,
+                     int32_t linear_only, float* out, cudaStream_t stream);
+size_t dips_bicgstab_workspace_bytes(int64_t n);
+/* Solve K x = b from the initial x (in place).  Every check_every iterations the host reads
+   the residual norm (and, with u_exact, the relative max error); the solve stops at
+   ||r||/||b|| <= rtol, at max_iter, or -- with u_exact and target_rel_linf > 0 -- as soon as
+   the relative max error reaches the target.  stats: host pointer, may be NULL. */
+int dips_bicgstab(const dips_records_t* rec, int32_t nx, int32_t ny, int32_t nz, float* x, const float* u_exact,
+                  int32_t max_iter, double rtol, int32_t check_every, float target_rel_linf, void* workspace,
+                  size_t ws_bytes, dips_krylov_stats_t* stats, cudaStream_t stream);
 
 #ifdef __cplusplus
 }

@@ -331,6 +331,28 @@ __global__ void k_batch_ids(int64_t n, uint64_t key, int half, int64_t start, in
   ids[b] = (int32_t)v;
 }
 
+// batch ids from a device step counter (graph-replay friendly): step = *counter,
+// batch = step % nb, epoch = step / nb.  mode 0: consecutive ranges (the reference's fixed
+// sequential batches, data_management.py:104-159); mode 1: a per-epoch seeded permutation.
+__global__ void k_batch_ids_dev(int64_t n, int64_t B, int64_t nb, uint64_t seed, int mode, int half,
+                                const int64_t* __restrict__ counter, int32_t* __restrict__ ids) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int64_t step = *counter;
+  const int64_t bi = step % nb, epoch = step / nb;
+  if (mode == 0) {
+    ids[b] = (int32_t)(bi * B + b);
+    return;
+  }
+  const uint64_t key = seed * 0x9E3779B97F4A7C15ull ^ (uint64_t)(epoch + 1) * 0xD1B54A32D192ED03ull;
+  uint64_t v = (uint64_t)(bi * B + b);
+  for (int it = 0; it < (1 << 24); ++it) {
+    v = feistel(v, half, key);
+    if (v < (uint64_t)n) break;
+  }
+  ids[b] = (int32_t)v;
+}
+
 // ----------------------------------------------------------------------------------------
 // network-shape table
 // ----------------------------------------------------------------------------------------
@@ -511,6 +533,20 @@ extern "C" int dips_batch_ids(int64_t n, int64_t epoch_index, uint64_t seed, int
   const uint64_t key = seed * 0x9E3779B97F4A7C15ull ^ (uint64_t)(epoch_index + 1) * 0xD1B54A32D192ED03ull;
   k_batch_ids<<<div_up(batch, 256), 256, 0, stream>>>(n, key, half, batch_index * batch, batch, ids);
   DIPS_CHECK_LAUNCH("dips_batch_ids");
+  return DIPS_OK;
+}
+
+extern "C" int dips_batch_ids_device(int64_t n, int64_t batch, int64_t n_batches, uint64_t seed, int32_t mode,
+                                     const int64_t* step_counter, int32_t* ids, cudaStream_t stream) {
+  DIPS_REQUIRE(n > 0 && n <= 0x7fffffff && batch > 0 && n_batches > 0 && step_counter && ids && (mode == 0 || mode == 1),
+               DIPS_E_ARG, "dips_batch_ids_device: bad argument");
+  DIPS_REQUIRE(n_batches * batch <= n, DIPS_E_ARG, "dips_batch_ids_device: %lld batches of %lld exceed n=%lld",
+               (long long)n_batches, (long long)batch, (long long)n);
+  int bits = 1;
+  while ((1ll << bits) < n) ++bits;
+  k_batch_ids_dev<<<div_up(batch, 256), 256, 0, stream>>>(n, batch, n_batches, seed, mode, (bits + 1) / 2,
+                                                          step_counter, ids);
+  DIPS_CHECK_LAUNCH("dips_batch_ids_device");
   return DIPS_OK;
 }
 

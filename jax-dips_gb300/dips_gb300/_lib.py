@@ -174,10 +174,16 @@ class AdamT(ctypes.Structure):
     _fields_ = [(n, c_f32) for n in ("lr", "decay_rate", "transition_steps", "max_norm", "b1", "b2", "eps")]
 
 
+class KrylovStatsT(ctypes.Structure):
+    _fields_ = [("iterations", c_i32), ("target_iteration", c_i32), ("breakdown", c_i32),
+                ("rel_residual", ctypes.c_double), ("rel_linf", c_f32)]
+
+
 P = ctypes.POINTER
 _SIGS = {
     "dips_last_error": (ctypes.c_char_p, []),
     "dips_version": (ctypes.c_char_p, []),
+    "dips_fp32_fma_probe": (c_i32, [c_void_p, c_i32, c_i32, c_void_p]),
     "dips_phi_ghost_layer": (c_i32, [c_void_p, c_i32, c_i32, c_i32, c_void_p, c_void_p]),
     "dips_phi_trilinear": (c_i32, [P(LevelSetT), c_void_p, c_i64, c_void_p, c_void_p]),
     "dips_geometry_classify": (
@@ -213,12 +219,13 @@ _SIGS = {
          ctypes.c_size_t, c_void_p, c_void_p, c_void_p],
     ),
     "dips_batch_ids": (c_i32, [c_i64, c_i64, ctypes.c_uint64, c_i64, c_i64, c_void_p, c_void_p]),
+    "dips_batch_ids_device": (c_i32, [c_i64, c_i64, c_i64, ctypes.c_uint64, c_i32, c_void_p, c_void_p, c_void_p]),
     "dips_mlp_eval": (c_i32, [P(ArchT), c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),
-    "dips_fv_apply": (c_i32, [P(RecordsT), c_void_p, c_void_p, c_i32, c_i32, c_i32, c_void_p, c_void_p]),
+    "dips_fv_residual": (c_i32, [P(RecordsT), c_i32, c_i32, c_i32, c_void_p, c_i32, c_void_p, c_void_p]),
     "dips_bicgstab": (
         c_i32,
-        [P(RecordsT), c_void_p, c_i32, c_i32, c_i32, c_void_p, c_void_p, c_void_p, c_i32, ctypes.c_double,
-         c_void_p, ctypes.c_size_t, c_void_p, c_void_p],
+        [P(RecordsT), c_i32, c_i32, c_i32, c_void_p, c_void_p, c_i32, ctypes.c_double, c_i32, c_f32, c_void_p,
+         ctypes.c_size_t, P(KrylovStatsT), c_void_p],
     ),
     "dips_bicgstab_workspace_bytes": (ctypes.c_size_t, [c_i64]),
 }

@@ -1,0 +1,328 @@
+"""``setup -> init_fn -> solve_fn``: the reference's NBM Poisson API (mirror of
+jax_dips/solvers/poisson/trainer.py:980-1137) running on the GB300 kernels.
+
+Differences from the reference, all on purpose:
+
+* Coefficient callables receive coordinates as an array ``r`` of shape (3, M) (a torch
+  tensor on the GPU) instead of one point; ``x, y, z = r`` and ``r[0]`` work unchanged.
+* phi is sampled on ``lvl_gstate`` and interpolated trilinearly
+  (domain/interpolate.py:906-1021); the reference evaluates the callable directly
+  (discretization.py:90).
+* The training step is one CUDA graph: batch ids from the device step counter, residual
+  forward, adjoint, gradient reduction, chained Adam.
+* ``model_dict["preconditioner"]`` may be absent (the reference requires it,
+  trainer.py:229); an enabled preconditioner is not supported.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+import logging
+import os
+import pickle
+from typing import Callable
+
+import numpy as np
+import torch
+
+from . import _lib, levelset, nn, ops
+from .mesh import GridState
+from .records import FVLevel, eval_callable
+
+logger = logging.getLogger(__name__)
+F32 = np.float32
+
+
+@dataclasses.dataclass
+class PoissonSimStateFn:
+    """The 13 callables (solvers/simulation_states.py:11-25)."""
+
+    u_0_fn: Callable
+    dir_bc_fn: Callable
+    phi_fn: Callable
+    mu_m_fn: Callable
+    mu_p_fn: Callable
+    k_m_fn: Callable
+    k_p_fn: Callable
+    f_m_fn: Callable
+    f_p_fn: Callable
+    alpha_fn: Callable
+    beta_fn: Callable
+    nonlinear_op_m: Callable
+    nonlinear_op_p: Callable
+
+
+@dataclasses.dataclass
+class PoissonSimState:
+    """The 13 arrays (solvers/simulation_states.py:58-80)."""
+
+    phi: object
+    solution: object
+    dirichlet_bc: object
+    mu_m: object
+    mu_p: object
+    k_m: object
+    k_p: object
+    f_m: object
+    f_p: object
+    alpha: object
+    beta: object
+    grad_solution: object
+    grad_normal_solution: object
+
+
+DEFAULT_OPTIMIZER = {"optimizer_name": "custom", "learning_rate": 1e-3,
+                     "sched": {"scheduler_name": "exponential", "decay_rate": 0.9}}
+DEFAULT_MODEL = {"name": None, "model_type": "mlp",
+                 "mlp": {"hidden_layers_m": 1, "hidden_dim_m": 1, "activation_m": "jnp.tanh",
+                         "hidden_layers_p": 2, "hidden_dim_p": 10, "activation_p": "jnp.tanh"}}
+
+
+def adam_state_from_dict(n_params, optimizer_dict, device):
+    """``get_optimizer`` (solvers/optimizers.py:57-97) for the Adam variants."""
+    name = optimizer_dict.get("optimizer_name", "custom")
+    lr = float(optimizer_dict.get("learning_rate", 1e-3))
+    sched = optimizer_dict.get("sched", {}) or {}
+    if name == "custom":
+        if sched.get("scheduler_name", "exponential") != "exponential":
+            raise NotImplementedError("only the exponential schedule is on the GB300 path")
+        return ops.AdamState(n_params, lr=lr, decay_rate=float(sched.get("decay_rate", 0.96)), transition_steps=1000,
+                             max_norm=1.0, device=device)
+    if name == "adam":  # optax.adam: no clipping, constant rate
+        return ops.AdamState(n_params, lr=lr, decay_rate=1.0, transition_steps=1000, max_norm=float("inf"),
+                             device=device)
+    if name in ("rmsprop", "lbfgs"):
+        raise NotImplementedError(f"optimizer {name!r} is outside the GB300 path")
+    raise ValueError(f"Unknown optimizer: {name}")
+
+
+def _levels(num_epochs):
+    q = max(num_epochs // 4, 1)
+    return (num_epochs - 1) // q + 1 if num_epochs > 0 else 1
+
+
+class Trainer:
+    """NBM training on one GPU (Trainer, solvers/poisson/trainer.py:81-977)."""
+
+    def __init__(self, lvl_gstate: GridState, tr_gstate: GridState, eval_gstate: GridState, sim_state_fn,
+                 num_epochs=1000, batch_size=131072, optimizer_dict=None, model_dict=None, batching="sequential",
+                 seed=0, checkpoint_dir=None, restart=False, restart_checkpoint_dir=None, use_graph=True,
+                 device="cuda"):
+        if not torch.cuda.is_available():
+            raise RuntimeError("dips_gb300 runs on a CUDA GPU; none is available")
+        _lib.load()
+        self.device = device
+        self.fn = sim_state_fn
+        self.lvl_gstate, self.tr_gstate, self.eval_gstate = lvl_gstate, tr_gstate, eval_gstate
+        model_dict = dict(model_dict or DEFAULT_MODEL)
+        pre = model_dict.get("preconditioner", {"enable": False}) or {"enable": False}
+        if pre.get("enable", False):
+            raise NotImplementedError("the learned preconditioner is not on the GB300 path yet")
+        self.arch = nn.arch_from_model_dict(model_dict)
+        if not _lib.load().dips_arch_supported(self.arch.ctype()):
+            raise NotImplementedError(_lib.load().dips_last_error().decode())
+        self.num_epochs = int(num_epochs)
+        self.seed = seed
+        self.batching = batching
+        self.use_graph = use_graph
+        self.checkpoint_dir = checkpoint_dir
+        # ---- level set on the level-set grid (samples of the user's phi callable)
+        self.ls = levelset.LevelSetGrid.from_callable(lvl_gstate, sim_state_fn.phi_fn, device)
+        # ---- training points, batches (DatasetDict, data/data_management.py:79-159)
+        pts = np.asarray(tr_gstate.R, F32)
+        n = pts.shape[0]
+        bs = min(int(batch_size), n)
+        if batching == "sequential":
+            nb, extra = n // bs, n % bs
+            if extra:
+                pad = self._padding_points(pts, bs - extra)
+                pts = np.concatenate([pts, pad]).astype(F32)
+                nb += 1
+        elif batching == "uniform":
+            nb = n // bs
+        else:
+            raise ValueError("batching must be 'sequential' or 'uniform'")
+        self.n_points, self.batch, self.n_batches = n, bs, nb
+        self.points = torch.as_tensor(pts, device=device)
+        self.h0 = np.array([tr_gstate.dx, tr_gstate.dy, tr_gstate.dz], F32)
+        self.n_levels = _levels(self.num_epochs)
+        # ---- params and optimizer
+        P = nn.n_params(self.arch)
+        self.params = torch.as_tensor(nn.init_params(self.arch, 42 if seed is None else seed), device=device)
+        self.opt = adam_state_from_dict(P, optimizer_dict or DEFAULT_OPTIMIZER, device)
+        self.epoch_start = 0
+        if restart:
+            self._restore(restart_checkpoint_dir)
+        self.loss_dev = torch.zeros((), dtype=torch.float64, device=device)
+        self.loss_epoch_acc = torch.zeros((), dtype=torch.float64, device=device)
+        self.ids = torch.empty(self.batch, dtype=torch.int32, device=device)
+        self._level_cache = {}
+
+    # ------------------------------------------------------------------ data
+    @staticmethod
+    def _padding_points(pts, count, seed=0):
+        """Random points rescaled to the data range (generate_random_points_like,
+        data_management.py:70-76); drawn with numpy instead of jax's PRNGKey(0)."""
+        rng = np.random.default_rng(seed)
+        dR = rng.standard_normal((count, 3))
+        lo, hi = float(pts.min()), float(pts.max())
+        return (lo + (hi - lo) * (dR - dR.min()) / (dR.max() - dR.min())).astype(F32)
+
+    def level(self, k) -> FVLevel:
+        if k not in self._level_cache:
+            self._level_cache.clear()
+            h = self.h0 * F32(0.5**k)
+            fns = {"mu_m": self.fn.mu_m_fn, "mu_p": self.fn.mu_p_fn, "k_m": self.fn.k_m_fn, "k_p": self.fn.k_p_fn,
+                   "f_m": self.fn.f_m_fn, "f_p": self.fn.f_p_fn, "alpha": self.fn.alpha_fn, "beta": self.fn.beta_fn,
+                   "g": self.fn.dir_bc_fn}
+            self._level_cache[k] = FVLevel(self.ls, fns, self.points, h)
+        return self._level_cache[k]
+
+    # ------------------------------------------------------------------ step
+    def _step(self, lvl, ws):
+        lib = _lib.load()
+        mode = 0 if self.batching == "sequential" else 1
+        n_ids = self.points.shape[0] if mode == 0 else self.n_points
+        _lib.check(lib.dips_batch_ids_device(n_ids, self.batch, self.n_batches, self.seed or 0, mode,
+                                             _lib.ptr(self.opt.count), _lib.ptr(self.ids), _lib.stream_handle()),
+                   "dips_batch_ids_device")
+        ops.train_step(self.arch, self.params, self.opt, lvl, self.ids, ws, self.loss_dev)
+        self.loss_epoch_acc += self.loss_dev
+
+    def _make_runner(self, lvl):
+        ws = ops.StepWorkspace(self.arch, self.batch, lvl.max_jobs(self.batch, distinct=True), self.device)
+        if not self.use_graph:
+            return lambda: self._step(lvl, ws), ws
+        # warm up outside the capture (sets kernel attributes), then undo its effect
+        saved = [t.clone() for t in (self.params, self.opt.mu, self.opt.nu, self.opt.count, self.loss_epoch_acc)]
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self._step(lvl, ws)
+        torch.cuda.current_stream().wait_stream(s)
+        for t, v in zip((self.params, self.opt.mu, self.opt.nu, self.opt.count, self.loss_epoch_acc), saved):
+            t.copy_(v)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self._step(lvl, ws)
+        return g.replay, ws
+
+    def solve(self, print_rate=1, callback=None):
+        """Epoch loop (single_GPU_train, trainer.py:501-591)."""
+        loss_epochs = np.zeros(self.num_epochs - self.epoch_start)
+        q = max(self.num_epochs // 4, 1)
+        cur, run = None, None
+        for epoch in range(self.epoch_start, self.num_epochs):
+            k = epoch // q  # alternate_res_sequentially (data_management.py:319-326)
+            if k != cur:
+                lvl = self.level(k)
+                run, _ = self._make_runner(lvl)
+                cur = k
+            self.loss_epoch_acc.zero_()
+            for _ in range(self.n_batches):
+                run()
+            loss_epochs[epoch - self.epoch_start] = float(self.loss_epoch_acc) / self.n_batches
+            if print_rate and (epoch % print_rate == 0):
+                logger.info("epoch %d loss %.6e", epoch, loss_epochs[epoch - self.epoch_start])
+            if callback is not None:
+                callback(epoch, loss_epochs[epoch - self.epoch_start])
+        self.epoch_store = np.arange(self.epoch_start, self.num_epochs)
+        self.loss_epochs = loss_epochs
+        if self.checkpoint_dir:
+            self.save_checkpoint(self.checkpoint_dir, self.num_epochs)
+        return self.epoch_store, loss_epochs
+
+    # ------------------------------------------------------------------ evaluation
+    def evaluate_solution_and_gradients(self, gstate: GridState):
+        """u, grad u and d_n u on a grid (trainer.py:929-977)."""
+        R = torch.as_tensor(gstate.R, device=self.device)
+        phi = self.ls(R)
+        u, gu = nn.mlp_eval(self.arch, self.params, R, phi, want_grad=True)
+        h = (gstate.dx, gstate.dy, gstate.dz)
+        d = []
+        for a in range(3):
+            rp, rm = R.clone(), R.clone()
+            rp[:, a] += float(h[a])
+            rm[:, a] -= float(h[a])
+            d.append((self.ls(rp) - self.ls(rm)) / (2.0 * float(h[a])))
+        nrm = torch.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+        gn = (gu[:, 0] * d[0] + gu[:, 1] * d[1] + gu[:, 2] * d[2]) / nrm
+        return u, gu, gn
+
+    # ------------------------------------------------------------------ checkpoints
+    def save_checkpoint(self, checkpoint_dir, epoch):
+        """pickle of {opt_state, params, epoch, batch_size, resolution} (trainer.py:340-351)."""
+        os.makedirs(checkpoint_dir, exist_ok=True)
+        state = {
+            "opt_state": {"mu": self.opt.mu.cpu().numpy(), "nu": self.opt.nu.cpu().numpy(),
+                          "count": int(self.opt.count.item())},
+            "params": {k: ({kk: np.asarray(vv.cpu()) for kk, vv in v.items()} if v else {})
+                       for k, v in nn.params_to_tree(self.params, self.arch).items()},
+            "epoch": int(epoch),
+            "batch_size": int(self.batch),
+            "resolution": f"{self.h0[0]}, {self.h0[1]}, {self.h0[2]}",
+        }
+        path = os.path.join(checkpoint_dir, "checkpoint_" + str(epoch))
+        with open(path, "wb") as f:
+            pickle.dump(state, f)
+        return path
+
+    def _restore(self, checkpoint_dir):
+        """fetch_checkpoint (trainer.py:326-338): the highest-numbered checkpoint.  The reference
+        picks max() by string and then resets the epoch to 0 (trainer.py:261); here the epoch
+        number is compared numerically and training resumes at the stored epoch."""
+        if not checkpoint_dir or not os.path.isdir(checkpoint_dir):
+            return
+        cks = [p for p in os.listdir(checkpoint_dir) if p.startswith("checkpoint_")]
+        if not cks:
+            return
+        best = max(cks, key=lambda p: int(p.split("_")[-1]))
+        with open(os.path.join(checkpoint_dir, best), "rb") as f:
+            state = pickle.load(f)
+        self.params.copy_(nn.tree_to_params(state["params"], self.arch, self.device))
+        self.opt.mu.copy_(torch.as_tensor(state["opt_state"]["mu"], device=self.device))
+        self.opt.nu.copy_(torch.as_tensor(state["opt_state"]["nu"], device=self.device))
+        self.opt.count.fill_(int(state["opt_state"]["count"]))
+        self.epoch_start = min(int(state["epoch"]), self.num_epochs)
+
+
+def setup(initial_value_fn, dirichlet_bc_fn, lvl_set_fn, mu_m_fn_, mu_p_fn_, k_m_fn_, k_p_fn_, f_m_fn_, f_p_fn_,
+          alpha_fn_, beta_fn_, nonlinear_op_m=None, nonlinear_op_p=None):
+    """``trainer.setup`` (trainer.py:980-1137)."""
+    if nonlinear_op_m is not None or nonlinear_op_p is not None:
+        raise NotImplementedError("nonlinear operators are not on the GB300 path (the reference's default is 0)")
+    zero = lambda u: 0.0  # noqa: E731
+    fn = PoissonSimStateFn(initial_value_fn, dirichlet_bc_fn, lvl_set_fn, mu_m_fn_, mu_p_fn_, k_m_fn_, k_p_fn_,
+                           f_m_fn_, f_p_fn_, alpha_fn_, beta_fn_, zero, zero)
+
+    def init_fn(lvl_gstate: GridState = None, tr_gstate: GridState = None, eval_gstate: GridState = None,
+                num_epochs: int = 1000, batch_size: int = 131072, algorithm: int = 0,
+                mgrad_over_pgrad_scalefactor: int = 1, multi_gpu: bool = False, checkpoint_interval: int = 1000,
+                checkpoint_dir: str = "./checkpoints", results_dir: str = "./", loss_plot_name: str = "solver_loss",
+                optimizer_dict: dict = None, model_dict: dict = None, restart: bool = False,
+                restart_checkpoint_dir: str = "./checkpoints", print_rate: int = 1, batching: str = "sequential",
+                seed: int = 42, use_graph: bool = True):
+        if algorithm != 0:
+            raise NotImplementedError("algorithm 1 (network extrapolation) is unimplemented in the reference too")
+        if multi_gpu:
+            raise NotImplementedError("one GPU per process; use dips_gb300.parallel for data parallelism")
+        R = torch.as_tensor(eval_gstate.R, device="cuda")
+        ev = lambda f: eval_callable(f, R)  # noqa: E731
+        state = PoissonSimState(ev(lvl_set_fn), ev(initial_value_fn), ev(dirichlet_bc_fn), ev(mu_m_fn_),
+                                ev(mu_p_fn_), ev(k_m_fn_), ev(k_p_fn_), ev(f_m_fn_), ev(f_p_fn_), ev(alpha_fn_),
+                                ev(beta_fn_), None, None)
+
+        def solve_fn(sim_state: PoissonSimState):
+            tr = Trainer(lvl_gstate, tr_gstate, eval_gstate, fn, num_epochs=num_epochs, batch_size=batch_size,
+                         optimizer_dict=optimizer_dict, model_dict=model_dict, batching=batching, seed=seed,
+                         checkpoint_dir=checkpoint_dir, restart=restart, restart_checkpoint_dir=restart_checkpoint_dir,
+                         use_graph=use_graph)
+            epoch_store, loss_epochs = tr.solve(print_rate=print_rate)
+            u, gu, gn = tr.evaluate_solution_and_gradients(eval_gstate)
+            new = dataclasses.replace(sim_state, solution=u, grad_solution=gu, grad_normal_solution=gn)
+            solve_fn.trainer = tr
+            return new, epoch_store, loss_epochs
+
+        return state, solve_fn
+
+    return init_fn

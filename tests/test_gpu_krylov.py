@@ -1,0 +1,84 @@
+"""Plain method on the GPU: the FV operator of a nodal vector against the oracle, and
+BiCGSTAB against a float64 direct solve of the oracle's operator."""
+
+import numpy as np
+import pytest
+
+import _parity
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+L = _parity.L
+
+
+def _nodal_lookup(n, h0):
+    """Network values replaced by grid-node values of u (exact at nodes, as the reference's
+    quadratic interpolant of a nodal vector is)."""
+
+    def make(u):
+        def values(net, x, phi_x):
+            q = x.reshape(-1, 3).double()
+            idx = torch.round((q + 1.0) / float(h0)).long().clamp(0, n - 1)
+            lin = (idx[:, 0] * n + idx[:, 1]) * n + idx[:, 2]
+            return u.to(q.dtype)[lin].reshape(x.shape[:-1])
+
+        return values
+
+    return make
+
+
+def test_fv_residual_matches_oracle_nodal_operator():
+    from dips_gb300 import krylov
+
+    n = 20
+    case = _parity.build_case("star", n=n)
+    lvl = case.gpu_level()
+    rng = np.random.default_rng(0)
+    u = rng.standard_normal(n**3).astype(np.float32)
+    got = krylov.fv_residual(lvl, (n, n, n), torch.as_tensor(u, device="cuda")).cpu().numpy()
+    orig = L.nn_eval
+    try:
+        L.nn_eval = _nodal_lookup(n, case.grid.dx)(torch.as_tensor(u))
+        ref = L.residual(torch.zeros(L.n_params(case.arch)), case.arch, case.oracle_geometry(), torch.float64).numpy()
+    finally:
+        L.nn_eval = orig
+    np.testing.assert_allclose(got, ref, rtol=1e-4, atol=1e-5 * np.abs(ref).max())
+
+
+def test_bicgstab_solves_the_fv_system():
+    import scipy.sparse.linalg as spla
+
+    from dips_gb300 import krylov, problems
+
+    n = 16
+    case = _parity.build_case("sphere", n=n)
+    lvl = case.gpu_level()
+    ex = problems.exact_solution(case.fns, case.grid.R)
+    res = krylov.bicgstab(lvl, (n, n, n), u_exact=torch.as_tensor(ex, device="cuda"), max_iter=2000, rtol=1e-6,
+                          check_every=5)
+    assert not res.breakdown and res.rel_residual <= 1e-6
+    x = res.x.cpu().numpy().astype(np.float64)
+    # float64 reference solve of the oracle's nodal operator
+    rg = case.oracle_geometry()
+    U = {}
+    look = _nodal_lookup(n, case.grid.dx)
+    orig = L.nn_eval
+    try:
+        z = torch.zeros(L.n_params(case.arch), dtype=torch.float64)
+        L.nn_eval = lambda net, xx, ph: look(U["u"])(net, xx, ph)  # noqa: E731
+        U["u"] = torch.zeros(n**3, dtype=torch.float64)
+        r0 = L.residual(z, case.arch, rg, torch.float64).numpy()
+
+        def mv(v):
+            U["u"] = torch.as_tensor(v)
+            return L.residual(z, case.arch, rg, torch.float64).numpy() - r0
+
+        A = spla.LinearOperator((n**3, n**3), matvec=mv, dtype=np.float64)
+        sol, info = spla.bicgstab(A, -r0, rtol=1e-10, maxiter=2000)
+    finally:
+        L.nn_eval = orig
+    assert info == 0
+    assert np.abs(x - sol).max() <= 1e-4 * np.abs(sol).max()
+    err = np.abs(sol - ex).max() / np.abs(ex).max()
+    assert abs(res.rel_linf - err) <= 1e-3
