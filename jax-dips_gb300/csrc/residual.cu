@@ -33,6 +33,7 @@ static size_t carve(Workspace* w, char* base, int64_t B, int64_t max_jobs, int P
   W.nres = (B + 255) / 256;
   W.jcap = max_jobs + 64;
   W.grid = kAdjGrid;
+  W.n_params = P;
   W.ctl = (Ctl*)take(sizeof(Ctl));
   W.cm = (int32_t*)take(sizeof(int32_t) * B);
   W.cp = (int32_t*)take(sizeof(int32_t) * B);

@@ -1,9 +1,15 @@
 // Per-network-shape kernels of the residual path (included once per shape by the
-// residual_a_*.cu translation units, which define DIPS_LM, DIPS_WM, DIPS_LP, DIPS_WP).
+// residual_a*.cu translation units, which define DIPS_LM, DIPS_WM, DIPS_LP, DIPS_WP).
 //
-// Forward and adjoint run one thread per job on the FP32 pipe: the weights are read as
-// constant-bank operands of FFMA; dW is accumulated with a per-warp shared-memory
-// outer-product GEMM and reduced to one partial gradient row per CTA.
+// Everything runs on the FP32 pipe.  Each network (u- and u+) gets its own launches, so a
+// kernel holds one network's fully unrolled code:
+//   forward  one thread per job; the weights are constant-bank operands of FFMA
+//   adjoint  one thread per job recomputes the activations and stages them in the warp's
+//            shared-memory tile; the output gradients propagate thread-per-job (again with
+//            constant operands) and overwrite the tile in place; each layer's dW is a warp
+//            GEMM over the tile's 32 jobs (lane = output unit, broadcast float4 rows)
+//            accumulated with shared-memory atomics into one CTA accumulator, written out
+//            as one partial gradient row per CTA.
 // Reference: DoubleMLP (nn/mlp/MLP.py:93-139), value_and_grad in Trainer.update
 // (solvers/poisson/trainer.py:783-789).
 
@@ -20,7 +26,24 @@ static __constant__ float c_w[kMaxConstParams];
 constexpr int kThreads = kAdjThreads;
 constexpr int kWarps = kThreads / 32;
 
-__device__ __forceinline__ float act_tanh(float z) { return tanhf(z); }
+// tanh, accurate to ~2.5e-7 relative (float32): an odd least-squares polynomial
+// x + x^3 P(x^2) of degree 4 in x^2 for |x| < 0.625, and 1 - 2/(1 + e^{2|x|}) with the
+// hardware exp2 and reciprocal approximations (relative error <= 2^-22) above.
+__device__ __forceinline__ float act_tanh(float x) {
+  const float t = fabsf(x);
+  const float s = x * x;
+  float p = fmaf(s, -0.0057189627550542355f, 0.020653124898672104f);
+  p = fmaf(p, s, -0.05374465882778168f);
+  p = fmaf(p, s, 0.13331513106822968f);
+  p = fmaf(p, s, -0.3333328664302826f);
+  const float small = fmaf(x * s, p, x);
+  float e;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(t * 2.8853900817779268f));  // e^{2t}
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(1.0f + e));
+  const float big = copysignf(fmaf(-2.0f, r, 1.0f), x);
+  return t < 0.625f ? small : big;
+}
 
 // ----------------------------------------------------------------------------------------
 // network shapes and parameter offsets (flat layout documented in dips.h)
@@ -32,6 +55,9 @@ struct Net {
   static constexpr int kParams = 3 * W + W + (L - 1) * (W * W + W) + W + 1;
   static constexpr int kOut = 4 * W + (L - 1) * (W * W + W);
   __host__ __device__ static constexpr int layer_off(int l) { return l == 0 ? 0 : 4 * W + (l - 1) * (W * W + W); }
+  // shared-memory tile: rows of one job, float4-aligned, 4 floats of padding
+  static constexpr int kRow = (W + 3) / 4 * 4 + 4;
+  static constexpr int kTileFloats = 32 * 4 + L * 32 * kRow + 32;  // x, activations / deltas, g
 };
 
 template <int LM, int WM, int LP, int WP>
@@ -40,7 +66,6 @@ struct Arch {
   using P = Net<LP, WP>;
   static constexpr int kOffP = M::kParams;
   static constexpr int kParams = M::kParams + P::kParams;
-  static constexpr int kMaxW = WM > WP ? WM : WP;
 };
 
 // forward, activations discarded
@@ -74,10 +99,214 @@ __device__ __forceinline__ float net_forward(const float x[3]) {
   return u + c_w[OFF + N::kOut + W];
 }
 
-// forward keeping every hidden activation
+template <int W>
+__device__ __forceinline__ void store_row(float* row, const float* v) {
+  if constexpr (W % 4 == 0) {
+#pragma unroll
+    for (int i = 0; i < W; i += 4) *reinterpret_cast<float4*>(row + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < W; ++i) row[i] = v[i];
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void load_row(const float* row, float* v) {
+  if constexpr (W % 4 == 0) {
+#pragma unroll
+    for (int i = 0; i < W; i += 4) {
+      const float4 q = *reinterpret_cast<const float4*>(row + i);
+      v[i] = q.x;
+      v[i + 1] = q.y;
+      v[i + 2] = q.z;
+      v[i + 3] = q.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < W; ++i) v[i] = row[i];
+  }
+}
+
+// forward of one job, staging x and every hidden activation in the warp tile row `lane`;
+// returns the last hidden activation in h
 template <class N, int OFF>
-__device__ __forceinline__ float net_forward_act(const float x[3], float act[N::kL][N::kW]) {
+__device__ __forceinline__ void net_forward_stage(const float x[3], float* X, float* B, int lane, float h[N::kW]) {
+  constexpr int W = N::kW, L = N::kL, R = N::kRow;
+  *reinterpret_cast<float4*>(X + 4 * lane) = make_float4(x[0], x[1], x[2], 0.0f);
+#pragma unroll
+  for (int o = 0; o < W; ++o) {
+    float z = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) z = fmaf(x[i], c_w[OFF + i * W + o], z);
+    h[o] = act_tanh(z + c_w[OFF + 3 * W + o]);
+  }
+  store_row<W>(B + lane * R, h);
+#pragma unroll
+  for (int l = 1; l < L; ++l) {
+    const int off = OFF + N::layer_off(l);
+    float t[W];
+#pragma unroll
+    for (int o = 0; o < W; ++o) t[o] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < W; ++i)
+#pragma unroll
+      for (int o = 0; o < W; ++o) t[o] = fmaf(h[i], c_w[off + i * W + o], t[o]);
+#pragma unroll
+    for (int o = 0; o < W; ++o) h[o] = act_tanh(t[o] + c_w[off + W * W + o]);
+    store_row<W>(B + (l * 32 + lane) * R, h);
+  }
+}
+
+// dW[i][o] += sum_e H[e][i] D[e][o], db[o] += sum_e D[e][o] over the tile's 32 rows.
+// lane = o; when OUT < 32 the lane groups split the rows.  Shared-memory atomics add the
+// tile's contribution into the CTA accumulator.
+template <int IN, int OUT, int RIN, int RD>
+__device__ __forceinline__ void tile_gemm(const float* H, const float* D, float* accW, float* accb, int lane) {
+  constexpr int G = 32 / OUT;
+  const int o = lane % OUT, q = lane / OUT;
+  if (q >= G) return;
+  const int e0 = (q * 32) / G, e1 = ((q + 1) * 32) / G;
+  float s[IN];
+#pragma unroll
+  for (int i = 0; i < IN; ++i) s[i] = 0.0f;
+  float sb = 0.0f;
+#pragma unroll 4
+  for (int e = e0; e < e1; ++e) {
+    const float dv = D[e * RD + o];
+    sb += dv;
+    const float* row = H + e * RIN;
+    if constexpr (IN % 4 == 0 || IN == 3) {
+#pragma unroll
+      for (int i = 0; i < IN; i += 4) {
+        const float4 v = *reinterpret_cast<const float4*>(row + i);
+        s[i] = fmaf(v.x, dv, s[i]);
+        if (i + 1 < IN) s[i + 1] = fmaf(v.y, dv, s[i + 1]);
+        if (i + 2 < IN) s[i + 2] = fmaf(v.z, dv, s[i + 2]);
+        if (i + 3 < IN) s[i + 3] = fmaf(v.w, dv, s[i + 3]);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < IN; ++i) s[i] = fmaf(row[i], dv, s[i]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < IN; ++i) atomicAdd(accW + i * OUT + o, s[i]);
+  atomicAdd(accb + o, sb);
+}
+
+// one tile of 32 jobs of network N: forward recompute, backpropagation of g, dW accumulation
+template <class N, int OFF, int BOFF>
+__device__ __forceinline__ void net_adjoint_tile(const float x[3], float g, float* tile, float* acc, int lane) {
+  constexpr int W = N::kW, L = N::kL, R = N::kRow;
+  float* X = tile;
+  float* B = tile + 32 * 4;
+  float* gs = B + L * 32 * R;
+  float h[W];
+  net_forward_stage<N, OFF>(x, X, B, lane, h);
+  gs[lane] = g;
+  __syncwarp();
+  // output layer u = sum_i Wo[i] h[i] + bo: dWo[i] += sum_e h[e][i] g[e] (lane = i)
+  {
+    const float* HL = B + (L - 1) * 32 * R;
+    if (lane < W) {
+      float s = 0.0f;
+#pragma unroll 8
+      for (int e = 0; e < 32; ++e) s = fmaf(HL[e * R + lane], gs[e], s);
+      atomicAdd(acc + N::kOut + lane, s);
+    }
+    if (lane == 0) {
+      float sb = 0.0f;
+      for (int e = 0; e < 32; ++e) sb += gs[e];
+      atomicAdd(acc + N::kOut + W, sb);
+    }
+  }
+  float d[W];
+#pragma unroll
+  for (int i = 0; i < W; ++i) d[i] = g * c_w[BOFF + OFF + N::kOut + i] * fmaf(-h[i], h[i], 1.0f);
+  __syncwarp();
+  store_row<W>(B + ((L - 1) * 32 + lane) * R, d);  // the last tile buffer now holds delta_{L-1}
+  __syncwarp();
+#pragma unroll
+  for (int l = L - 1; l >= 1; --l) {
+    const int off = N::layer_off(l);
+    float* Hin = B + (l - 1) * 32 * R;
+    tile_gemm<W, W, R, R>(Hin, B + l * 32 * R, acc + off, acc + off + W * W, lane);
+    float a[W];
+    load_row<W>(Hin + lane * R, a);
+    float dn[W];
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      float s = 0.0f;
+#pragma unroll
+      for (int o = 0; o < W; ++o) s = fmaf(c_w[BOFF + OFF + off + i * W + o], d[o], s);
+      dn[i] = s * fmaf(-a[i], a[i], 1.0f);
+    }
+    __syncwarp();
+    store_row<W>(Hin + lane * R, dn);
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < W; ++i) d[i] = dn[i];
+  }
+  tile_gemm<3, W, 4, R>(X, B, acc, acc + 3 * W, lane);
+  __syncwarp();
+}
+
+template <class N, int OFF>
+__global__ void __launch_bounds__(256) k_job_forward(PtsH ph, const int32_t* __restrict__ ids, Workspace w, int net_p) {
+  const Ctl ctl = *w.ctl;
+  const int64_t begin = net_p ? ctl.jm_pad : 0;
+  const int64_t end = net_p ? ctl.total : ctl.jm;
+  for (int64_t j = begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < end; j += (int64_t)gridDim.x * blockDim.x) {
+    float x[3];
+    job_point(ph, ids, w.jslot[j], w.jcode[j], x);
+    w.ju[j] = net_forward<N, OFF>(x);
+  }
+}
+
+template <class N>
+constexpr size_t adj_smem_bytes() {
+  return sizeof(float) * ((size_t)(N::kParams + 3) / 4 * 4 + (size_t)kWarps * N::kTileFloats);
+}
+
+template <class N, int OFF, int BOFF>
+__global__ void __launch_bounds__(kThreads, 3) k_job_adjoint(PtsH ph, const int32_t* __restrict__ ids, Workspace w,
+                                                             int net_p) {
+  extern __shared__ float4 smem4[];
+  float* smem = reinterpret_cast<float*>(smem4);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float* acc = smem;
+  float* tile = smem + (N::kParams + 3) / 4 * 4 + warp * N::kTileFloats;
+  for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) acc[i] = 0.0f;
+  __syncthreads();
+  const Ctl ctl = *w.ctl;
+  const int64_t begin = net_p ? ctl.jm_pad : 0;
+  const int64_t end = net_p ? ctl.total : ctl.jm;
+  const int64_t tiles = (end - begin + 31) / 32;
+  for (int64_t t = (int64_t)blockIdx.x * kWarps + warp; t < tiles; t += (int64_t)gridDim.x * kWarps) {
+    const int64_t j = begin + t * 32 + lane;
+    float x[3] = {0.0f, 0.0f, 0.0f};
+    float g = 0.0f;
+    if (j < end) {
+      const int32_t slot = w.jslot[j];
+      if (slot >= 0) {
+        job_point(ph, ids, slot, w.jcode[j], x);
+        g = w.gs[slot] * w.jA[j];
+      }
+    }
+    net_adjoint_tile<N, OFF, BOFF>(x, g, tile, acc, lane);
+  }
+  __syncthreads();
+  float* row = w.partials + (size_t)blockIdx.x * w.n_params + OFF;
+  for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) row[i] = acc[i];
+}
+
+// ----------------------------------------------------------------------------------------
+// network evaluation with input gradient
+// ----------------------------------------------------------------------------------------
+template <class N, int OFF, int BOFF>
+__device__ __forceinline__ float net_eval_grad(const float x[3], float gx[3]) {
   constexpr int W = N::kW, L = N::kL;
+  float act[L][W];
 #pragma unroll
   for (int o = 0; o < W; ++o) {
     float z = 0.0f;
@@ -101,212 +330,7 @@ __device__ __forceinline__ float net_forward_act(const float x[3], float act[N::
   float u = 0.0f;
 #pragma unroll
   for (int i = 0; i < W; ++i) u = fmaf(act[L - 1][i], c_w[OFF + N::kOut + i], u);
-  return u + c_w[OFF + N::kOut + W];
-}
-
-// ----------------------------------------------------------------------------------------
-// per-warp outer-product accumulation  accW[i][o] += sum_lanes in[i]*d[o],  accb[o] += sum d[o]
-// ----------------------------------------------------------------------------------------
-constexpr int kStageIn = 36;   // float4-aligned row stride of the staged inputs (<= 32 used)
-constexpr int kStageD = 33;    // row stride of the staged output gradients
-constexpr int kStageFloats = 32 * kStageIn + 32 * kStageD;
-
-template <int IN, int OUT>
-__device__ __forceinline__ void warp_stage(const float* in, const float* d, float* sIn, float* sD, int lane) {
-#pragma unroll
-  for (int i = 0; i < IN; ++i) sIn[lane * kStageIn + i] = in[i];
-#pragma unroll
-  for (int o = 0; o < OUT; ++o) sD[lane * kStageD + o] = d[o];
-  __syncwarp();
-}
-
-// accW[i][o] += sum_e sIn[e][i] * sD[e][o];  accb[o] += sum_e sD[e][o]  (e = the warp's 32 lanes)
-template <int IN, int OUT>
-__device__ __forceinline__ void warp_gemm_acc(const float* sIn, const float* sD, float* accW, float* accb, int lane) {
-  constexpr int IG = 32 / OUT;            // lane groups splitting the inputs
-  constexpr int CH = (IN + IG - 1) / IG;  // inputs per lane
-  constexpr int CK = CH > 16 ? 16 : CH;   // inputs per pass (bounds live accumulators)
-  const int o = lane % OUT;
-  const int ig = lane / OUT;
-  if (ig < IG) {
-    const int i0 = ig * CH;
-#pragma unroll
-    for (int c0 = 0; c0 < CH; c0 += CK) {
-      float s[CK];
-#pragma unroll
-      for (int c = 0; c < CK; ++c) s[c] = 0.0f;
-      float sb = 0.0f;
-#pragma unroll 4
-      for (int e = 0; e < 32; ++e) {
-        const float dv = sD[e * kStageD + o];
-        if (c0 == 0) sb += dv;
-        const float* row = sIn + e * kStageIn + i0 + c0;
-        if constexpr (CK % 4 == 0) {
-#pragma unroll
-          for (int c = 0; c < CK; c += 4) {
-            const float4 v = *reinterpret_cast<const float4*>(row + c);
-            s[c] = fmaf(v.x, dv, s[c]);
-            s[c + 1] = fmaf(v.y, dv, s[c + 1]);
-            s[c + 2] = fmaf(v.z, dv, s[c + 2]);
-            s[c + 3] = fmaf(v.w, dv, s[c + 3]);
-          }
-        } else {
-#pragma unroll
-          for (int c = 0; c < CK; ++c)
-            if (i0 + c0 + c < IN) s[c] = fmaf(row[c], dv, s[c]);
-        }
-      }
-#pragma unroll
-      for (int c = 0; c < CK; ++c)
-        if (c0 + c < CH && i0 + c0 + c < IN) accW[(i0 + c0 + c) * OUT + o] += s[c];
-      if (c0 == 0 && ig == 0) accb[o] += sb;
-    }
-  }
-  __syncwarp();
-}
-
-// backpropagate g = dL/du through network N at x, accumulating into the warp's accumulator
-// The backward pass reads the weights from a second copy in the constant bank (offset BOFF):
-// with a single copy the compiler keeps every weight used by both passes in registers.
-template <class N, int OFF, int BOFF>
-__device__ __forceinline__ void net_adjoint(const float x[3], float g, float* sIn, float* sD, float* acc, int lane) {
-  constexpr int W = N::kW, L = N::kL;
-  float act[L][W];
-  net_forward_act<N, OFF>(x, act);
-  float d[W];
-  // output layer u = sum_i Wo[i] h[i] + bo
-  {
-    const float gg[1] = {g};
-    warp_stage<W, 1>(act[L - 1], gg, sIn, sD, lane);
-#pragma unroll
-    for (int i = 0; i < W; ++i) {
-      const float hv = act[L - 1][i];
-      d[i] = g * c_w[BOFF + OFF + N::kOut + i] * fmaf(-hv, hv, 1.0f);
-    }
-    warp_gemm_acc<W, 1>(sIn, sD, acc + N::kOut, acc + N::kOut + W, lane);
-  }
-#pragma unroll
-  for (int l = L - 1; l >= 1; --l) {
-    const int off = N::layer_off(l);
-    warp_stage<W, W>(act[l - 1], d, sIn, sD, lane);
-    float dn[W];
-#pragma unroll
-    for (int i = 0; i < W; ++i) {
-      float s = 0.0f;
-#pragma unroll
-      for (int o = 0; o < W; ++o) s = fmaf(c_w[BOFF + OFF + off + i * W + o], d[o], s);
-      const float hv = act[l - 1][i];
-      dn[i] = s * fmaf(-hv, hv, 1.0f);
-    }
-    warp_gemm_acc<W, W>(sIn, sD, acc + off, acc + off + W * W, lane);
-#pragma unroll
-    for (int i = 0; i < W; ++i) d[i] = dn[i];
-  }
-  warp_stage<3, W>(x, d, sIn, sD, lane);
-  warp_gemm_acc<3, W>(sIn, sD, acc, acc + 3 * W, lane);
-}
-
-template <class A>
-__global__ void __launch_bounds__(256) k_job_forward(PtsH ph, const int32_t* __restrict__ ids, Workspace w) {
-  const Ctl ctl = *w.ctl;
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < ctl.total; j += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t slot = w.jslot[j];
-    float u = 0.0f;
-    if (slot >= 0) {
-      float x[3];
-      job_point(ph, ids, slot, w.jcode[j], x);
-      if (j < ctl.jm_pad)
-        u = net_forward<typename A::M, 0>(x);
-      else
-        u = net_forward<typename A::P, A::kOffP>(x);
-    }
-    w.ju[j] = u;
-  }
-}
-
-// ----------------------------------------------------------------------------------------
-// adjoint over jobs
-// ----------------------------------------------------------------------------------------
-template <class A>
-struct AdjSmem {
-  static constexpr int kAccM = A::M::kParams;
-  static constexpr int kAccP = A::P::kParams;
-  static constexpr int kAcc = kAccM > kAccP ? kAccM : kAccP;
-  static constexpr int kPerWarp = kStageFloats + (kAcc + 3) / 4 * 4;  // keeps float4 rows aligned
-  static constexpr size_t kBytes = sizeof(float) * (size_t)kPerWarp * kWarps;
-};
-
-template <class A>
-__global__ void __launch_bounds__(kThreads, 1) k_job_adjoint(PtsH ph, const int32_t* __restrict__ ids, Workspace w) {
-  extern __shared__ float smem[];
-  using S = AdjSmem<A>;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float* sIn = smem + warp * S::kPerWarp;
-  float* sD = sIn + 32 * kStageIn;
-  float* acc = sD + 32 * kStageD;
-  for (int i = lane; i < S::kAcc; i += 32) acc[i] = 0.0f;
-  __syncwarp();
-
-  const Ctl ctl = *w.ctl;
-  const int64_t tiles_m = ctl.jm_pad / 32;
-  const int64_t tiles_p = (ctl.jp + 31) / 32;
-  const int64_t tiles = tiles_m + tiles_p;
-  // CTAs [0, gm) take u- tiles, the rest take u+ tiles (in proportion to the tile counts)
-  int gm = 0;
-  if (tiles > 0) {
-    gm = (int)((tiles_m * (int64_t)gridDim.x + tiles / 2) / tiles);
-    if (tiles_m > 0 && gm < 1) gm = 1;
-    if (tiles_p > 0 && gm > (int)gridDim.x - 1) gm = gridDim.x - 1;
-    if (tiles_p == 0) gm = gridDim.x;
-  }
-  const bool net_p = (int)blockIdx.x >= gm;
-  const int64_t my_tiles = net_p ? tiles_p : tiles_m;
-  const int64_t cta = net_p ? blockIdx.x - gm : blockIdx.x;
-  const int64_t nctas = net_p ? (int64_t)gridDim.x - gm : gm;
-  const int64_t base = net_p ? ctl.jm_pad : 0;
-  const int64_t end = net_p ? ctl.total : ctl.jm;
-
-  if (nctas > 0) {
-    for (int64_t t = cta * kWarps + warp; t < my_tiles; t += nctas * kWarps) {
-      const int64_t j = base + t * 32 + lane;
-      float x[3] = {0.0f, 0.0f, 0.0f};
-      float g = 0.0f;
-      if (j < end) {
-        const int32_t slot = w.jslot[j];
-        if (slot >= 0) {
-          job_point(ph, ids, slot, w.jcode[j], x);
-          g = w.gs[slot] * w.jA[j];
-        }
-      }
-      if (net_p)
-        net_adjoint<typename A::P, A::kOffP, A::kParams>(x, g, sIn, sD, acc, lane);
-      else
-        net_adjoint<typename A::M, 0, A::kParams>(x, g, sIn, sD, acc, lane);
-    }
-  }
-  __syncthreads();
-  // fixed-order reduction of the warps' accumulators into this CTA's partial row
-  const int np = net_p ? A::P::kParams : A::M::kParams;
-  const int off = net_p ? A::kOffP : 0;
-  float* row = w.partials + (size_t)blockIdx.x * A::kParams;
-  for (int i = threadIdx.x; i < A::kParams; i += blockDim.x) {
-    float v = 0.0f;
-    const int li = i - off;
-    if (li >= 0 && li < np && nctas > 0) {
-      for (int q = 0; q < kWarps; ++q) v += smem[q * S::kPerWarp + kStageFloats + li];
-    }
-    row[i] = v;
-  }
-}
-
-// ----------------------------------------------------------------------------------------
-// network evaluation with input gradient
-// ----------------------------------------------------------------------------------------
-template <class N, int OFF, int BOFF>
-__device__ __forceinline__ float net_eval_grad(const float x[3], float gx[3]) {
-  constexpr int W = N::kW, L = N::kL;
-  float act[L][W];
-  const float u = net_forward_act<N, OFF>(x, act);
+  u += c_w[OFF + N::kOut + W];
   float d[W];
 #pragma unroll
   for (int i = 0; i < W; ++i) {
@@ -338,17 +362,15 @@ __device__ __forceinline__ float net_eval_grad(const float x[3], float gx[3]) {
   return u;
 }
 
-template <class A>
-__global__ void __launch_bounds__(128) k_mlp_eval(const float* __restrict__ pts, const float* __restrict__ phi, int64_t n,
-                                                  float* __restrict__ u_out, float* __restrict__ g_out) {
+template <class N, int OFF, int BOFF>
+__global__ void __launch_bounds__(128) k_mlp_eval(const float* __restrict__ pts, const float* __restrict__ phi,
+                                                  int64_t n, float* __restrict__ u_out, float* __restrict__ g_out,
+                                                  int net_p) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if ((phi[i] >= 0.0f) != (net_p != 0)) continue;
     const float x[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
     float gx[3];
-    float u;
-    if (phi[i] >= 0.0f)
-      u = net_eval_grad<typename A::P, A::kOffP, A::kParams>(x, gx);
-    else
-      u = net_eval_grad<typename A::M, 0, A::kParams>(x, gx);
+    const float u = net_eval_grad<N, OFF, BOFF>(x, gx);
     u_out[i] = u;
     if (g_out) {
       g_out[3 * i] = gx[0];
@@ -358,12 +380,12 @@ __global__ void __launch_bounds__(128) k_mlp_eval(const float* __restrict__ pts,
   }
 }
 
-
 using A = Arch<DIPS_LM, DIPS_WM, DIPS_LP, DIPS_WP>;
 
 static int load_params(const float* params, cudaStream_t s) {
   static_assert(2 * A::kParams <= kMaxConstParams, "network too large for the constant bank");
-  // two copies: forward-pass operands at 0, backward-pass operands at kParams
+  // two copies: forward-pass operands at 0, backward-pass operands at kParams (with one
+  // copy the compiler keeps every weight used by both passes in registers)
   cudaError_t e = cudaMemcpyToSymbolAsync(c_w, params, sizeof(float) * A::kParams, 0, cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess)
     e = cudaMemcpyToSymbolAsync(c_w, params, sizeof(float) * A::kParams, sizeof(float) * A::kParams,
@@ -372,20 +394,31 @@ static int load_params(const float* params, cudaStream_t s) {
 }
 
 static int job_forward(const PtsH& ph, const int32_t* ids, const Workspace& w, cudaStream_t s) {
-  k_job_forward<A><<<152 * 8, 256, 0, s>>>(ph, ids, w);
+  k_job_forward<typename A::M, 0><<<152 * 8, 256, 0, s>>>(ph, ids, w, 0);
+  k_job_forward<typename A::P, A::kOffP><<<152 * 8, 256, 0, s>>>(ph, ids, w, 1);
   DIPS_CHECK_LAUNCH("job forward");
   return DIPS_OK;
 }
 
-static int job_adjoint(const PtsH& ph, const int32_t* ids, const Workspace& w, cudaStream_t s) {
+template <class N, int OFF>
+static int adjoint_launch(const PtsH& ph, const int32_t* ids, const Workspace& w, int net_p, cudaStream_t s) {
+  constexpr size_t bytes = adj_smem_bytes<N>();
   static bool attr_done = false;
   if (!attr_done) {
-    cudaError_t e =
-        cudaFuncSetAttribute(k_job_adjoint<A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AdjSmem<A>::kBytes);
+    cudaError_t e = cudaFuncSetAttribute(k_job_adjoint<N, OFF, A::kParams>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)bytes);
     if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(adjoint smem)");
     attr_done = true;
   }
-  k_job_adjoint<A><<<w.grid, kThreads, AdjSmem<A>::kBytes, s>>>(ph, ids, w);
+  k_job_adjoint<N, OFF, A::kParams><<<w.grid, kThreads, bytes, s>>>(ph, ids, w, net_p);
+  return DIPS_OK;
+}
+
+static int job_adjoint(const PtsH& ph, const int32_t* ids, const Workspace& w, cudaStream_t s) {
+  int st = adjoint_launch<typename A::M, 0>(ph, ids, w, 0, s);
+  if (st) return st;
+  st = adjoint_launch<typename A::P, A::kOffP>(ph, ids, w, 1, s);
+  if (st) return st;
   DIPS_CHECK_LAUNCH("job adjoint");
   return DIPS_OK;
 }
@@ -393,7 +426,8 @@ static int job_adjoint(const PtsH& ph, const int32_t* ids, const Workspace& w, c
 static int mlp_eval(const float* pts, const float* phi, int64_t n, float* u, float* g, cudaStream_t s) {
   int64_t grid = (n + 127) / 128;
   if (grid > 152 * 16) grid = 152 * 16;
-  k_mlp_eval<A><<<(int)grid, 128, 0, s>>>(pts, phi, n, u, g);
+  k_mlp_eval<typename A::M, 0, A::kParams><<<(int)grid, 128, 0, s>>>(pts, phi, n, u, g, 0);
+  k_mlp_eval<typename A::P, A::kOffP, A::kParams><<<(int)grid, 128, 0, s>>>(pts, phi, n, u, g, 1);
   DIPS_CHECK_LAUNCH("mlp eval");
   return DIPS_OK;
 }

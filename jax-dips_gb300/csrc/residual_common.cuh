@@ -7,8 +7,8 @@
 namespace dips {
 
 constexpr int kScanBlock = 1024;
-constexpr int kAdjThreads = 256;  // adjoint CTA: 8 warps
-constexpr int kAdjGrid = 152;     // one adjoint CTA per SM (GB300 has 152 SMs)
+constexpr int kAdjThreads = 128;     // adjoint CTA: 4 warps
+constexpr int kAdjGrid = 152 * 3;    // three adjoint CTAs per SM (GB300 has 152 SMs)
 
 // ----------------------------------------------------------------------------------------
 // workspace
@@ -36,6 +36,7 @@ struct Workspace {
   float* grad;       // [P]
   int64_t nblk, nres, jcap;
   int grid;
+  int n_params;      // row stride of partials
 };
 
 struct PtsH {
