@@ -168,6 +168,16 @@ int dips_train_step(const dips_arch_t* arch, const dips_adam_t* hp, float* param
                     int64_t* count, const dips_records_t* rec, const int32_t* batch_ids, int64_t batch,
                     void* workspace, size_t ws_bytes, double* loss_out, float* grad_out,
                     cudaStream_t stream);
+/* dips_train_step without a workspace argument, for callers that cannot allocate device
+   memory (e.g. an XLA custom-call handler, which gets only the buffers XLA planned for it).
+   No counterpart in the reference.  The scratch is a 64 MiB device array inside the library:
+   every GPU that loads it keeps the 64 MiB until exit; batches whose workspace for max_jobs
+   jobs (dips_step_workspace_bytes) exceeds it fail with DIPS_E_WORKSPACE; the first call on a
+   device resolves the array's address (make it before any stream capture); all calls share
+   the array, so calls that overlap on the GPU race.  Allocates nothing. */
+int dips_train_step_noalloc(const dips_arch_t* arch, const dips_adam_t* hp, float* params, float* mu, float* nu,
+                            int64_t* count, const dips_records_t* rec, const int32_t* batch_ids, int64_t batch,
+                            int64_t max_jobs, double* loss_out, float* grad_out, cudaStream_t stream);
 /* Batch ids of batch `index` of an epoch: a seeded bijective permutation of 0..n-1
    (uniform minibatches without replacement), written to ids[0..B).  epoch_index and
    seed select the permutation. */

@@ -34,6 +34,7 @@ UNITS = {
     "residual_a2_16_2_16.cu": [],
     "residual_a3_32_3_32.cu": [],
     "krylov.cu": [],
+    "residual_static.cu": [],
 }
 
 _lock = threading.Lock()
@@ -217,6 +218,11 @@ _SIGS = {
         c_i32,
         [P(ArchT), P(AdamT), c_void_p, c_void_p, c_void_p, c_void_p, P(RecordsT), c_void_p, c_i64, c_void_p,
          ctypes.c_size_t, c_void_p, c_void_p, c_void_p],
+    ),
+    "dips_train_step_noalloc": (
+        c_i32,
+        [P(ArchT), P(AdamT), c_void_p, c_void_p, c_void_p, c_void_p, P(RecordsT), c_void_p, c_i64, c_i64, c_void_p,
+         c_void_p, c_void_p],
     ),
     "dips_batch_ids": (c_i32, [c_i64, c_i64, ctypes.c_uint64, c_i64, c_i64, c_void_p, c_void_p]),
     "dips_batch_ids_device": (c_i32, [c_i64, c_i64, c_i64, ctypes.c_uint64, c_i32, c_void_p, c_void_p, c_void_p]),
