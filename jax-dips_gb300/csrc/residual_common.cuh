@@ -7,8 +7,8 @@
 namespace dips {
 
 constexpr int kScanBlock = 1024;
-constexpr int kAdjThreads = 128;     // adjoint CTA: 4 warps
-constexpr int kAdjGrid = 152 * 3;    // three adjoint CTAs per SM (GB300 has 152 SMs)
+constexpr int kAdjThreads = 256;     // adjoint CTA: 8 warps
+constexpr int kAdjGrid = 152 * 2;    // two adjoint CTAs per SM (GB300 has 152 SMs)
 
 // ----------------------------------------------------------------------------------------
 // workspace
