@@ -29,32 +29,39 @@ static size_t carve(Workspace* w, char* base, int64_t B, int64_t max_jobs, int P
     return p;
   };
   Workspace W;
+  W.B = B;
   W.nblk = (B + kScanBlock - 1) / kScanBlock;
   W.nres = (B + 255) / 256;
   W.jcap = max_jobs + 64;
   W.grid = kAdjGrid;
+  W.fgrid = kFusedGrid;
   W.n_params = P;
   W.ctl = (Ctl*)take(sizeof(Ctl));
   W.cm = (int32_t*)take(sizeof(int32_t) * B);
   W.cp = (int32_t*)take(sizeof(int32_t) * B);
   W.om = (int64_t*)take(sizeof(int64_t) * B);
   W.op = (int64_t*)take(sizeof(int64_t) * B);
+  W.bk = (int32_t*)take(sizeof(int32_t) * B);
+  W.ob = (int64_t*)take(sizeof(int64_t) * B);
+  W.bulk = (int32_t*)take(sizeof(int32_t) * 2 * B);
   W.gs = (float*)take(sizeof(float) * B);
-  W.res = (float*)take(sizeof(float) * B);
-  W.blk = (int64_t*)take(sizeof(int64_t) * 2 * (W.nblk + 1));
+  W.blk = (int64_t*)take(sizeof(int64_t) * 4 * (W.nblk + 1));
   W.lossp = (double*)take(sizeof(double) * W.nres);
+  W.floss = (double*)take(sizeof(double) * 2 * W.fgrid);
   W.jslot = (int32_t*)take(sizeof(int32_t) * W.jcap);
   W.jcode = (uint16_t*)take(sizeof(uint16_t) * W.jcap);
   W.jA = (float*)take(sizeof(float) * W.jcap);
   W.ju = (float*)take(sizeof(float) * W.jcap);
-  W.partials = (float*)take(sizeof(float) * (size_t)W.grid * P);
+  W.jx = (float4*)take(sizeof(float4) * W.jcap);
+  W.jg = (float*)take(sizeof(float) * W.jcap);
+  W.partials = (float*)take(sizeof(float) * (size_t)(W.grid + W.fgrid) * P);
   W.grad = (float*)take(sizeof(float) * P);
   if (w) *w = W;
   return off;
 }
 
 // ----------------------------------------------------------------------------------------
-// expansion of a batch into jobs
+// expansion of a batch: bulk points into two slot lists, the others into jobs
 // ----------------------------------------------------------------------------------------
 template <typename T>
 __device__ __forceinline__ T warp_incl_scan(T v, int lane) {
@@ -66,81 +73,93 @@ __device__ __forceinline__ T warp_incl_scan(T v, int lane) {
   return v;
 }
 
-// exclusive block scan of two counters; returns block totals through *tot
-__device__ __forceinline__ void block_scan2(int64_t a, int64_t b, int64_t* ea, int64_t* eb, int64_t* ta, int64_t* tb) {
-  __shared__ int64_t wa[32], wb[32], tot[2];
+// exclusive block scan of four counters; block totals in tot
+__device__ __forceinline__ void block_scan4(const int64_t v[4], int64_t ex[4], int64_t tot[4]) {
+  __shared__ int64_t ws[4][32], ts[4];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  int64_t ia = warp_incl_scan(a, lane), ib = warp_incl_scan(b, lane);
-  if (lane == 31) {
-    wa[wid] = ia;
-    wb[wid] = ib;
+  int64_t inc[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    inc[k] = warp_incl_scan(v[k], lane);
+    if (lane == 31) ws[k][wid] = inc[k];
   }
   __syncthreads();
   if (wid == 0) {
-    int64_t va = lane < nw ? wa[lane] : 0, vb = lane < nw ? wb[lane] : 0;
-    int64_t sa = warp_incl_scan(va, lane), sb = warp_incl_scan(vb, lane);
-    if (lane < nw) {
-      wa[lane] = sa - va;
-      wb[lane] = sb - vb;
-    }
-    if (lane == nw - 1) {
-      tot[0] = sa;
-      tot[1] = sb;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int64_t a = lane < nw ? ws[k][lane] : 0;
+      const int64_t sa = warp_incl_scan(a, lane);
+      if (lane < nw) ws[k][lane] = sa - a;
+      if (lane == nw - 1) ts[k] = sa;
     }
   }
   __syncthreads();
-  *ea = wa[wid] + ia - a;
-  *eb = wb[wid] + ib - b;
-  *ta = tot[0];
-  *tb = tot[1];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    ex[k] = ws[k][wid] + inc[k] - v[k];
+    tot[k] = ts[k];
+  }
   __syncthreads();
 }
 
+// A point is "bulk" when it has exactly 7 jobs (its stencil points, no cube vertices) all of
+// one network; the fused kernel handles it.
 __global__ void k_count(const int32_t* __restrict__ ids, int64_t B, int64_t n_pts, const int32_t* __restrict__ cnt,
                         const int32_t* __restrict__ cnt_m, Workspace w) {
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int64_t a = 0, c = 0;
+  int64_t v[4] = {0, 0, 0, 0};  // bulk u-, bulk u+, general u- jobs, general u+ jobs
   if (b < B) {
     const int64_t pid = batch_pid(ids, b);
-    if (pid >= 0 && pid < n_pts) {  // an out-of-range id gets no jobs and a NaN residual
-      a = cnt_m[pid];
-      c = cnt[pid] - a;
+    int kind = 3;                   // an out-of-range id gets no work and a NaN residual
+    if (pid >= 0 && pid < n_pts) {
+      const int c = cnt[pid], m = cnt_m[pid];
+      if (c == kStencil && (m == kStencil || m == 0)) {
+        kind = m ? 1 : 2;
+        v[m ? 0 : 1] = 1;
+      } else {
+        kind = 0;
+        v[2] = m;
+        v[3] = c - m;
+      }
     }
-    w.cm[b] = (int32_t)a;
-    w.cp[b] = (int32_t)c;
+    w.bk[b] = kind;
+    w.cm[b] = (int32_t)v[2];
+    w.cp[b] = (int32_t)v[3];
   }
-  int64_t ea, eb, ta, tb;
-  block_scan2(a, c, &ea, &eb, &ta, &tb);
+  int64_t ex[4], tot[4];
+  block_scan4(v, ex, tot);
   if (b < B) {
-    w.om[b] = ea;
-    w.op[b] = eb;
+    w.ob[b] = v[0] ? ex[0] : ex[1];
+    w.om[b] = ex[2];
+    w.op[b] = ex[3];
   }
-  if (threadIdx.x == 0) {
-    w.blk[2 * blockIdx.x] = ta;
-    w.blk[2 * blockIdx.x + 1] = tb;
-  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 4; ++k) w.blk[4 * blockIdx.x + k] = tot[k];
 }
 
 __global__ void k_scan_blocks(Workspace w) {
-  int64_t carry_a = 0, carry_b = 0;
+  int64_t carry[4] = {0, 0, 0, 0};
   for (int64_t base = 0; base < w.nblk; base += blockDim.x) {
     const int64_t i = base + threadIdx.x;
-    const int64_t a = i < w.nblk ? w.blk[2 * i] : 0, b = i < w.nblk ? w.blk[2 * i + 1] : 0;
-    int64_t ea, eb, ta, tb;
-    block_scan2(a, b, &ea, &eb, &ta, &tb);
-    if (i < w.nblk) {
-      w.blk[2 * i] = ea + carry_a;
-      w.blk[2 * i + 1] = eb + carry_b;
-    }
-    carry_a += ta;
-    carry_b += tb;
+    int64_t v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = i < w.nblk ? w.blk[4 * i + k] : 0;
+    int64_t ex[4], tot[4];
+    block_scan4(v, ex, tot);
+    if (i < w.nblk)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) w.blk[4 * i + k] = ex[k] + carry[k];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) carry[k] += tot[k];
   }
   if (threadIdx.x == 0) {
-    const int64_t jm = carry_a, jp = carry_b;
+    const int64_t jm = carry[2], jp = carry[3];
     const int64_t jm_pad = (jm + 31) / 32 * 32;
     const bool over = jm_pad + jp > w.jcap;
     // on overflow no job is expanded or evaluated and every residual becomes NaN
     w.ctl->overflow = over ? 1 : 0;
+    w.ctl->nbm = over ? 0 : carry[0];
+    w.ctl->nbp = over ? 0 : carry[1];
     w.ctl->jm = over ? 0 : jm;
     w.ctl->jp = over ? 0 : jp;
     w.ctl->jm_pad = over ? 0 : jm_pad;
@@ -157,32 +176,42 @@ __global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, dips_records_
       w.jslot[j] = -1;
       w.jcode[j] = job_code(0, kCubeCentre, false);
       w.jA[j] = 0.0f;
+      w.jx[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      w.jg[j] = 0.0f;
     }
   }
   if (b >= B) return;
+  const int kind = w.bk[b];
+  if (kind == 3) return;
+  if (kind == 1 || kind == 2) {
+    const int net = kind - 1;
+    w.bulk[net * B + w.ob[b] + w.blk[4 * blockIdx.x + net]] = (int32_t)b;
+    return;
+  }
   const int64_t pid = batch_pid(ids, b);
-  const int64_t om = w.om[b] + w.blk[2 * blockIdx.x];
-  const int64_t op = w.op[b] + w.blk[2 * blockIdx.x + 1] + ctl.jm_pad;
+  const int64_t om = w.om[b] + w.blk[4 * blockIdx.x + 2];
+  const int64_t op = w.op[b] + w.blk[4 * blockIdx.x + 3] + ctl.jm_pad;
   w.om[b] = om;
   w.op[b] = op;
   const int cm = w.cm[b], cp = w.cp[b];
-  if (cm == 0 && cp == 0) return;
   const int64_t src_m = rec.job_off[pid];
   const int64_t src_p = rec.job_off[pid + 1] - cp;
-  for (int q = 0; q < cm; ++q) {
-    w.jslot[om + q] = (int32_t)b;
-    w.jcode[om + q] = rec.job_code[src_m + q];
-    w.jA[om + q] = rec.job_A[src_m + q];
-  }
-  for (int q = 0; q < cp; ++q) {
-    w.jslot[op + q] = (int32_t)b;
-    w.jcode[op + q] = rec.job_code[src_p + q];
-    w.jA[op + q] = rec.job_A[src_p + q];
+  const float p[3] = {rec.pts[3 * pid], rec.pts[3 * pid + 1], rec.pts[3 * pid + 2]};
+  for (int q = 0; q < cm + cp; ++q) {
+    const int64_t dst = q < cm ? om + q : op + (q - cm);
+    const int64_t src = q < cm ? src_m + q : src_p + (q - cm);
+    const uint16_t code = rec.job_code[src];
+    float x[3];
+    job_coords(p, rec.h, code, x);
+    w.jslot[dst] = (int32_t)b;
+    w.jcode[dst] = code;
+    w.jA[dst] = rec.job_A[src];
+    w.jx[dst] = make_float4(x[0], x[1], x[2], 0.0f);
   }
 }
 
 // ----------------------------------------------------------------------------------------
-// residual and loss per batch point
+// residual and loss of the general points
 // ----------------------------------------------------------------------------------------
 __device__ __forceinline__ double block_sum_d(double v) {
   __shared__ double ws[32];
@@ -206,31 +235,29 @@ __global__ void k_residual(const int32_t* __restrict__ ids, int64_t B, dips_reco
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool overflow = w.ctl->overflow != 0;
   double l = 0.0;
-  if (b < B && overflow) {
-    w.res[b] = nanf("");
-    w.gs[b] = 0.0f;
-    if (residual_out) residual_out[b] = nanf("");
-    l = nan("");
-  } else if (b < B && (batch_pid(ids, b) < 0 || batch_pid(ids, b) >= rec.n_pts)) {
-    w.res[b] = nanf("");
-    w.gs[b] = 0.0f;
-    if (residual_out) residual_out[b] = nanf("");
-    l = nan("");
-  } else if (b < B) {
-    const int64_t pid = batch_pid(ids, b);
-    float lhs = rec.lhs0[pid];
-    const int64_t om = w.om[b], op = w.op[b];
-    const int cm = w.cm[b], cp = w.cp[b];
-    for (int q = 0; q < cm; ++q) lhs = fmaf(w.jA[om + q], w.ju[om + q], lhs);
-    for (int q = 0; q < cp; ++q) lhs = fmaf(w.jA[op + q], w.ju[op + q], lhs);
-    const float diag = rec.diag[pid];
-    const float q = lhs / diag;
-    const float r = nan_to_num(q) - rec.rod[pid];
-    w.res[b] = r;
-    // d(mean 0.5 r^2)/d lhs; nan_to_num has zero derivative where lhs/diag is not finite
-    w.gs[b] = isfinite(q) ? (r / (float)B) / diag : 0.0f;
-    if (residual_out) residual_out[b] = r;
-    l = 0.5 * (double)r * (double)r;
+  if (b < B) {
+    const int kind = overflow ? 3 : w.bk[b];
+    if (kind == 3) {
+      if (residual_out) residual_out[b] = nanf("");
+      l = nan("");
+    } else if (kind == 0) {
+      const int64_t pid = batch_pid(ids, b);
+      float lhs = rec.lhs0[pid];
+      const int64_t om = w.om[b], op = w.op[b];
+      const int cm = w.cm[b], cp = w.cp[b];
+      for (int q = 0; q < cm; ++q) lhs = fmaf(w.jA[om + q], w.ju[om + q], lhs);
+      for (int q = 0; q < cp; ++q) lhs = fmaf(w.jA[op + q], w.ju[op + q], lhs);
+      const float diag = rec.diag[pid];
+      const float qv = lhs / diag;
+      const float r = nan_to_num(qv) - rec.rod[pid];
+      // d(mean 0.5 r^2)/d lhs; nan_to_num has zero derivative where lhs/diag is not finite
+      const float gs = isfinite(qv) ? (r / (float)B) / diag : 0.0f;
+      w.gs[b] = gs;
+      for (int q = 0; q < cm; ++q) w.jg[om + q] = gs * w.jA[om + q];
+      for (int q = 0; q < cp; ++q) w.jg[op + q] = gs * w.jA[op + q];
+      if (residual_out) residual_out[b] = r;
+      l = 0.5 * (double)r * (double)r;
+    }
   }
   const double t = block_sum_d(l);
   if (threadIdx.x == 0) w.lossp[blockIdx.x] = t;
@@ -239,6 +266,7 @@ __global__ void k_residual(const int32_t* __restrict__ ids, int64_t B, dips_reco
 __global__ void k_loss_final(Workspace w, int64_t B, double* __restrict__ loss_out) {
   double v = 0.0;
   for (int64_t i = threadIdx.x; i < w.nres; i += blockDim.x) v += w.lossp[i];
+  for (int64_t i = threadIdx.x; i < 2 * w.fgrid; i += blockDim.x) v += w.floss[i];
   const double t = block_sum_d(v);
   if (threadIdx.x == 0) *loss_out = t / (double)B;
 }
@@ -247,13 +275,10 @@ __global__ void k_grad_reduce(Workspace w, int P, float* __restrict__ grad_out) 
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P) return;
   float v = 0.0f;
-  for (int c = 0; c < w.grid; ++c) v += w.partials[(size_t)c * P + i];
+  for (int c = 0; c < w.grid + w.fgrid; ++c) v += w.partials[(size_t)c * P + i];
   grad_out[i] = v;
 }
 
-// ----------------------------------------------------------------------------------------
-// chained Adam (optax 0.1.5 semantics)
-// ----------------------------------------------------------------------------------------
 __global__ void k_adam(dips_adam_t hp, int P, float* __restrict__ params, const float* __restrict__ grad,
                        float* __restrict__ mu, float* __restrict__ nu, int64_t* __restrict__ count) {
   __shared__ float red[32];
@@ -421,23 +446,32 @@ static int prep_ws(const dips_arch_t* arch, int64_t B, void* ws, size_t ws_bytes
   return DIPS_OK;
 }
 
-static int run_forward(const ArchOps* ops, const float* params, const dips_records_t* rec, const int32_t* ids,
-                       int64_t B, Workspace& W, double* loss_out, float* residual_out, cudaStream_t s) {
-  int st = ops->load_params(params, s);
-  if (st) return st;
+static int expand(const dips_records_t* rec, const int32_t* ids, int64_t B, Workspace& W, cudaStream_t s) {
   const int nblk = (int)W.nblk;
   k_count<<<nblk, kScanBlock, 0, s>>>(ids, B, rec->n_pts, rec->cnt, rec->cnt_m, W);
   k_scan_blocks<<<1, kScanBlock, 0, s>>>(W);
   k_emit<<<nblk, kScanBlock, 0, s>>>(ids, B, *rec, W);
-  DIPS_CHECK_LAUNCH("job expansion");
-  st = ops->job_forward(make_ph(rec), ids, W, s);
-  if (st) return st;
-  k_residual<<<(int)W.nres, 256, 0, s>>>(ids, B, *rec, W, residual_out);
-  if (loss_out) k_loss_final<<<1, 256, 0, s>>>(W, B, loss_out);
-  DIPS_CHECK_LAUNCH("residual");
+  DIPS_CHECK_LAUNCH("batch expansion");
   return DIPS_OK;
 }
 
+// expansion, general forward + residual, fused bulk kernel (with or without its gradient)
+static int run_forward(const ArchOps* ops, const dips_records_t* rec, const int32_t* ids, int64_t B, Workspace& W,
+                       double* loss_out, float* residual_out, bool fused_bwd, cudaStream_t s) {
+  int st = expand(rec, ids, B, W, s);
+  if (st) return st;
+  st = ops->job_forward(make_ph(rec), ids, W, s);
+  if (st) return st;
+  k_residual<<<(int)W.nres, 256, 0, s>>>(ids, B, *rec, W, residual_out);
+  DIPS_CHECK_LAUNCH("residual");
+  st = ops->bulk_fused(make_ph(rec), ids, W, *rec, residual_out, fused_bwd, s);
+  if (st) return st;
+  if (loss_out) k_loss_final<<<1, 256, 0, s>>>(W, B, loss_out);
+  DIPS_CHECK_LAUNCH("loss");
+  return DIPS_OK;
+}
+
+// general adjoint and the reduction of all partial gradient rows
 static int run_backward(const ArchOps* ops, const dips_records_t* rec, const int32_t* ids, Workspace& W,
                         float* grad_out, cudaStream_t s) {
   int st = ops->job_adjoint(make_ph(rec), ids, W, s);
@@ -472,7 +506,9 @@ extern "C" int dips_residual_fwd(const dips_arch_t* arch, const float* params, c
   Workspace W;
   st = prep_ws(arch, batch, workspace, ws_bytes, &W);
   if (st) return st;
-  return run_forward(ops, params, rec, batch_ids, batch, W, loss_out, residual_out, stream);
+  st = ops->load_params(params, stream);
+  if (st) return st;
+  return run_forward(ops, rec, batch_ids, batch, W, loss_out, residual_out, false, stream);
 }
 
 extern "C" int dips_residual_bwd(const dips_arch_t* arch, const float* params, const dips_records_t* rec,
@@ -487,6 +523,9 @@ extern "C" int dips_residual_bwd(const dips_arch_t* arch, const float* params, c
   st = prep_ws(arch, batch, workspace, ws_bytes, &W);
   if (st) return st;
   st = ops->load_params(params, stream);
+  if (st) return st;
+  // the bulk points' gradient comes from the fused kernel, run again with its backward half
+  st = ops->bulk_fused(make_ph(rec), batch_ids, W, *rec, nullptr, true, stream);
   if (st) return st;
   return run_backward(ops, rec, batch_ids, W, grad_out, stream);
 }
@@ -512,7 +551,9 @@ extern "C" int dips_train_step(const dips_arch_t* arch, const dips_adam_t* hp, f
   Workspace W;
   st = prep_ws(arch, batch, workspace, ws_bytes, &W);
   if (st) return st;
-  st = run_forward(ops, params, rec, batch_ids, batch, W, loss_out, nullptr, stream);
+  st = ops->load_params(params, stream);
+  if (st) return st;
+  st = run_forward(ops, rec, batch_ids, batch, W, loss_out, nullptr, true, stream);
   if (st) return st;
   float* g = grad_out ? grad_out : W.grad;
   st = run_backward(ops, rec, batch_ids, W, g, stream);

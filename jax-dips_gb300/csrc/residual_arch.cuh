@@ -134,9 +134,10 @@ __device__ __forceinline__ void load_row(const float* buf, int e, float* v) {
   }
 }
 
-// forward of one job, staging x and every hidden activation in the warp tile row `lane`
-// (activations with act_tanh_bwd); returns the last hidden activation in h
-template <class N, int OFF>
+// forward of one job, staging x and every hidden activation in the warp tile row `lane`;
+// returns the last hidden activation in h.  ACC selects tanhf (the fused kernel, whose
+// activations also give the loss) or act_tanh_bwd (the adjoint's recompute).
+template <class N, int OFF, bool ACC>
 __device__ __forceinline__ void net_forward_stage(const float x[3], float* X, float* B, int lane, float h[N::kW]) {
   constexpr int W = N::kW, L = N::kL;
   *reinterpret_cast<float4*>(X + 4 * lane) = make_float4(x[0], x[1], x[2], 0.0f);
@@ -145,7 +146,7 @@ __device__ __forceinline__ void net_forward_stage(const float x[3], float* X, fl
     float z = 0.0f;
 #pragma unroll
     for (int i = 0; i < 3; ++i) z = fmaf(x[i], c_w[OFF + i * W + o], z);
-    h[o] = act_tanh_bwd(z + c_w[OFF + 3 * W + o]);
+    h[o] = ACC ? act_tanh(z + c_w[OFF + 3 * W + o]) : act_tanh_bwd(z + c_w[OFF + 3 * W + o]);
   }
   store_row<N>(B, lane, h);
 #pragma unroll
@@ -159,7 +160,7 @@ __device__ __forceinline__ void net_forward_stage(const float x[3], float* X, fl
 #pragma unroll
       for (int o = 0; o < W; ++o) t[o] = fmaf(h[i], c_w[off + i * W + o], t[o]);
 #pragma unroll
-    for (int o = 0; o < W; ++o) h[o] = act_tanh_bwd(t[o] + c_w[off + W * W + o]);
+    for (int o = 0; o < W; ++o) h[o] = ACC ? act_tanh(t[o] + c_w[off + W * W + o]) : act_tanh_bwd(t[o] + c_w[off + W * W + o]);
     store_row<N>(B + l * 32 * N::kRow, lane, h);
   }
 }
@@ -207,15 +208,15 @@ __device__ __forceinline__ void tile_gemm(const float* H, const float* D, float*
   atomicAdd(accb + o, sb);
 }
 
-// one tile of 32 jobs of network N: forward recompute, backpropagation of g, dW accumulation
+// Backward half of a tile whose activations are staged in `tile` (h = last hidden layer of
+// this lane's job, g = d loss / d u of this lane's job): output-layer grads, then for each
+// hidden layer the delta (thread per job, constant operands) and the dW warp GEMM.
 template <class N, int OFF, int BOFF>
-__device__ __forceinline__ void net_adjoint_tile(const float x[3], float g, float* tile, float* acc, int lane) {
+__device__ __forceinline__ void net_backward_tile(const float h[N::kW], float g, float* tile, float* acc, int lane) {
   constexpr int W = N::kW, L = N::kL, BUF = 32 * N::kRow;
   float* X = tile;
   float* B = tile + 32 * 4;
   float* gs = B + L * BUF;
-  float h[W];
-  net_forward_stage<N, OFF>(x, X, B, lane, h);
   gs[lane] = g;
   __syncwarp();
   // output layer u = sum_i Wo[i] h[i] + bo: dWo[i] += sum_e h[e][i] g[e] (lane = i)
@@ -270,14 +271,22 @@ __device__ __forceinline__ void net_adjoint_tile(const float x[3], float g, floa
   __syncwarp();
 }
 
+// one tile of 32 jobs of network N: forward recompute, backpropagation of g, dW accumulation
+template <class N, int OFF, int BOFF>
+__device__ __forceinline__ void net_adjoint_tile(const float x[3], float g, float* tile, float* acc, int lane) {
+  float h[N::kW];
+  net_forward_stage<N, OFF, false>(x, tile, tile + 32 * 4, lane, h);
+  net_backward_tile<N, OFF, BOFF>(h, g, tile, acc, lane);
+}
+
 template <class N, int OFF>
 __global__ void __launch_bounds__(256) k_job_forward(PtsH ph, const int32_t* __restrict__ ids, Workspace w, int net_p) {
   const Ctl ctl = *w.ctl;
   const int64_t begin = net_p ? ctl.jm_pad : 0;
   const int64_t end = net_p ? ctl.total : ctl.jm;
   for (int64_t j = begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < end; j += (int64_t)gridDim.x * blockDim.x) {
-    float x[3];
-    job_point(ph, ids, w.jslot[j], w.jcode[j], x);
+    const float4 xv = w.jx[j];
+    const float x[3] = {xv.x, xv.y, xv.z};
     w.ju[j] = net_forward<N, OFF>(x);
   }
 }
@@ -306,17 +315,99 @@ __global__ void __launch_bounds__(kThreads, 2) k_job_adjoint(PtsH ph, const int3
     float x[3] = {0.0f, 0.0f, 0.0f};
     float g = 0.0f;
     if (j < end) {
-      const int32_t slot = w.jslot[j];
-      if (slot >= 0) {
-        job_point(ph, ids, slot, w.jcode[j], x);
-        g = w.gs[slot] * w.jA[j];
-      }
+      const float4 xv = w.jx[j];
+      x[0] = xv.x;
+      x[1] = xv.y;
+      x[2] = xv.z;
+      g = w.jg[j];
     }
     net_adjoint_tile<N, OFF, BOFF>(x, g, tile, acc, lane);
   }
   __syncthreads();
   float* row = w.partials + (size_t)blockIdx.x * w.n_params + OFF;
   for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) row[i] = acc[i];
+}
+
+// ----------------------------------------------------------------------------------------
+// fused kernel for bulk points (7 jobs of one network: the stencil points)
+// ----------------------------------------------------------------------------------------
+// CTA = 7 warps; warp j evaluates stencil point j of 32 consecutive bulk points (lane = point).
+// One forward (tanhf) gives both the residual and the staged activations; the residual goes
+// through shared memory; with BWD the backward half of the adjoint tile follows.
+template <class N>
+constexpr size_t fused_smem_bytes() {
+  return sizeof(float) * ((size_t)(N::kParams + 3) / 4 * 4 + (size_t)kStencil * N::kTileFloats + kStencil * 32);
+}
+
+template <class N, int OFF, int BOFF, bool BWD>
+__global__ void __launch_bounds__(kFusedThreads, 2) k_bulk_fused(PtsH ph, const int32_t* __restrict__ ids, Workspace w,
+                                                                 dips_records_t rec, int net_p,
+                                                                 float* __restrict__ residual_out) {
+  constexpr int W = N::kW;
+  extern __shared__ float4 smem4[];
+  float* smem = reinterpret_cast<float*>(smem4);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;  // warp = stencil point
+  float* acc = smem;
+  float* tile = smem + (N::kParams + 3) / 4 * 4 + warp * N::kTileFloats;
+  float* sU = smem + (N::kParams + 3) / 4 * 4 + kStencil * N::kTileFloats;  // [7][32] A_j u_j
+  if (BWD)
+    for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) acc[i] = 0.0f;
+  __syncthreads();
+  const int64_t nb = net_p ? w.ctl->nbp : w.ctl->nbm;
+  const int32_t* list = w.bulk + (net_p ? w.B : 0);
+  const float Bf = (float)w.B;
+  double lsum = 0.0;
+  for (int64_t base = (int64_t)blockIdx.x * 32; base < nb; base += (int64_t)gridDim.x * 32) {
+    const int64_t idx = base + lane;
+    const bool valid = idx < nb;
+    const int32_t slot = valid ? list[idx] : 0;
+    const int64_t pid = valid ? batch_pid(ids, slot) : 0;
+    float x[3] = {0.0f, 0.0f, 0.0f};
+    float A = 0.0f;
+    if (valid) {
+      const float p[3] = {ph.pts[3 * pid], ph.pts[3 * pid + 1], ph.pts[3 * pid + 2]};
+      stencil_point(p, ph.h, warp, x);
+      const int64_t jb = net_p ? rec.job_off[pid + 1] - kStencil : rec.job_off[pid];
+#pragma unroll
+      for (int q = 0; q < kStencil; ++q)
+        if (job_stencil(rec.job_code[jb + q]) == warp) A = rec.job_A[jb + q];
+    }
+    float h[W];
+    net_forward_stage<N, OFF, true>(x, tile, tile + 32 * 4, lane, h);
+    float u = 0.0f;
+#pragma unroll
+    for (int i = 0; i < W; ++i) u = fmaf(h[i], c_w[OFF + N::kOut + i], u);
+    u += c_w[OFF + N::kOut + W];
+    sU[warp * 32 + lane] = valid ? A * u : 0.0f;
+    __syncthreads();
+    float gc = 0.0f;
+    if (valid) {
+      float lhs = rec.lhs0[pid];
+#pragma unroll
+      for (int j = 0; j < kStencil; ++j) lhs += sU[j * 32 + lane];
+      const float diag = rec.diag[pid];
+      const float qv = lhs / diag;
+      const float r = nan_to_num(qv) - rec.rod[pid];
+      gc = isfinite(qv) ? (r / Bf) / diag : 0.0f;
+      if (warp == 0) {
+        lsum += 0.5 * (double)r * (double)r;
+        if (residual_out) residual_out[slot] = r;
+      }
+    }
+    __syncthreads();  // sU is rewritten by the next group
+    if (BWD) net_backward_tile<N, OFF, BOFF>(h, gc * A, tile, acc, lane);
+  }
+  // loss partial of this CTA (warp 0 holds the sums)
+  if (warp == 0) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+    if (lane == 0) w.floss[net_p * w.fgrid + blockIdx.x] = lsum;
+  }
+  if (BWD) {
+    __syncthreads();
+    float* row = w.partials + (size_t)(w.grid + blockIdx.x) * w.n_params + OFF;
+    for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) row[i] = acc[i];
+  }
 }
 
 // ----------------------------------------------------------------------------------------
@@ -442,6 +533,36 @@ static int job_adjoint(const PtsH& ph, const int32_t* ids, const Workspace& w, c
   return DIPS_OK;
 }
 
+template <class N, int OFF, bool BWD>
+static int fused_launch(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
+                        float* residual_out, int net_p, cudaStream_t s) {
+  constexpr size_t bytes = fused_smem_bytes<N>();
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(k_bulk_fused<N, OFF, A::kParams, BWD>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(fused smem)");
+    attr_done = true;
+  }
+  k_bulk_fused<N, OFF, A::kParams, BWD><<<w.fgrid, kFusedThreads, bytes, s>>>(ph, ids, w, rec, net_p, residual_out);
+  return DIPS_OK;
+}
+
+static int bulk_fused(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
+                      float* residual_out, bool bwd, cudaStream_t s) {
+  int st;
+  if (bwd) {
+    st = fused_launch<typename A::M, 0, true>(ph, ids, w, rec, residual_out, 0, s);
+    if (!st) st = fused_launch<typename A::P, A::kOffP, true>(ph, ids, w, rec, residual_out, 1, s);
+  } else {
+    st = fused_launch<typename A::M, 0, false>(ph, ids, w, rec, residual_out, 0, s);
+    if (!st) st = fused_launch<typename A::P, A::kOffP, false>(ph, ids, w, rec, residual_out, 1, s);
+  }
+  if (st) return st;
+  DIPS_CHECK_LAUNCH("fused bulk kernel");
+  return DIPS_OK;
+}
+
 static int mlp_eval(const float* pts, const float* phi, int64_t n, float* u, float* g, cudaStream_t s) {
   int64_t grid = (n + 127) / 128;
   if (grid > 152 * 16) grid = 152 * 16;
@@ -454,8 +575,10 @@ static int mlp_eval(const float* pts, const float* phi, int64_t n, float* u, flo
 }  // namespace DIPS_NS
 
 const ArchOps* DIPS_GETTER() {
-  static const ArchOps ops = {DIPS_LM, DIPS_WM, DIPS_LP, DIPS_WP, DIPS_NS::A::kParams,
-                              DIPS_NS::load_params, DIPS_NS::job_forward, DIPS_NS::job_adjoint, DIPS_NS::mlp_eval};
+  static const ArchOps ops = {DIPS_LM,           DIPS_WM,          DIPS_LP,
+                              DIPS_WP,           DIPS_NS::A::kParams, DIPS_NS::load_params,
+                              DIPS_NS::job_forward, DIPS_NS::job_adjoint, DIPS_NS::bulk_fused,
+                              DIPS_NS::mlp_eval};
   return &ops;
 }
 

@@ -9,33 +9,43 @@ namespace dips {
 constexpr int kScanBlock = 1024;
 constexpr int kAdjThreads = 256;     // adjoint CTA: 8 warps
 constexpr int kAdjGrid = 152 * 2;    // two adjoint CTAs per SM (GB300 has 152 SMs)
+constexpr int kFusedThreads = 224;   // fused bulk CTA: one warp per stencil point
+constexpr int kFusedGrid = 152 * 2;
 
 // ----------------------------------------------------------------------------------------
 // workspace
 // ----------------------------------------------------------------------------------------
 struct Ctl {
-  int64_t jm, jp, jm_pad, total;
-  int64_t overflow;  // 1 when the batch's jobs exceed the workspace's job capacity
+  int64_t jm, jp, jm_pad, total;  // jobs of the general points: u-, u+, padded u- count, all
+  int64_t overflow;               // 1 when the batch's jobs exceed the workspace's job capacity
+  int64_t nbm, nbp;               // bulk points (7 jobs of one network) of the u- / u+ network
 };
 
+// Step workspace, carved from one caller-owned buffer.  Bulk points go to the fused kernel
+// through two slot lists; the other ("general") points are expanded into jobs.
 struct Workspace {
   Ctl* ctl;
-  int32_t* cm;
-  int32_t* cp;
-  int64_t* om;
-  int64_t* op;
-  float* gs;
-  float* res;
-  int64_t* blk;      // [2*nblk] block sums, then block offsets
-  double* lossp;     // [nres] loss partials
+  int32_t* cm;       // [B] general u- jobs of the slot
+  int32_t* cp;       // [B] general u+ jobs
+  int64_t* om;       // [B] first u- job
+  int64_t* op;       // [B] first u+ job
+  int32_t* bk;       // [B] 0 general, 1 bulk u-, 2 bulk u+, 3 invalid id
+  int64_t* ob;       // [B] position in its bulk list
+  int32_t* bulk;     // [2][B] bulk slot lists (u- then u+)
+  float* gs;         // [B] d loss / d lhs of general slots
+  int64_t* blk;      // [4*(nblk+1)] block sums, then block offsets
+  double* lossp;     // [nres] loss partials of general slots
+  double* floss;     // [2*fgrid] loss partials of the fused kernels
   int32_t* jslot;
   uint16_t* jcode;
   float* jA;
   float* ju;
-  float* partials;   // [grid][P]
+  float4* jx;        // [jcap] job coordinates (w unused)
+  float* jg;         // [jcap] d loss / d u of the job
+  float* partials;   // [2*grid][P]: rows [0, grid) general adjoint, [grid, 2*grid) fused
   float* grad;       // [P]
-  int64_t nblk, nres, jcap;
-  int grid;
+  int64_t nblk, nres, jcap, B;
+  int grid, fgrid;
   int n_params;      // row stride of partials
 };
 
@@ -60,6 +70,10 @@ struct ArchOps {
   int (*load_params)(const float* params, cudaStream_t s);
   int (*job_forward)(const PtsH& ph, const int32_t* ids, const Workspace& w, cudaStream_t s);
   int (*job_adjoint)(const PtsH& ph, const int32_t* ids, const Workspace& w, cudaStream_t s);
+  // bulk points: forward, residual, loss partials, residual_out (may be NULL) and, with bwd,
+  // the gradient partial rows
+  int (*bulk_fused)(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
+                    float* residual_out, bool bwd, cudaStream_t s);
   int (*mlp_eval)(const float* pts, const float* phi, int64_t n, float* u, float* g, cudaStream_t s);
 };
 
