@@ -36,6 +36,11 @@ UNIT = "residual_pts/s"
 ARCH = (3, 32, 3, 32)
 
 
+# DRAM bytes (read + write) of one launch of the dominant kernel at the default workload (128^3,
+# batch 2^18), from an ncu capture (dram__bytes_read.sum 110.22 MB + dram__bytes_write.sum 1.36 MB).
+FUSED_TRAFFIC = {(128, 1 << 18): 111_580_000}
+
+
 def net_flops(layers, width):
     """Forward FLOPs of one network evaluation: sum of 2*in*out + out per layer + one per tanh."""
     f = 2 * 3 * width + width
@@ -259,28 +264,27 @@ def run_ours(args, rank, world):
         torch.distributed.barrier()
     value = B * world * args.steps / t_total
 
-    # ---- dominant kernel (adjoint) timed live with CUDA events on the launching stream
+    # ---- every kernel of the step timed live with CUDA events at its phase boundaries, on the
+    # launching stream (dips_train_step_profiled), on a fixed uniform batch; L2 flushed before each
     ids_m = ops.batch_ids(lvl.n, B, epoch=0, batch_index=0, seed=123)
-    cnt = lvl.cnt[ids_m.long()].long()
-    cntm = lvl.cnt_m[ids_m.long()].long()
+    idl = ids_m.long()
+    cnt = lvl.cnt[idl].long()
+    cntm = lvl.cnt_m[idl].long()
     jobs_m, jobs_p = int(cntm.sum()), int((cnt - cntm).sum())
-    fwd_flops = jobs_m * net_flops(ARCH[0], ARCH[1]) + jobs_p * net_flops(ARCH[2], ARCH[3])
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-    t_fwd, t_adj = [], []
-    for _ in range(5):
+    bulk_m = int(((cnt == 7) & (cntm == 7)).sum())
+    bulk_p = int(((cnt == 7) & (cntm == 0)).sum())
+    f_m, f_p = net_flops(ARCH[0], ARCH[1]), net_flops(ARCH[2], ARCH[3])
+    fwd_flops = jobs_m * f_m + jobs_p * f_p
+    phases = []
+    for _ in range(7):
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(len(ops.STEP_PHASES) + 1)]
         flush.zero_()
-        ev[0].record()
-        l_, _, ws_ = ops.residual_forward(arch, params, lvl, ids_m, ws)
-        ev[1].record()
-        flush.zero_()
-        ev[2].record()
-        ops.residual_backward(arch, params, lvl, ids_m, ws)
-        ev[3].record()
+        ops.train_step_profiled(arch, params, opt, lvl, ids_m, ws, loss, evs)
         torch.cuda.synchronize()
-        t_fwd.append(ev[0].elapsed_time(ev[1]) / 1e3)
-        t_adj.append(ev[2].elapsed_time(ev[3]) / 1e3)
-    t_adj_med = statistics.median(t_adj)
-    t_fwd_med = statistics.median(t_fwd)
+        phases.append(ops.phase_ms(evs))
+    phase_med = {k: statistics.median(p[k] for p in phases) for k in ops.STEP_PHASES}
+    t_dom = phase_med["fused_p"] / 1e3
+    dom_flops = 3 * 7 * bulk_p * f_p  # forward + adjoint of the 7 stencil evaluations of each bulk u+ point
     # FP32 FMA peak of this GPU (measured)
     probe = torch.empty(152 * 16 * 256, dtype=torch.float32, device=dev)
     iters = 4096
@@ -291,8 +295,8 @@ def run_ours(args, rank, world):
     pe1.record()
     torch.cuda.synchronize()
     fp32_peak = 152 * 16 * 256 * 8 * 16 * iters * 2 / (pe0.elapsed_time(pe1) / 1e3) / 1e12
-    adj_tflops = 2 * fwd_flops / t_adj_med / 1e12
-    step_tflops = 3 * fwd_flops / (t_total / args.steps) / 1e12 * (1 if world == 1 else 1)
+    dom_tflops = dom_flops / t_dom / 1e12
+    step_tflops = 3 * fwd_flops / (t_total / args.steps) / 1e12
 
     # ---- e2e through the public API with host buffers
     host_ids = torch.empty(B, dtype=torch.int32).pin_memory()
@@ -344,16 +348,20 @@ def run_ours(args, rank, world):
                        "global_batch": B * world, "points": int(lvl.n), "jobs_per_step": jobs_m + jobs_p,
                        "l2": "flushed (256 MB write) between timed steps", "cuda_graph": world == 1,
                        "setup_s": setup_s, "wall_s_timed": wall},
-            "roofline": {"bound": "fp32", "kernel": "k_job_adjoint (recompute + backpropagation + dW)",
-                         "achieved": adj_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
-                         "frac": adj_tflops / fp32_peak, "traffic": None,
-                         "algorithmic": "2 x forward FLOPs per job (sum 2*in*out+out per layer + tanh count)",
-                         "peak_source": "measured FFMA probe (dips_fp32_fma_probe), not in MEASURED_PEAKS.json",
-                         "adjoint_ms": 1e3 * t_adj_med, "forward_ms": 1e3 * t_fwd_med,
-                         "step_tflops": step_tflops, "step_frac": step_tflops / fp32_peak},
+            "roofline": {"bound": "fp32", "kernel": "k_bulk_fused<u+ net, backward> (forward, residual, adjoint "
+                                                    "and dW of the points whose 7 stencil values come from the u+ net)",
+                         "achieved": dom_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": dom_tflops / fp32_peak, "traffic": FUSED_TRAFFIC.get((args.n, B)),
+                         "algorithmic": f"3 x F(u+) x 7 per bulk u+ point, F = sum(2*in*out+out) + tanh count = "
+                                        f"{f_p}; {bulk_p} bulk u+ points per launch",
+                         "peak_source": "measured FFMA probe (dips_fp32_fma_probe) in this run; "
+                                        "MEASURED_PEAKS.json has no FP32 figure",
+                         "phase_ms": phase_med,
+                         "step_tflops": step_tflops, "step_frac": step_tflops / fp32_peak,
+                         "step_algorithmic": "3 x F x (all jobs of the batch) per step"},
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "gpu_launches": 10 * args.steps,
+            "gpu_launches": 14 * args.steps,
             "clocks": clk,
             "time_to_target": tta,
         }

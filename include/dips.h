@@ -168,6 +168,16 @@ int dips_train_step(const dips_arch_t* arch, const dips_adam_t* hp, float* param
                     int64_t* count, const dips_records_t* rec, const int32_t* batch_ids, int64_t batch,
                     void* workspace, size_t ws_bytes, double* loss_out, float* grad_out,
                     cudaStream_t stream);
+/* Diagnostic form of dips_train_step: same work, plus events[i] (i < n_events; NULL entries
+   skipped) recorded on `stream` at the phase boundaries, so that each kernel can be timed live:
+   0 start, 1 batch expansion (count, scan, emit), 2 general forward u-, 3 general forward u+,
+   4 general residual, 5 fused bulk kernel u-, 6 fused bulk kernel u+, 7 loss, 8 general adjoint
+   u-, 9 general adjoint u+, 10 gradient reduction, 11 Adam.  No counterpart in the reference. */
+#define DIPS_STEP_EVENTS 12
+int dips_train_step_profiled(const dips_arch_t* arch, const dips_adam_t* hp, float* params, float* mu, float* nu,
+                             int64_t* count, const dips_records_t* rec, const int32_t* batch_ids, int64_t batch,
+                             void* workspace, size_t ws_bytes, double* loss_out, float* grad_out,
+                             cudaEvent_t* events, int32_t n_events, cudaStream_t stream);
 /* dips_train_step without a workspace argument, for callers that cannot allocate device
    memory (e.g. an XLA custom-call handler, which gets only the buffers XLA planned for it).
    No counterpart in the reference.  The scratch is a 64 MiB device array inside the library:

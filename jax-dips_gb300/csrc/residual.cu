@@ -446,38 +446,44 @@ static int prep_ws(const dips_arch_t* arch, int64_t B, void* ws, size_t ws_bytes
   return DIPS_OK;
 }
 
-static int expand(const dips_records_t* rec, const int32_t* ids, int64_t B, Workspace& W, cudaStream_t s) {
+static int expand(const dips_records_t* rec, const int32_t* ids, int64_t B, Workspace& W, const Marks* mk,
+                  cudaStream_t s) {
   const int nblk = (int)W.nblk;
+  mark(mk, kMarkStart, s);
   k_count<<<nblk, kScanBlock, 0, s>>>(ids, B, rec->n_pts, rec->cnt, rec->cnt_m, W);
   k_scan_blocks<<<1, kScanBlock, 0, s>>>(W);
   k_emit<<<nblk, kScanBlock, 0, s>>>(ids, B, *rec, W);
   DIPS_CHECK_LAUNCH("batch expansion");
+  mark(mk, kMarkExpand, s);
   return DIPS_OK;
 }
 
 // expansion, general forward + residual, fused bulk kernel (with or without its gradient)
 static int run_forward(const ArchOps* ops, const dips_records_t* rec, const int32_t* ids, int64_t B, Workspace& W,
-                       double* loss_out, float* residual_out, bool fused_bwd, cudaStream_t s) {
-  int st = expand(rec, ids, B, W, s);
+                       double* loss_out, float* residual_out, bool fused_bwd, const Marks* mk, cudaStream_t s) {
+  int st = expand(rec, ids, B, W, mk, s);
   if (st) return st;
-  st = ops->job_forward(make_ph(rec), ids, W, s);
+  st = ops->job_forward(make_ph(rec), ids, W, mk, s);
   if (st) return st;
   k_residual<<<(int)W.nres, 256, 0, s>>>(ids, B, *rec, W, residual_out);
   DIPS_CHECK_LAUNCH("residual");
-  st = ops->bulk_fused(make_ph(rec), ids, W, *rec, residual_out, fused_bwd, s);
+  mark(mk, kMarkResidual, s);
+  st = ops->bulk_fused(make_ph(rec), ids, W, *rec, residual_out, fused_bwd, mk, s);
   if (st) return st;
   if (loss_out) k_loss_final<<<1, 256, 0, s>>>(W, B, loss_out);
   DIPS_CHECK_LAUNCH("loss");
+  mark(mk, kMarkLoss, s);
   return DIPS_OK;
 }
 
 // general adjoint and the reduction of all partial gradient rows
 static int run_backward(const ArchOps* ops, const dips_records_t* rec, const int32_t* ids, Workspace& W,
-                        float* grad_out, cudaStream_t s) {
-  int st = ops->job_adjoint(make_ph(rec), ids, W, s);
+                        float* grad_out, const Marks* mk, cudaStream_t s) {
+  int st = ops->job_adjoint(make_ph(rec), ids, W, mk, s);
   if (st) return st;
   k_grad_reduce<<<div_up(ops->n_params, 256), 256, 0, s>>>(W, ops->n_params, grad_out);
   DIPS_CHECK_LAUNCH("gradient reduction");
+  mark(mk, kMarkReduce, s);
   return DIPS_OK;
 }
 
@@ -508,7 +514,7 @@ extern "C" int dips_residual_fwd(const dips_arch_t* arch, const float* params, c
   if (st) return st;
   st = ops->load_params(params, stream);
   if (st) return st;
-  return run_forward(ops, rec, batch_ids, batch, W, loss_out, residual_out, false, stream);
+  return run_forward(ops, rec, batch_ids, batch, W, loss_out, residual_out, false, nullptr, stream);
 }
 
 extern "C" int dips_residual_bwd(const dips_arch_t* arch, const float* params, const dips_records_t* rec,
@@ -525,9 +531,9 @@ extern "C" int dips_residual_bwd(const dips_arch_t* arch, const float* params, c
   st = ops->load_params(params, stream);
   if (st) return st;
   // the bulk points' gradient comes from the fused kernel, run again with its backward half
-  st = ops->bulk_fused(make_ph(rec), batch_ids, W, *rec, nullptr, true, stream);
+  st = ops->bulk_fused(make_ph(rec), batch_ids, W, *rec, nullptr, true, nullptr, stream);
   if (st) return st;
-  return run_backward(ops, rec, batch_ids, W, grad_out, stream);
+  return run_backward(ops, rec, batch_ids, W, grad_out, nullptr, stream);
 }
 
 extern "C" int dips_adam_step(const dips_arch_t* arch, const dips_adam_t* hp, float* params, const float* grad,
@@ -539,10 +545,10 @@ extern "C" int dips_adam_step(const dips_arch_t* arch, const dips_adam_t* hp, fl
   return DIPS_OK;
 }
 
-extern "C" int dips_train_step(const dips_arch_t* arch, const dips_adam_t* hp, float* params, float* mu, float* nu,
-                               int64_t* count, const dips_records_t* rec, const int32_t* batch_ids, int64_t batch,
-                               void* workspace, size_t ws_bytes, double* loss_out, float* grad_out,
-                               cudaStream_t stream) {
+static int train_step(const dips_arch_t* arch, const dips_adam_t* hp, float* params, float* mu, float* nu,
+                      int64_t* count, const dips_records_t* rec, const int32_t* batch_ids, int64_t batch,
+                      void* workspace, size_t ws_bytes, double* loss_out, float* grad_out, const Marks* mk,
+                      cudaStream_t stream) {
   int st = check_rec(rec, batch);
   if (st) return st;
   DIPS_REQUIRE(hp && params && mu && nu && count, DIPS_E_ARG, "dips_train_step: null pointer");
@@ -553,14 +559,34 @@ extern "C" int dips_train_step(const dips_arch_t* arch, const dips_adam_t* hp, f
   if (st) return st;
   st = ops->load_params(params, stream);
   if (st) return st;
-  st = run_forward(ops, rec, batch_ids, batch, W, loss_out, nullptr, true, stream);
+  st = run_forward(ops, rec, batch_ids, batch, W, loss_out, nullptr, true, mk, stream);
   if (st) return st;
   float* g = grad_out ? grad_out : W.grad;
-  st = run_backward(ops, rec, batch_ids, W, g, stream);
+  st = run_backward(ops, rec, batch_ids, W, g, mk, stream);
   if (st) return st;
   k_adam<<<1, 1024, 0, stream>>>(*hp, ops->n_params, params, g, mu, nu, count);
   DIPS_CHECK_LAUNCH("dips_train_step adam");
+  mark(mk, kMarkAdam, stream);
   return DIPS_OK;
+}
+
+extern "C" int dips_train_step(const dips_arch_t* arch, const dips_adam_t* hp, float* params, float* mu, float* nu,
+                               int64_t* count, const dips_records_t* rec, const int32_t* batch_ids, int64_t batch,
+                               void* workspace, size_t ws_bytes, double* loss_out, float* grad_out,
+                               cudaStream_t stream) {
+  return train_step(arch, hp, params, mu, nu, count, rec, batch_ids, batch, workspace, ws_bytes, loss_out, grad_out,
+                    nullptr, stream);
+}
+
+extern "C" int dips_train_step_profiled(const dips_arch_t* arch, const dips_adam_t* hp, float* params, float* mu,
+                                        float* nu, int64_t* count, const dips_records_t* rec,
+                                        const int32_t* batch_ids, int64_t batch, void* workspace, size_t ws_bytes,
+                                        double* loss_out, float* grad_out, cudaEvent_t* events, int32_t n_events,
+                                        cudaStream_t stream) {
+  DIPS_REQUIRE(events && n_events >= 0, DIPS_E_ARG, "dips_train_step_profiled: null event array");
+  const Marks mk = {events, n_events < kMarkCount ? n_events : (int)kMarkCount};
+  return train_step(arch, hp, params, mu, nu, count, rec, batch_ids, batch, workspace, ws_bytes, loss_out, grad_out,
+                    &mk, stream);
 }
 
 extern "C" int dips_batch_ids(int64_t n, int64_t epoch_index, uint64_t seed, int64_t batch_index, int64_t batch,

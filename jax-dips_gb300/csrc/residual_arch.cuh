@@ -503,9 +503,11 @@ static int load_params(const float* params, cudaStream_t s) {
   return e == cudaSuccess ? DIPS_OK : cuda_status(e, "cudaMemcpyToSymbolAsync(params)");
 }
 
-static int job_forward(const PtsH& ph, const int32_t* ids, const Workspace& w, cudaStream_t s) {
+static int job_forward(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s) {
   k_job_forward<typename A::M, 0><<<152 * 24, 256, 0, s>>>(ph, ids, w, 0);
+  mark(mk, kMarkFwdM, s);
   k_job_forward<typename A::P, A::kOffP><<<152 * 24, 256, 0, s>>>(ph, ids, w, 1);
+  mark(mk, kMarkFwdP, s);
   DIPS_CHECK_LAUNCH("job forward");
   return DIPS_OK;
 }
@@ -524,11 +526,13 @@ static int adjoint_launch(const PtsH& ph, const int32_t* ids, const Workspace& w
   return DIPS_OK;
 }
 
-static int job_adjoint(const PtsH& ph, const int32_t* ids, const Workspace& w, cudaStream_t s) {
+static int job_adjoint(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s) {
   int st = adjoint_launch<typename A::M, 0>(ph, ids, w, 0, s);
   if (st) return st;
+  mark(mk, kMarkAdjM, s);
   st = adjoint_launch<typename A::P, A::kOffP>(ph, ids, w, 1, s);
   if (st) return st;
+  mark(mk, kMarkAdjP, s);
   DIPS_CHECK_LAUNCH("job adjoint");
   return DIPS_OK;
 }
@@ -549,16 +553,19 @@ static int fused_launch(const PtsH& ph, const int32_t* ids, const Workspace& w, 
 }
 
 static int bulk_fused(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
-                      float* residual_out, bool bwd, cudaStream_t s) {
+                      float* residual_out, bool bwd, const Marks* mk, cudaStream_t s) {
   int st;
   if (bwd) {
     st = fused_launch<typename A::M, 0, true>(ph, ids, w, rec, residual_out, 0, s);
+    if (!st) mark(mk, kMarkFusedM, s);
     if (!st) st = fused_launch<typename A::P, A::kOffP, true>(ph, ids, w, rec, residual_out, 1, s);
   } else {
     st = fused_launch<typename A::M, 0, false>(ph, ids, w, rec, residual_out, 0, s);
+    if (!st) mark(mk, kMarkFusedM, s);
     if (!st) st = fused_launch<typename A::P, A::kOffP, false>(ph, ids, w, rec, residual_out, 1, s);
   }
   if (st) return st;
+  mark(mk, kMarkFusedP, s);
   DIPS_CHECK_LAUNCH("fused bulk kernel");
   return DIPS_OK;
 }

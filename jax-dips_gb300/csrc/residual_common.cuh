@@ -64,16 +64,41 @@ __device__ __forceinline__ void job_point(const PtsH& ph, const int32_t* ids, in
 
 // Kernels and launches of one DoubleMLP shape (one translation unit per shape, each with
 // its own constant-bank copy of the weights).
+// Optional CUDA events recorded on the launching stream at the step's phase boundaries
+// (slot numbers as in dips_train_step_profiled).  A null Marks pointer records nothing.
+struct Marks {
+  cudaEvent_t* ev;
+  int n;
+};
+enum MarkSlot {
+  kMarkStart = 0,
+  kMarkExpand,
+  kMarkFwdM,
+  kMarkFwdP,
+  kMarkResidual,
+  kMarkFusedM,
+  kMarkFusedP,
+  kMarkLoss,
+  kMarkAdjM,
+  kMarkAdjP,
+  kMarkReduce,
+  kMarkAdam,
+  kMarkCount
+};
+inline void mark(const Marks* m, int slot, cudaStream_t s) {
+  if (m && slot < m->n && m->ev[slot]) cudaEventRecord(m->ev[slot], s);
+}
+
 struct ArchOps {
   int m_layers, m_width, p_layers, p_width;
   int n_params;
   int (*load_params)(const float* params, cudaStream_t s);
-  int (*job_forward)(const PtsH& ph, const int32_t* ids, const Workspace& w, cudaStream_t s);
-  int (*job_adjoint)(const PtsH& ph, const int32_t* ids, const Workspace& w, cudaStream_t s);
+  int (*job_forward)(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s);
+  int (*job_adjoint)(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s);
   // bulk points: forward, residual, loss partials, residual_out (may be NULL) and, with bwd,
   // the gradient partial rows
   int (*bulk_fused)(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
-                    float* residual_out, bool bwd, cudaStream_t s);
+                    float* residual_out, bool bwd, const Marks* mk, cudaStream_t s);
   int (*mlp_eval)(const float* pts, const float* phi, int64_t n, float* u, float* g, cudaStream_t s);
 };
 

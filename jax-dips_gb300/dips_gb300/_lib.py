@@ -219,6 +219,11 @@ _SIGS = {
         [P(ArchT), P(AdamT), c_void_p, c_void_p, c_void_p, c_void_p, P(RecordsT), c_void_p, c_i64, c_void_p,
          ctypes.c_size_t, c_void_p, c_void_p, c_void_p],
     ),
+    "dips_train_step_profiled": (
+        c_i32,
+        [P(ArchT), P(AdamT), c_void_p, c_void_p, c_void_p, c_void_p, P(RecordsT), c_void_p, c_i64, c_void_p,
+         ctypes.c_size_t, c_void_p, c_void_p, c_void_p, c_i32, c_void_p],
+    ),
     "dips_train_step_noalloc": (
         c_i32,
         [P(ArchT), P(AdamT), c_void_p, c_void_p, c_void_p, c_void_p, P(RecordsT), c_void_p, c_i64, c_i64, c_void_p,

@@ -4,6 +4,8 @@
 
 from __future__ import annotations
 
+import ctypes
+
 import torch
 
 from . import _lib
@@ -103,6 +105,31 @@ def train_step(arch: Arch, params: torch.Tensor, opt: AdamState, level: FVLevel,
                                    _lib.ptr(opt.count), level.desc, _ids_ptr(batch_ids), B, _lib.ptr(ws.buf),
                                    ws.nbytes, _lib.ptr(loss_out), _lib.ptr(grad_out), _lib.stream_handle()),
                "dips_train_step")
+
+
+STEP_PHASES = ("expand", "forward_m", "forward_p", "residual", "fused_m", "fused_p", "loss", "adjoint_m",
+               "adjoint_p", "reduce", "adam")
+
+
+def train_step_profiled(arch: Arch, params: torch.Tensor, opt: AdamState, level: FVLevel, batch_ids,
+                        ws: StepWorkspace, loss_out: torch.Tensor, events):
+    """train_step with ``len(STEP_PHASES) + 1`` torch.cuda.Events recorded at the phase boundaries
+    on the current stream; returns nothing (read the events after a synchronise)."""
+    lib = _lib.load()
+    B = level.n if batch_ids is None else int(batch_ids.numel())
+    for e in events:  # creates the event and marks it recorded for torch; the library records it again
+        e.record()
+    arr = (ctypes.c_void_p * len(events))(*[e.cuda_event for e in events])
+    _lib.check(lib.dips_train_step_profiled(arch.ctype(), opt.hp, _lib.ptr(params), _lib.ptr(opt.mu),
+                                            _lib.ptr(opt.nu), _lib.ptr(opt.count), level.desc, _ids_ptr(batch_ids),
+                                            B, _lib.ptr(ws.buf), ws.nbytes, _lib.ptr(loss_out), None, arr,
+                                            len(events), _lib.stream_handle()),
+               "dips_train_step_profiled")
+
+
+def phase_ms(events):
+    """Milliseconds per phase from the events of one train_step_profiled call."""
+    return {name: events[i].elapsed_time(events[i + 1]) for i, name in enumerate(STEP_PHASES)}
 
 
 def batch_ids(n: int, batch: int, epoch: int, batch_index: int, seed: int = 0, out=None, device="cuda"):
