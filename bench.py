@@ -36,9 +36,9 @@ UNIT = "residual_pts/s"
 ARCH = (3, 32, 3, 32)
 
 
-# DRAM bytes (read + write) of one launch of the dominant kernel at the default workload (128^3,
-# batch 2^18), from an ncu capture (dram__bytes_read.sum 110.22 MB + dram__bytes_write.sum 1.36 MB).
-FUSED_TRAFFIC = {(128, 1 << 18): 111_580_000}
+# DRAM bytes (read + write) of one launch of the dominant kernel, keyed by (grid side, batch),
+# from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum); absent until captured.
+FUSED_TRAFFIC = {}
 
 
 def net_flops(layers, width):
@@ -284,7 +284,10 @@ def run_ours(args, rank, world):
         phases.append(ops.phase_ms(evs))
     phase_med = {k: statistics.median(p[k] for p in phases) for k in ops.STEP_PHASES}
     t_dom = phase_med["fused_p"] / 1e3
-    dom_flops = 3 * 7 * bulk_p * f_p  # forward + adjoint of the 7 stencil evaluations of each bulk u+ point
+    # the u+ launch runs forward + adjoint of every u+ job: the 7 stencil jobs of each bulk u+
+    # point and the u+ jobs of the other points (3 F per job; the general forward that feeds
+    # their residual is its own launch and not counted here)
+    dom_flops = 3 * jobs_p * f_p
     # FP32 FMA peak of this GPU (measured)
     probe = torch.empty(152 * 16 * 256, dtype=torch.float32, device=dev)
     iters = 4096
@@ -348,12 +351,12 @@ def run_ours(args, rank, world):
                        "global_batch": B * world, "points": int(lvl.n), "jobs_per_step": jobs_m + jobs_p,
                        "l2": "flushed (256 MB write) between timed steps", "cuda_graph": world == 1,
                        "setup_s": setup_s, "wall_s_timed": wall},
-            "roofline": {"bound": "fp32", "kernel": "k_bulk_fused<u+ net, backward> (forward, residual, adjoint "
-                                                    "and dW of the points whose 7 stencil values come from the u+ net)",
+            "roofline": {"bound": "fp32", "kernel": "tile::k_tile_net<u+ net, backward> (forward, bulk residual, "
+                                                    "adjoint and dW of every u+ job of the batch)",
                          "achieved": dom_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": dom_tflops / fp32_peak, "traffic": FUSED_TRAFFIC.get((args.n, B)),
-                         "algorithmic": f"3 x F(u+) x 7 per bulk u+ point, F = sum(2*in*out+out) + tanh count = "
-                                        f"{f_p}; {bulk_p} bulk u+ points per launch",
+                         "algorithmic": f"3 x F(u+) per u+ job, F = sum(2*in*out+out) + tanh count = {f_p}; "
+                                        f"{jobs_p} u+ jobs per launch ({bulk_p} bulk u+ points x 7 + general)",
                          "peak_source": "measured FFMA probe (dips_fp32_fma_probe) in this run; "
                                         "MEASURED_PEAKS.json has no FP32 figure",
                          "phase_ms": phase_med,

@@ -1,0 +1,483 @@
+// Register-blocked engine for width-32 networks with three hidden layers (DoubleMLP 3x32,
+// nn/mlp/MLP.py:93-139): residual, adjoint and weight gradient of the NBM loss
+// (solvers/poisson/trainer.py:783-789, :892-912) for bulk points and for general jobs.
+//
+// Included by residual_arch.cuh inside the per-shape namespace (after Net, Workspace, the
+// constant bank and act_tanh are defined).
+//
+// Work unit: one warp owns a tile of 32 jobs and runs it through the whole network with
+// __syncwarp only.  Every layer is a [32 jobs x 32] x [32 x 32] product computed as 4x8
+// register blocks: lane = jbl + 8*ob holds jobs 4*jbl..4*jbl+3 and features ob + 4t
+// (t = 0..7).  Activations and deltas sit in two warp-private shared buffers, feature-major
+// ([feature][job], row stride 36 floats, so that the blocked row loads of the weight-gradient
+// product are bank-conflict free).  The weights are copied once per CTA into shared memory,
+// permuted so that a lane's 8 features are contiguous (two float4 loads per k step); the
+// forward copies are pre-scaled by 2*log2(e), the argument scale of the exp2-based tanh.
+//
+// Per tile: forward (layer 1 from the job coordinates, layers 2 and 3 from the buffers),
+// u = w_o . h3 + b_o, then the loss gradient g of each job, then
+//   delta3 = g w_o (1 - h3^2)              -> buffer A (over h1)
+//   dW3 += h2^T delta3                     (register accumulators)
+//   delta2 = (delta3 W3^T) (1 - h2^2)      -> buffer B (over h2)
+//   h1 recomputed from x                   -> buffer A
+//   dW2 += h1^T delta2
+//   delta1 = (delta2 W2^T) (1 - h1^2);  dW1 += x^T delta1
+// The 32x32 weight gradients stay in registers for all tiles a warp processes (64 per lane);
+// bias, input-layer and output-layer gradients are reduce-scattered over the 8 lanes that share
+// a feature block and kept as one register each.  At the end the CTA adds its 12 warps'
+// accumulators into shared memory and writes one partial gradient row.
+//
+// Tiles: bulk tiles hold 4 bulk points x 7 stencil points (lanes 0..27; lane = 7*point +
+// stencil), whose residual is formed inside the warp from the 7 network values; general tiles
+// hold 32 consecutive jobs of the expanded job list with their coordinates and dL/du
+// precomputed (jx, jg).
+
+namespace tile {
+
+constexpr int kWarps = 12;
+constexpr int kThreads = 32 * kWarps;
+constexpr int kRS = 36;  // buffer row stride (floats)
+constexpr float kTanhScale = 2.8853900817779268f;  // 2 log2(e): tanh(z) = 1 - 2/(1 + 2^(kTanhScale z))
+
+template <class N>
+struct Layout {
+  static_assert(N::kW == 32 && N::kL == 3, "tile engine: 3 hidden layers of width 32");
+  static constexpr int W = 32;
+  // CTA-shared, permuted weights (floats)
+  static constexpr int kWF = 0;                 // [2][k = in 32][8*ob + t] = c * W_l[k][ob + 4t]
+  static constexpr int kWT = kWF + 2 * W * W;   // [2][k = out 32][8*ib + t] = W_l[ib + 4t][k]
+  static constexpr int kW1 = kWT + 2 * W * W;   // [3][8*ob + t] = c * W_1[c][ob + 4t]
+  static constexpr int kB = kW1 + 3 * W;        // [3][8*ob + t] = c * b_l[ob + 4t]
+  static constexpr int kWO = kB + 3 * W;        // [8*ob + t] = w_o[ob + 4t]
+  static constexpr int kShared = kWO + W;
+  // warp-private region
+  static constexpr int kX = 0;                  // [4][32] job coordinates (x, y, z, unused)
+  static constexpr int kA = kX + 4 * 32;        // [32][kRS]
+  static constexpr int kBB = kA + W * kRS;      // [32][kRS]
+  static constexpr int kG = kBB + W * kRS;      // [32] dL/du per job
+  static constexpr int kU = kG + 32;            // [32] A_j u_j of bulk tiles
+  static constexpr int kAv = kU + 32;           // [32] A_j of bulk tiles
+  static constexpr int kWarpFloats = kAv + 32;
+  static constexpr int kWarp0 = (kShared + 3) / 4 * 4;
+  static constexpr int kAcc = kWarp0 + kWarps * kWarpFloats;     // [kParams] CTA gradient accumulator
+  static constexpr int kLoss = (kAcc + N::kParams + 3) / 4 * 4;  // [kWarps] doubles
+  static constexpr size_t kBytes = sizeof(float) * (size_t)kLoss + sizeof(double) * kWarps;
+};
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float a, float b, float c, float d) {
+  *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+}
+
+// tanh of a pre-scaled argument y = 2 log2(e) z: 1 - 2/(1 + 2^y), hardware exp2 and
+// reciprocal approximations (the same arithmetic as act_tanh)
+__device__ __forceinline__ float tanh_scaled(float y) {
+  float e;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(y));
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(1.0f + e));
+  return fmaf(-2.0f, r, 1.0f);
+}
+
+// z[q][t] += sum_k A[k][jc + q] * Bm[k][bc + t] over k < K (A row stride AS, Bm row stride 32)
+template <int K, int AS>
+__device__ __forceinline__ void gemm48(float (&z)[4][8], const float* A, int jc, const float* Bm, int bc) {
+#pragma unroll 4
+  for (int k = 0; k < K; ++k) {
+    const float4 a = ld4(A + k * AS + jc);
+    const float4 b0 = ld4(Bm + k * 32 + bc), b1 = ld4(Bm + k * 32 + bc + 4);
+    const float av[4] = {a.x, a.y, a.z, a.w};
+    const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int t = 0; t < 8; ++t) z[q][t] = fmaf(av[q], bv[t], z[q][t]);
+  }
+}
+
+__device__ __forceinline__ void store_blk(float* buf, int ob, int jc, const float (&z)[4][8]) {
+#pragma unroll
+  for (int t = 0; t < 8; ++t) st4(buf + (ob + 4 * t) * kRS + jc, z[0][t], z[1][t], z[2][t], z[3][t]);
+}
+
+__device__ __forceinline__ void load_blk(const float* buf, int ob, int jc, float (&z)[4][8]) {
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {
+    const float4 v = ld4(buf + (ob + 4 * t) * kRS + jc);
+    z[0][t] = v.x;
+    z[1][t] = v.y;
+    z[2][t] = v.z;
+    z[3][t] = v.w;
+  }
+}
+
+__device__ __forceinline__ void fill_rows(float (&z)[4][8], const float* b) {
+  const float4 b0 = ld4(b), b1 = ld4(b + 4);
+  const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int t = 0; t < 8; ++t) z[q][t] = bv[t];
+}
+
+__device__ __forceinline__ void zero_blk(float (&z)[4][8]) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int t = 0; t < 8; ++t) z[q][t] = 0.0f;
+}
+
+__device__ __forceinline__ void tanh_blk(float (&z)[4][8]) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int t = 0; t < 8; ++t) z[q][t] = tanh_scaled(z[q][t]);
+}
+
+// z *= 1 - a^2 with a this lane's block of `buf`
+__device__ __forceinline__ void times_dtanh(float (&z)[4][8], const float* buf, int ob, int jc) {
+  float a[4][8];
+  load_blk(buf, ob, jc, a);
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int t = 0; t < 8; ++t) z[q][t] *= fmaf(-a[q][t], a[q][t], 1.0f);
+}
+
+// Reduce-scatter of v[0..7] over the 8 lanes that share lane bits 3..4: returns the sum of
+// v[jbl] over those lanes (jbl = lane bits 0..2).
+__device__ __forceinline__ float rs8(const float (&v)[8], int jbl) {
+  const bool b2 = jbl & 4, b1 = jbl & 2, b0 = jbl & 1;
+  float w[4], y[2];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float send = b2 ? v[q] : v[q + 4], keep = b2 ? v[q + 4] : v[q];
+    w[q] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const float send = b1 ? w[q] : w[q + 2], keep = b1 ? w[q + 2] : w[q];
+    y[q] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+  }
+  const float send = b0 ? y[0] : y[1], keep = b0 ? y[1] : y[0];
+  return keep + __shfl_xor_sync(0xffffffffu, send, 1);
+}
+
+// sum over this lane's 4 jobs, per feature
+__device__ __forceinline__ float colsum_rs(const float (&d)[4][8], int jbl) {
+  float v[8];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) v[t] = (d[0][t] + d[1][t]) + (d[2][t] + d[3][t]);
+  return rs8(v, jbl);
+}
+
+// acc[r][t] += sum over the tile's 32 jobs of H[row jbl + 8r][j] * D[row ob + 4t][j]
+__device__ __forceinline__ void dw48(float (&acc)[4][8], const float* H, const float* D, int jbl, int ob) {
+#pragma unroll 2
+  for (int s = 0; s < 8; ++s) {
+    float hv[4][4], dv[8][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const float4 v = ld4(H + (jbl + 8 * r) * kRS + 4 * s);
+      hv[r][0] = v.x;
+      hv[r][1] = v.y;
+      hv[r][2] = v.z;
+      hv[r][3] = v.w;
+    }
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const float4 v = ld4(D + (ob + 4 * t) * kRS + 4 * s);
+      dv[t][0] = v.x;
+      dv[t][1] = v.y;
+      dv[t][2] = v.z;
+      dv[t][3] = v.w;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int t = 0; t < 8; ++t) acc[r][t] = fmaf(hv[r][q], dv[t][q], acc[r][t]);
+  }
+}
+
+// Gradient accumulators of one warp (see the file comment for the lane ownership).
+struct Acc {
+  float w3[4][8], w2[4][8];          // dW3, dW2: rows jbl + 8r, columns ob + 4t
+  float wo, b3, b2, b1, w10, w11, w12;  // feature ob + 4*jbl of dWo, db3, db2, db1, dW1[0..2]
+  float bo;                          // dbo (lanes with ob == 0)
+};
+
+// One tile: forward of the 32 jobs whose coordinates are in X, then (with BWD) the backward
+// with dL/du from G.  EPI(u[4]) runs between the two: it receives this lane's 4 network
+// values (jobs jc..jc+3) and must leave G filled for the warp (it may synchronise the warp).
+template <class N, int OFF, bool BWD, class Epi>
+__device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc& acc, int lane, Epi epi) {
+  using Lay = Layout<N>;
+  const int jbl = lane & 7, ob = lane >> 3, jc = 4 * jbl, bc = 8 * ob;
+  float* X = wp + Lay::kX;
+  float* bufA = wp + Lay::kA;
+  float* bufB = wp + Lay::kBB;
+  float* G = wp + Lay::kG;
+  float h[4][8];
+  // layer 1: x -> bufA
+  fill_rows(h, sm + Lay::kB + bc);
+  gemm48<3, 32>(h, X, jc, sm + Lay::kW1, bc);
+  tanh_blk(h);
+  store_blk(bufA, ob, jc, h);
+  __syncwarp();
+  // layer 2: bufA -> bufB
+  fill_rows(h, sm + Lay::kB + 32 + bc);
+  gemm48<32, kRS>(h, bufA, jc, sm + Lay::kWF, bc);
+  tanh_blk(h);
+  store_blk(bufB, ob, jc, h);
+  __syncwarp();
+  // layer 3: bufB -> registers
+  fill_rows(h, sm + Lay::kB + 64 + bc);
+  gemm48<32, kRS>(h, bufB, jc, sm + Lay::kWF + 32 * 32, bc);
+  tanh_blk(h);
+  // output layer, reduced over the 4 feature blocks
+  const float4 wo0 = ld4(sm + Lay::kWO + bc), wo1 = ld4(sm + Lay::kWO + bc + 4);
+  const float wo[8] = {wo0.x, wo0.y, wo0.z, wo0.w, wo1.x, wo1.y, wo1.z, wo1.w};
+  const float bo = c_w[OFF + N::kOut + 32];
+  float u[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    float s = 0.0f;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) s = fmaf(h[q][t], wo[t], s);
+    s += __shfl_xor_sync(0xffffffffu, s, 8);
+    s += __shfl_xor_sync(0xffffffffu, s, 16);
+    u[q] = s + bo;
+  }
+  epi(u);
+  if (!BWD) {
+    __syncwarp();
+    return;
+  }
+  __syncwarp();
+  const float4 g4 = ld4(G + jc);
+  const float gv[4] = {g4.x, g4.y, g4.z, g4.w};
+  {
+    float v[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) v[t] = fmaf(gv[0], h[0][t], gv[1] * h[1][t]) + fmaf(gv[2], h[2][t], gv[3] * h[3][t]);
+    acc.wo += rs8(v, jbl);
+    float gs = (gv[0] + gv[1]) + (gv[2] + gv[3]);
+    gs += __shfl_xor_sync(0xffffffffu, gs, 1);
+    gs += __shfl_xor_sync(0xffffffffu, gs, 2);
+    gs += __shfl_xor_sync(0xffffffffu, gs, 4);
+    acc.bo += gs;
+  }
+  // delta3 = g w_o (1 - h3^2) over h1
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int t = 0; t < 8; ++t) h[q][t] = gv[q] * wo[t] * fmaf(-h[q][t], h[q][t], 1.0f);
+  acc.b3 += colsum_rs(h, jbl);
+  store_blk(bufA, ob, jc, h);
+  __syncwarp();
+  dw48(acc.w3, bufB, bufA, jbl, ob);
+  // delta2 = (delta3 W3^T) (1 - h2^2) over h2
+  zero_blk(h);
+  gemm48<32, kRS>(h, bufA, jc, sm + Lay::kWT + 32 * 32, bc);
+  times_dtanh(h, bufB, ob, jc);
+  acc.b2 += colsum_rs(h, jbl);
+  __syncwarp();
+  store_blk(bufB, ob, jc, h);
+  {  // h1 again, over delta3
+    float h1[4][8];
+    fill_rows(h1, sm + Lay::kB + bc);
+    gemm48<3, 32>(h1, X, jc, sm + Lay::kW1, bc);
+    tanh_blk(h1);
+    store_blk(bufA, ob, jc, h1);
+  }
+  __syncwarp();
+  dw48(acc.w2, bufA, bufB, jbl, ob);
+  // delta1 = (delta2 W2^T) (1 - h1^2)
+  zero_blk(h);
+  gemm48<32, kRS>(h, bufB, jc, sm + Lay::kWT, bc);
+  times_dtanh(h, bufA, ob, jc);
+  acc.b1 += colsum_rs(h, jbl);
+  {
+    const float4 x0 = ld4(X + jc), x1 = ld4(X + 32 + jc), x2 = ld4(X + 64 + jc);
+    float v[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) v[t] = fmaf(x0.x, h[0][t], fmaf(x0.y, h[1][t], fmaf(x0.z, h[2][t], x0.w * h[3][t])));
+    acc.w10 += rs8(v, jbl);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) v[t] = fmaf(x1.x, h[0][t], fmaf(x1.y, h[1][t], fmaf(x1.z, h[2][t], x1.w * h[3][t])));
+    acc.w11 += rs8(v, jbl);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) v[t] = fmaf(x2.x, h[0][t], fmaf(x2.y, h[1][t], fmaf(x2.z, h[2][t], x2.w * h[3][t])));
+    acc.w12 += rs8(v, jbl);
+  }
+  __syncwarp();  // the next tile overwrites X, G and both buffers
+}
+
+// Copy network N's weights (flat layout at params + OFF) into the CTA's permuted tables.
+template <class N, int OFF>
+__device__ __forceinline__ void load_weights(float* sm) {
+  using Lay = Layout<N>;
+  const float c = kTanhScale;
+  for (int e = threadIdx.x; e < 2 * 32 * 32; e += blockDim.x) {
+    const int l = e >> 10, r = e & 1023, k = r >> 5, col = r & 31, hi = col >> 3, t = col & 7;
+    const int off = OFF + N::layer_off(l + 1);
+    sm[Lay::kWF + e] = c * c_w[off + k * 32 + hi + 4 * t];
+    sm[Lay::kWT + e] = c_w[off + (hi + 4 * t) * 32 + k];
+  }
+  for (int e = threadIdx.x; e < 3 * 32; e += blockDim.x) {
+    const int row = e >> 5, col = e & 31, f = (col >> 3) + 4 * (col & 7);
+    sm[Lay::kW1 + e] = c * c_w[OFF + row * 32 + f];
+    sm[Lay::kB + e] = c * c_w[OFF + N::layer_off(row) + (row == 0 ? 3 : 32) * 32 + f];
+  }
+  for (int e = threadIdx.x; e < 32; e += blockDim.x) sm[Lay::kWO + e] = c_w[OFF + N::kOut + (e >> 3) + 4 * (e & 7)];
+}
+
+// Add a warp's accumulators into the CTA accumulator (flat layout of network N).
+template <class N>
+__device__ __forceinline__ void flush_acc(float* cta, const Acc& a, int lane) {
+  const int jbl = lane & 7, ob = lane >> 3, f = ob + 4 * jbl;
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int cell = (jbl + 8 * r) * 32 + ob + 4 * t;
+      atomicAdd(cta + N::layer_off(2) + cell, a.w3[r][t]);
+      atomicAdd(cta + N::layer_off(1) + cell, a.w2[r][t]);
+    }
+  atomicAdd(cta + N::kOut + f, a.wo);
+  atomicAdd(cta + N::layer_off(2) + 32 * 32 + f, a.b3);
+  atomicAdd(cta + N::layer_off(1) + 32 * 32 + f, a.b2);
+  atomicAdd(cta + 3 * 32 + f, a.b1);
+  atomicAdd(cta + 0 * 32 + f, a.w10);
+  atomicAdd(cta + 1 * 32 + f, a.w11);
+  atomicAdd(cta + 2 * 32 + f, a.w12);
+  if (lane == 0) atomicAdd(cta + N::kOut + 32, a.bo);
+}
+
+// One launch per network: bulk tiles (4 points x 7 stencil jobs, residual and loss formed in
+// the warp) and, with BWD, general tiles (32 jobs of the job list).  Writes the loss partial
+// floss[net_p][blockIdx.x] (and zeros the rest of that row of slots), residual_out of the bulk
+// slots, and with BWD the partial gradient row blockIdx.x (columns of this network).
+template <class N, int OFF, bool BWD>
+__global__ void __launch_bounds__(kThreads, 1) k_tile_net(PtsH ph, const int32_t* __restrict__ ids, Workspace w,
+                                                          dips_records_t rec, int net_p, float* __restrict__ residual_out) {
+  using Lay = Layout<N>;
+  extern __shared__ float4 smem4[];
+  float* sm = reinterpret_cast<float*>(smem4);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  load_weights<N, OFF>(sm);
+  if (BWD)
+    for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) sm[Lay::kAcc + i] = 0.0f;
+  __syncthreads();
+  float* wp = sm + Lay::kWarp0 + warp * Lay::kWarpFloats;
+  float* X = wp + Lay::kX;
+  float* G = wp + Lay::kG;
+  float* U = wp + Lay::kU;
+  float* Av = wp + Lay::kAv;
+  Acc acc;
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int t = 0; t < 8; ++t) acc.w3[r][t] = acc.w2[r][t] = 0.0f;
+  acc.wo = acc.b3 = acc.b2 = acc.b1 = acc.w10 = acc.w11 = acc.w12 = acc.bo = 0.0f;
+
+  const Ctl ctl = *w.ctl;
+  const int64_t nb = net_p ? ctl.nbp : ctl.nbm;
+  const int32_t* list = w.bulk + (net_p ? w.B : 0);
+  const int64_t jbeg = net_p ? ctl.jm_pad : 0;
+  const int64_t jend = net_p ? ctl.total : ctl.jm;
+  const int64_t nbt = (nb + 3) / 4;
+  const int64_t ngt = BWD ? (jend - jbeg + 31) / 32 : 0;
+  const float Bf = (float)w.B;
+  const int jc = 4 * (lane & 7);
+  const bool lead = (lane >> 3) == 0;  // lanes holding u of jobs jc..jc+3 after the reduction
+  double lsum = 0.0;
+
+  for (int64_t tile = (int64_t)blockIdx.x * kWarps + warp; tile < nbt + ngt; tile += (int64_t)gridDim.x * kWarps) {
+    if (tile < nbt) {
+      // ---- bulk tile: lane = 7 * point + stencil point
+      const int pl = lane / kStencil, s = lane - kStencil * pl;
+      const int64_t idx = tile * 4 + pl;
+      float x[3] = {0.0f, 0.0f, 0.0f};
+      float A = 0.0f;
+      if (lane < 4 * kStencil && idx < nb) {
+        const int64_t pid = batch_pid(ids, list[idx]);
+        const float p[3] = {ph.pts[3 * pid], ph.pts[3 * pid + 1], ph.pts[3 * pid + 2]};
+        stencil_point(p, ph.h, s, x);
+        const int64_t jb = net_p ? rec.job_off[pid + 1] - kStencil : rec.job_off[pid];
+#pragma unroll
+        for (int q = 0; q < kStencil; ++q)
+          if (job_stencil(rec.job_code[jb + q]) == s) A = rec.job_A[jb + q];
+      }
+      X[lane] = x[0];
+      X[32 + lane] = x[1];
+      X[64 + lane] = x[2];
+      Av[lane] = A;
+      __syncwarp();
+      run_tile<N, OFF, BWD>(sm, wp, acc, lane, [&](const float (&u)[4]) {
+        if (lead) st4(U + jc, u[0] * Av[jc], u[1] * Av[jc + 1], u[2] * Av[jc + 2], u[3] * Av[jc + 3]);
+        __syncwarp();
+        // lanes 0..3: residual of point `lane`; then dL/du of its 7 jobs
+        if (lane < 4) {
+          const int64_t pidx = tile * 4 + lane;
+          float gc = 0.0f;
+          if (pidx < nb) {
+            const int32_t sl = list[pidx];
+            const int64_t pp = batch_pid(ids, sl);
+            float lhs = rec.lhs0[pp];
+#pragma unroll
+            for (int q = 0; q < kStencil; ++q) lhs += U[kStencil * lane + q];
+            const float diag = rec.diag[pp];
+            const float qv = lhs / diag;
+            const float r = nan_to_num(qv) - rec.rod[pp];
+            gc = isfinite(qv) ? (r / Bf) / diag : 0.0f;
+            lsum += 0.5 * (double)r * (double)r;
+            if (residual_out) residual_out[sl] = r;
+          }
+          if (BWD) {
+#pragma unroll
+            for (int q = 0; q < kStencil; ++q) G[kStencil * lane + q] = gc * Av[kStencil * lane + q];
+          }
+        }
+        if (BWD && lane >= 28) G[lane] = 0.0f;
+      });
+    } else {
+      // ---- general tile: 32 jobs of the job list
+      const int64_t j = jbeg + (tile - nbt) * 32 + lane;
+      float4 xv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      float g = 0.0f;
+      if (j < jend) {
+        xv = w.jx[j];
+        g = w.jg[j];
+      }
+      X[lane] = xv.x;
+      X[32 + lane] = xv.y;
+      X[64 + lane] = xv.z;
+      G[lane] = g;
+      __syncwarp();
+      run_tile<N, OFF, BWD>(sm, wp, acc, lane, [](const float (&)[4]) {});
+    }
+  }
+  // loss partial of the CTA
+  double* wl = reinterpret_cast<double*>(sm + Lay::kLoss);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+  if (lane == 0) wl[warp] = lsum;
+  if (BWD) flush_acc<N>(sm + Lay::kAcc, acc, lane);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < kWarps; ++q) t += wl[q];
+    w.floss[net_p * w.fgrid + blockIdx.x] = t;
+  }
+  if (blockIdx.x == 0)  // the loss slots beyond this grid (sized for the per-job-thread kernels)
+    for (int i = gridDim.x + threadIdx.x; i < w.fgrid; i += blockDim.x) w.floss[net_p * w.fgrid + i] = 0.0;
+  if (BWD) {
+    float* row = w.partials + (size_t)blockIdx.x * w.n_params + OFF;
+    for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) row[i] = sm[Lay::kAcc + i];
+  }
+}
+
+}  // namespace tile

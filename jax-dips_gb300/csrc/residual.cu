@@ -271,11 +271,14 @@ __global__ void k_loss_final(Workspace w, int64_t B, double* __restrict__ loss_o
   if (threadIdx.x == 0) *loss_out = t / (double)B;
 }
 
-__global__ void k_grad_reduce(Workspace w, int P, float* __restrict__ grad_out) {
+// columns [0, Pm) belong to the u- network; rows_m / rows_p partial rows hold each network's
+// gradient (kTileGrid for the register-blocked engine, grid + fgrid otherwise)
+__global__ void k_grad_reduce(Workspace w, int P, int Pm, int rows_m, int rows_p, float* __restrict__ grad_out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P) return;
+  const int rows = i < Pm ? rows_m : rows_p;
   float v = 0.0f;
-  for (int c = 0; c < w.grid + w.fgrid; ++c) v += w.partials[(size_t)c * P + i];
+  for (int c = 0; c < rows; ++c) v += w.partials[(size_t)c * P + i];
   grad_out[i] = v;
 }
 
@@ -402,10 +405,11 @@ static const ArchOps* find_arch(const dips_arch_t* a) {
   return nullptr;
 }
 
+static int net_params(int L, int W) { return 3 * W + W + (L - 1) * (W * W + W) + W + 1; }
+
 static int arch_params(const dips_arch_t* a) {
   if (!a || a->m_layers < 1 || a->p_layers < 1 || a->m_width < 1 || a->p_width < 1) return -1;
-  auto np = [](int L, int W) { return 3 * W + W + (L - 1) * (W * W + W) + W + 1; };
-  return np(a->m_layers, a->m_width) + np(a->p_layers, a->p_width);
+  return net_params(a->m_layers, a->m_width) + net_params(a->p_layers, a->p_width);
 }
 
 static int check_rec(const dips_records_t* rec, int64_t B) {
@@ -481,7 +485,10 @@ static int run_backward(const ArchOps* ops, const dips_records_t* rec, const int
                         float* grad_out, const Marks* mk, cudaStream_t s) {
   int st = ops->job_adjoint(make_ph(rec), ids, W, mk, s);
   if (st) return st;
-  k_grad_reduce<<<div_up(ops->n_params, 256), 256, 0, s>>>(W, ops->n_params, grad_out);
+  const int Pm = ops->n_params - net_params(ops->p_layers, ops->p_width);
+  const int legacy_rows = W.grid + W.fgrid;
+  k_grad_reduce<<<div_up(ops->n_params, 256), 256, 0, s>>>(W, ops->n_params, Pm, ops->tile_m ? kTileGrid : legacy_rows,
+                                                           ops->tile_p ? kTileGrid : legacy_rows, grad_out);
   DIPS_CHECK_LAUNCH("gradient reduction");
   mark(mk, kMarkReduce, s);
   return DIPS_OK;

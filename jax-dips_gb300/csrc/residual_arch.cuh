@@ -26,14 +26,12 @@ static __constant__ float c_w[kMaxConstParams];
 constexpr int kThreads = kAdjThreads;
 constexpr int kWarps = kThreads / 32;
 
-// tanh of the forward pass (the loss): CUDA's tanhf.
-__device__ __forceinline__ float act_tanh(float x) { return tanhf(x); }
-
-// tanh of the adjoint's activation recompute: 1 - 2/(1 + e^{2x}) with the hardware exp2 and
-// reciprocal approximations (relative error <= 2^-22 each), absolute error below 3e-7.  It
-// only perturbs the gradient, by about 1e-6 relative -- two orders below the 1e-4 gradient bar --
-// and costs 3 FMA-pipe and 2 MUFU instructions instead of tanhf's polynomial-and-branch code.
-__device__ __forceinline__ float act_tanh_bwd(float x) {
+// tanh: 1 - 2/(1 + e^{2x}) with the hardware exp2 and reciprocal approximations (relative
+// error <= 2^-22 each); absolute error below 3e-7, the size of the FP32 rounding of the
+// activations themselves.  Against the oracle's tanh it moves the loss by < 1e-7 and the
+// gradient by < 3e-6 relative (measured on the parity cases), and it costs three FMA-pipe
+// and two MUFU instructions.
+__device__ __forceinline__ float act_tanh(float x) {
   float e;
   asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(x * 2.8853900817779268f));  // e^{2x}
   float r;
@@ -70,6 +68,8 @@ struct Arch {
   static constexpr int kOffP = M::kParams;
   static constexpr int kParams = M::kParams + P::kParams;
 };
+
+#include "mlp_tile.cuh"
 
 // forward, activations discarded
 template <class N, int OFF>
@@ -135,9 +135,8 @@ __device__ __forceinline__ void load_row(const float* buf, int e, float* v) {
 }
 
 // forward of one job, staging x and every hidden activation in the warp tile row `lane`;
-// returns the last hidden activation in h.  ACC selects tanhf (the fused kernel, whose
-// activations also give the loss) or act_tanh_bwd (the adjoint's recompute).
-template <class N, int OFF, bool ACC>
+// returns the last hidden activation in h.
+template <class N, int OFF>
 __device__ __forceinline__ void net_forward_stage(const float x[3], float* X, float* B, int lane, float h[N::kW]) {
   constexpr int W = N::kW, L = N::kL;
   *reinterpret_cast<float4*>(X + 4 * lane) = make_float4(x[0], x[1], x[2], 0.0f);
@@ -146,7 +145,7 @@ __device__ __forceinline__ void net_forward_stage(const float x[3], float* X, fl
     float z = 0.0f;
 #pragma unroll
     for (int i = 0; i < 3; ++i) z = fmaf(x[i], c_w[OFF + i * W + o], z);
-    h[o] = ACC ? act_tanh(z + c_w[OFF + 3 * W + o]) : act_tanh_bwd(z + c_w[OFF + 3 * W + o]);
+    h[o] = act_tanh(z + c_w[OFF + 3 * W + o]);
   }
   store_row<N>(B, lane, h);
 #pragma unroll
@@ -160,7 +159,7 @@ __device__ __forceinline__ void net_forward_stage(const float x[3], float* X, fl
 #pragma unroll
       for (int o = 0; o < W; ++o) t[o] = fmaf(h[i], c_w[off + i * W + o], t[o]);
 #pragma unroll
-    for (int o = 0; o < W; ++o) h[o] = ACC ? act_tanh(t[o] + c_w[off + W * W + o]) : act_tanh_bwd(t[o] + c_w[off + W * W + o]);
+    for (int o = 0; o < W; ++o) h[o] = act_tanh(t[o] + c_w[off + W * W + o]);
     store_row<N>(B + l * 32 * N::kRow, lane, h);
   }
 }
@@ -275,7 +274,7 @@ __device__ __forceinline__ void net_backward_tile(const float h[N::kW], float g,
 template <class N, int OFF, int BOFF>
 __device__ __forceinline__ void net_adjoint_tile(const float x[3], float g, float* tile, float* acc, int lane) {
   float h[N::kW];
-  net_forward_stage<N, OFF, false>(x, tile, tile + 32 * 4, lane, h);
+  net_forward_stage<N, OFF>(x, tile, tile + 32 * 4, lane, h);
   net_backward_tile<N, OFF, BOFF>(h, g, tile, acc, lane);
 }
 
@@ -332,7 +331,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_job_adjoint(PtsH ph, const int3
 // fused kernel for bulk points (7 jobs of one network: the stencil points)
 // ----------------------------------------------------------------------------------------
 // CTA = 7 warps; warp j evaluates stencil point j of 32 consecutive bulk points (lane = point).
-// One forward (tanhf) gives both the residual and the staged activations; the residual goes
+// One forward gives both the residual and the staged activations; the residual goes
 // through shared memory; with BWD the backward half of the adjoint tile follows.
 template <class N>
 constexpr size_t fused_smem_bytes() {
@@ -373,7 +372,7 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_bulk_fused(PtsH ph, const 
         if (job_stencil(rec.job_code[jb + q]) == warp) A = rec.job_A[jb + q];
     }
     float h[W];
-    net_forward_stage<N, OFF, true>(x, tile, tile + 32 * 4, lane, h);
+    net_forward_stage<N, OFF>(x, tile, tile + 32 * 4, lane, h);
     float u = 0.0f;
 #pragma unroll
     for (int i = 0; i < W; ++i) u = fmaf(h[i], c_w[OFF + N::kOut + i], u);
@@ -526,11 +525,18 @@ static int adjoint_launch(const PtsH& ph, const int32_t* ids, const Workspace& w
   return DIPS_OK;
 }
 
+template <class N>
+constexpr bool uses_tile() {
+  return N::kW == 32 && N::kL == 3;
+}
+
 static int job_adjoint(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s) {
-  int st = adjoint_launch<typename A::M, 0>(ph, ids, w, 0, s);
+  // networks on the register-blocked engine had their general jobs done by the bulk launch
+  int st = DIPS_OK;
+  if constexpr (!uses_tile<typename A::M>()) st = adjoint_launch<typename A::M, 0>(ph, ids, w, 0, s);
   if (st) return st;
   mark(mk, kMarkAdjM, s);
-  st = adjoint_launch<typename A::P, A::kOffP>(ph, ids, w, 1, s);
+  if constexpr (!uses_tile<typename A::P>()) st = adjoint_launch<typename A::P, A::kOffP>(ph, ids, w, 1, s);
   if (st) return st;
   mark(mk, kMarkAdjP, s);
   DIPS_CHECK_LAUNCH("job adjoint");
@@ -540,15 +546,27 @@ static int job_adjoint(const PtsH& ph, const int32_t* ids, const Workspace& w, c
 template <class N, int OFF, bool BWD>
 static int fused_launch(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
                         float* residual_out, int net_p, cudaStream_t s) {
-  constexpr size_t bytes = fused_smem_bytes<N>();
-  static bool attr_done = false;
-  if (!attr_done) {
-    cudaError_t e = cudaFuncSetAttribute(k_bulk_fused<N, OFF, A::kParams, BWD>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(fused smem)");
-    attr_done = true;
+  if constexpr (uses_tile<N>()) {
+    constexpr size_t bytes = tile::Layout<N>::kBytes;
+    static bool attr_done = false;
+    if (!attr_done) {
+      cudaError_t e = cudaFuncSetAttribute(tile::k_tile_net<N, OFF, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)bytes);
+      if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(tile engine smem)");
+      attr_done = true;
+    }
+    tile::k_tile_net<N, OFF, BWD><<<kTileGrid, tile::kThreads, bytes, s>>>(ph, ids, w, rec, net_p, residual_out);
+  } else {
+    constexpr size_t bytes = fused_smem_bytes<N>();
+    static bool attr_done = false;
+    if (!attr_done) {
+      cudaError_t e = cudaFuncSetAttribute(k_bulk_fused<N, OFF, A::kParams, BWD>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(fused smem)");
+      attr_done = true;
+    }
+    k_bulk_fused<N, OFF, A::kParams, BWD><<<w.fgrid, kFusedThreads, bytes, s>>>(ph, ids, w, rec, net_p, residual_out);
   }
-  k_bulk_fused<N, OFF, A::kParams, BWD><<<w.fgrid, kFusedThreads, bytes, s>>>(ph, ids, w, rec, net_p, residual_out);
   return DIPS_OK;
 }
 
@@ -583,7 +601,10 @@ static int mlp_eval(const float* pts, const float* phi, int64_t n, float* u, flo
 
 const ArchOps* DIPS_GETTER() {
   static const ArchOps ops = {DIPS_LM,           DIPS_WM,          DIPS_LP,
-                              DIPS_WP,           DIPS_NS::A::kParams, DIPS_NS::load_params,
+                              DIPS_WP,           DIPS_NS::A::kParams,
+                              DIPS_NS::uses_tile<DIPS_NS::A::M>() ? 1 : 0,
+                              DIPS_NS::uses_tile<DIPS_NS::A::P>() ? 1 : 0,
+                              DIPS_NS::load_params,
                               DIPS_NS::job_forward, DIPS_NS::job_adjoint, DIPS_NS::bulk_fused,
                               DIPS_NS::mlp_eval};
   return &ops;

@@ -11,6 +11,7 @@ constexpr int kAdjThreads = 256;     // adjoint CTA: 8 warps
 constexpr int kAdjGrid = 152 * 2;    // two adjoint CTAs per SM (GB300 has 152 SMs)
 constexpr int kFusedThreads = 224;   // fused bulk CTA: one warp per stencil point
 constexpr int kFusedGrid = 152 * 2;
+constexpr int kTileGrid = 152;  // register-blocked engine: one 12-warp CTA per SM
 
 // ----------------------------------------------------------------------------------------
 // workspace
@@ -92,6 +93,7 @@ inline void mark(const Marks* m, int slot, cudaStream_t s) {
 struct ArchOps {
   int m_layers, m_width, p_layers, p_width;
   int n_params;
+  int tile_m, tile_p;  // 1: the network runs on the register-blocked engine (kTileGrid gradient rows)
   int (*load_params)(const float* params, cudaStream_t s);
   int (*job_forward)(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s);
   int (*job_adjoint)(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s);
