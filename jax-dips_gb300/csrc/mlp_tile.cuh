@@ -28,9 +28,9 @@
 // accumulators into shared memory and writes one partial gradient row.
 //
 // Tiles: bulk tiles hold 4 bulk points x 7 stencil points (lanes 0..27; lane = 7*point +
-// stencil), whose residual is formed inside the warp from the 7 network values; general tiles
-// hold 32 consecutive jobs of the expanded job list with their coordinates and dL/du
-// precomputed (jx, jg).
+// stencil), whose residual is formed inside the warp from the 7 network values, plus (in the
+// backward) 4 general jobs in lanes 28..31; general tiles hold 32 consecutive jobs of the
+// expanded job list.  General jobs come with their coordinates and dL/du precomputed (jx, jg).
 
 namespace tile {
 
@@ -389,7 +389,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_tile_net(PtsH ph, const int32_t
   const int64_t jbeg = net_p ? ctl.jm_pad : 0;
   const int64_t jend = net_p ? ctl.total : ctl.jm;
   const int64_t nbt = (nb + 3) / 4;
-  const int64_t ngt = BWD ? (jend - jbeg + 31) / 32 : 0;
+  const int64_t nrest = jend - jbeg - 4 * nbt;  // general jobs beyond the bulk tiles' spare lanes
+  const int64_t ngt = BWD && nrest > 0 ? (nrest + 31) / 32 : 0;
   const float Bf = (float)w.B;
   const int jc = 4 * (lane & 7);
   const bool lead = (lane >> 3) == 0;  // lanes holding u of jobs jc..jc+3 after the reduction
@@ -397,19 +398,43 @@ __global__ void __launch_bounds__(kThreads, 1) k_tile_net(PtsH ph, const int32_t
 
   for (int64_t tile = (int64_t)blockIdx.x * kWarps + warp; tile < nbt + ngt; tile += (int64_t)gridDim.x * kWarps) {
     if (tile < nbt) {
-      // ---- bulk tile: lane = 7 * point + stencil point
+      // ---- bulk tile: lane = 7 * point + stencil point; with BWD, lanes 28..31 carry four
+      // general jobs (their dL/du is known) instead of idling
       const int pl = lane / kStencil, s = lane - kStencil * pl;
       const int64_t idx = tile * 4 + pl;
       float x[3] = {0.0f, 0.0f, 0.0f};
       float A = 0.0f;
-      if (lane < 4 * kStencil && idx < nb) {
-        const int64_t pid = batch_pid(ids, list[idx]);
-        const float p[3] = {ph.pts[3 * pid], ph.pts[3 * pid + 1], ph.pts[3 * pid + 2]};
-        stencil_point(p, ph.h, s, x);
-        const int64_t jb = net_p ? rec.job_off[pid + 1] - kStencil : rec.job_off[pid];
+      if (lane < 4 * kStencil) {
+        if (idx < nb) {
+          const int64_t pid = batch_pid(ids, list[idx]);
+          const float p[3] = {ph.pts[3 * pid], ph.pts[3 * pid + 1], ph.pts[3 * pid + 2]};
+          stencil_point(p, ph.h, s, x);
+          const int64_t jb = net_p ? rec.job_off[pid + 1] - kStencil : rec.job_off[pid];
 #pragma unroll
-        for (int q = 0; q < kStencil; ++q)
-          if (job_stencil(rec.job_code[jb + q]) == s) A = rec.job_A[jb + q];
+          for (int q = 0; q < kStencil; ++q)
+            if (job_stencil(rec.job_code[jb + q]) == s) A = rec.job_A[jb + q];
+        }
+      } else if (BWD) {
+        const int64_t j = jbeg + 4 * tile + (lane - 4 * kStencil);
+        float g = 0.0f;
+        if (j < jend) {
+          const float4 xv = w.jx[j];
+          x[0] = xv.x;
+          x[1] = xv.y;
+          x[2] = xv.z;
+          g = w.jg[j];
+        }
+        G[lane] = g;
+      }
+      // the residual's point records, for lanes 0..3 (point `lane` of the tile)
+      int32_t rslot = -1;
+      float r_lhs0 = 0.0f, r_diag = 1.0f, r_rod = 0.0f;
+      if (lane < 4 && tile * 4 + lane < nb) {
+        rslot = list[tile * 4 + lane];
+        const int64_t pp = batch_pid(ids, rslot);
+        r_lhs0 = rec.lhs0[pp];
+        r_diag = rec.diag[pp];
+        r_rod = rec.rod[pp];
       }
       X[lane] = x[0];
       X[32 + lane] = x[1];
@@ -421,31 +446,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_tile_net(PtsH ph, const int32_t
         __syncwarp();
         // lanes 0..3: residual of point `lane`; then dL/du of its 7 jobs
         if (lane < 4) {
-          const int64_t pidx = tile * 4 + lane;
           float gc = 0.0f;
-          if (pidx < nb) {
-            const int32_t sl = list[pidx];
-            const int64_t pp = batch_pid(ids, sl);
-            float lhs = rec.lhs0[pp];
+          if (rslot >= 0) {
+            float lhs = r_lhs0;
 #pragma unroll
             for (int q = 0; q < kStencil; ++q) lhs += U[kStencil * lane + q];
-            const float diag = rec.diag[pp];
-            const float qv = lhs / diag;
-            const float r = nan_to_num(qv) - rec.rod[pp];
-            gc = isfinite(qv) ? (r / Bf) / diag : 0.0f;
+            const float qv = lhs / r_diag;
+            const float r = nan_to_num(qv) - r_rod;
+            gc = isfinite(qv) ? (r / Bf) / r_diag : 0.0f;
             lsum += 0.5 * (double)r * (double)r;
-            if (residual_out) residual_out[sl] = r;
+            if (residual_out) residual_out[rslot] = r;
           }
           if (BWD) {
 #pragma unroll
             for (int q = 0; q < kStencil; ++q) G[kStencil * lane + q] = gc * Av[kStencil * lane + q];
           }
         }
-        if (BWD && lane >= 28) G[lane] = 0.0f;
       });
     } else {
-      // ---- general tile: 32 jobs of the job list
-      const int64_t j = jbeg + (tile - nbt) * 32 + lane;
+      // ---- general tile: 32 jobs of the job list (after those carried by the bulk tiles)
+      const int64_t j = jbeg + 4 * nbt + (tile - nbt) * 32 + lane;
       float4 xv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       float g = 0.0f;
       if (j < jend) {
