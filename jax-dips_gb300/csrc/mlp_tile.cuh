@@ -57,7 +57,9 @@ struct Layout {
   static constexpr int kG = kBB + W * kRS;      // [32] dL/du per job
   static constexpr int kU = kG + 32;            // [32] A_j u_j of bulk tiles
   static constexpr int kAv = kU + 32;           // [32] A_j of bulk tiles
-  static constexpr int kWarpFloats = kAv + 32;
+  static constexpr int kStage = kAv + 32;       // [2][160] inputs of the current and the next tile
+  static constexpr int kStageFloats = 160;
+  static constexpr int kWarpFloats = kStage + 2 * kStageFloats;
   static constexpr int kWarp0 = (kShared + 3) / 4 * 4;
   static constexpr int kAcc = kWarp0 + kWarps * kWarpFloats;     // [kParams] CTA gradient accumulator
   static constexpr int kLoss = (kAcc + N::kParams + 3) / 4 * 4;  // [kWarps] doubles
@@ -67,6 +69,21 @@ struct Layout {
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, float a, float b, float c, float d) {
   *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+}
+
+// asynchronous global -> shared copies (zero-filled when !valid; src must still be mapped)
+__device__ __forceinline__ void cp_async16(float* dst, const void* src, bool valid) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async4(float* dst, const void* src, bool valid) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 // tanh of a pre-scaled argument y = 2 log2(e) z: 1 - 2/(1 + 2^y), hardware exp2 and
@@ -385,7 +402,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tile_net(PtsH ph, const int32_t
 
   const Ctl ctl = *w.ctl;
   const int64_t nb = net_p ? ctl.nbp : ctl.nbm;
-  const int32_t* list = w.bulk + (net_p ? w.B : 0);
+  const float* recs = w.brec + (size_t)(net_p ? w.B : 0) * kRecFloats;
   const int64_t jbeg = net_p ? ctl.jm_pad : 0;
   const int64_t jend = net_p ? ctl.total : ctl.jm;
   const int64_t nbt = (nb + 3) / 4;
@@ -396,45 +413,71 @@ __global__ void __launch_bounds__(kThreads, 1) k_tile_net(PtsH ph, const int32_t
   const bool lead = (lane >> 3) == 0;  // lanes holding u of jobs jc..jc+3 after the reduction
   double lsum = 0.0;
 
-  for (int64_t tile = (int64_t)blockIdx.x * kWarps + warp; tile < nbt + ngt; tile += (int64_t)gridDim.x * kWarps) {
+  // Stage layout.  Bulk tile: 4 point records [0, 64), spare-lane coordinates [64, 80) and
+  // dL/du [80, 84).  General tile: coordinates [0, 128), dL/du [128, 160).
+  float* stage0 = wp + Lay::kStage;
+  auto issue = [&](int64_t t, float* st) {
+    if (t < nbt) {
+      if (lane < 16) {
+        const int64_t pidx = t * 4 + (lane >> 2);
+        const bool ok = pidx < nb;
+        cp_async16(st + 4 * lane, recs + (ok ? pidx : 0) * kRecFloats + 4 * (lane & 3), ok);
+      } else if (BWD && lane < 20) {
+        const int64_t j = jbeg + 4 * t + (lane - 16);
+        const bool ok = j < jend;
+        cp_async16(st + 64 + 4 * (lane - 16), w.jx + (ok ? j : 0), ok);
+      } else if (BWD && lane < 24) {
+        const int64_t j = jbeg + 4 * t + (lane - 20);
+        const bool ok = j < jend;
+        cp_async4(st + 80 + (lane - 20), w.jg + (ok ? j : 0), ok);
+      }
+    } else if (t < nbt + ngt) {
+      const int64_t j = jbeg + 4 * nbt + (t - nbt) * 32 + lane;
+      const bool ok = j < jend;
+      cp_async16(st + 4 * lane, w.jx + (ok ? j : 0), ok);
+      cp_async4(st + 128 + lane, w.jg + (ok ? j : 0), ok);
+    }
+    cp_commit();
+  };
+
+  const int64_t stride = (int64_t)gridDim.x * kWarps;
+  int64_t tile = (int64_t)blockIdx.x * kWarps + warp;
+  issue(tile, stage0);
+  int sidx = 0;
+  for (; tile < nbt + ngt; tile += stride, sidx ^= 1) {
+    issue(tile + stride, stage0 + (sidx ^ 1) * Lay::kStageFloats);
+    cp_wait<1>();  // this tile's copies have landed
+    __syncwarp();
+    const float* st = stage0 + sidx * Lay::kStageFloats;
     if (tile < nbt) {
       // ---- bulk tile: lane = 7 * point + stencil point; with BWD, lanes 28..31 carry four
       // general jobs (their dL/du is known) instead of idling
       const int pl = lane / kStencil, s = lane - kStencil * pl;
-      const int64_t idx = tile * 4 + pl;
       float x[3] = {0.0f, 0.0f, 0.0f};
       float A = 0.0f;
       if (lane < 4 * kStencil) {
-        if (idx < nb) {
-          const int64_t pid = batch_pid(ids, list[idx]);
-          const float p[3] = {ph.pts[3 * pid], ph.pts[3 * pid + 1], ph.pts[3 * pid + 2]};
+        if (tile * 4 + pl < nb) {
+          const float* r = st + pl * kRecFloats;
+          const float p[3] = {r[kRecP], r[kRecP + 1], r[kRecP + 2]};
           stencil_point(p, ph.h, s, x);
-          const int64_t jb = net_p ? rec.job_off[pid + 1] - kStencil : rec.job_off[pid];
-#pragma unroll
-          for (int q = 0; q < kStencil; ++q)
-            if (job_stencil(rec.job_code[jb + q]) == s) A = rec.job_A[jb + q];
+          A = r[kRecA + s];
         }
       } else if (BWD) {
-        const int64_t j = jbeg + 4 * tile + (lane - 4 * kStencil);
-        float g = 0.0f;
-        if (j < jend) {
-          const float4 xv = w.jx[j];
-          x[0] = xv.x;
-          x[1] = xv.y;
-          x[2] = xv.z;
-          g = w.jg[j];
-        }
-        G[lane] = g;
+        const float* xv = st + 64 + 4 * (lane - 4 * kStencil);
+        x[0] = xv[0];
+        x[1] = xv[1];
+        x[2] = xv[2];
+        G[lane] = st[80 + lane - 4 * kStencil];
       }
       // the residual's point records, for lanes 0..3 (point `lane` of the tile)
       int32_t rslot = -1;
       float r_lhs0 = 0.0f, r_diag = 1.0f, r_rod = 0.0f;
       if (lane < 4 && tile * 4 + lane < nb) {
-        rslot = list[tile * 4 + lane];
-        const int64_t pp = batch_pid(ids, rslot);
-        r_lhs0 = rec.lhs0[pp];
-        r_diag = rec.diag[pp];
-        r_rod = rec.rod[pp];
+        const float* r = st + lane * kRecFloats;
+        rslot = __float_as_int(r[kRecSlot]);
+        r_lhs0 = r[kRecLhs0];
+        r_diag = r[kRecDiag];
+        r_rod = r[kRecRod];
       }
       X[lane] = x[0];
       X[32 + lane] = x[1];
@@ -465,21 +508,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_tile_net(PtsH ph, const int32_t
       });
     } else {
       // ---- general tile: 32 jobs of the job list (after those carried by the bulk tiles)
-      const int64_t j = jbeg + 4 * nbt + (tile - nbt) * 32 + lane;
-      float4 xv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      float g = 0.0f;
-      if (j < jend) {
-        xv = w.jx[j];
-        g = w.jg[j];
-      }
-      X[lane] = xv.x;
-      X[32 + lane] = xv.y;
-      X[64 + lane] = xv.z;
-      G[lane] = g;
+      X[lane] = st[4 * lane];
+      X[32 + lane] = st[4 * lane + 1];
+      X[64 + lane] = st[4 * lane + 2];
+      G[lane] = st[128 + lane];
       __syncwarp();
       run_tile<N, OFF, BWD>(sm, wp, acc, lane, [](const float (&)[4]) {});
     }
   }
+  cp_wait<0>();
   // loss partial of the CTA
   double* wl = reinterpret_cast<double*>(sm + Lay::kLoss);
 #pragma unroll

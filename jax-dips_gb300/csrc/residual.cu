@@ -54,6 +54,7 @@ static size_t carve(Workspace* w, char* base, int64_t B, int64_t max_jobs, int P
   W.ju = (float*)take(sizeof(float) * W.jcap);
   W.jx = (float4*)take(sizeof(float4) * W.jcap);
   W.jg = (float*)take(sizeof(float) * W.jcap);
+  W.brec = (float*)take(sizeof(float) * kRecFloats * 2 * B);
   W.partials = (float*)take(sizeof(float) * (size_t)(W.grid + W.fgrid) * P);
   W.grad = (float*)take(sizeof(float) * P);
   if (w) *w = W;
@@ -185,7 +186,27 @@ __global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, dips_records_
   if (kind == 3) return;
   if (kind == 1 || kind == 2) {
     const int net = kind - 1;
-    w.bulk[net * B + w.ob[b] + w.blk[4 * blockIdx.x + net]] = (int32_t)b;
+    const int64_t pos = net * B + w.ob[b] + w.blk[4 * blockIdx.x + net];
+    w.bulk[pos] = (int32_t)b;
+    // the point's record, so that the tile engine reads one contiguous 64-byte block
+    const int64_t pid = batch_pid(ids, b);
+    const int64_t jb = net ? rec.job_off[pid + 1] - kStencil : rec.job_off[pid];
+    float A[kStencil];
+#pragma unroll
+    for (int t = 0; t < kStencil; ++t) A[t] = 0.0f;
+#pragma unroll
+    for (int q = 0; q < kStencil; ++q) {
+      const int sj = job_stencil(rec.job_code[jb + q]);
+      const float a = rec.job_A[jb + q];
+#pragma unroll
+      for (int t = 0; t < kStencil; ++t)
+        if (sj == t) A[t] = a;
+    }
+    float4* r4 = reinterpret_cast<float4*>(w.brec + pos * kRecFloats);
+    r4[0] = make_float4(rec.pts[3 * pid], rec.pts[3 * pid + 1], rec.pts[3 * pid + 2], rec.lhs0[pid]);
+    r4[1] = make_float4(A[0], A[1], A[2], A[3]);
+    r4[2] = make_float4(A[4], A[5], A[6], rec.diag[pid]);
+    r4[3] = make_float4(rec.rod[pid], __int_as_float((int32_t)b), 0.0f, 0.0f);
     return;
   }
   const int64_t pid = batch_pid(ids, b);

@@ -11,7 +11,9 @@ constexpr int kAdjThreads = 256;     // adjoint CTA: 8 warps
 constexpr int kAdjGrid = 152 * 2;    // two adjoint CTAs per SM (GB300 has 152 SMs)
 constexpr int kFusedThreads = 224;   // fused bulk CTA: one warp per stencil point
 constexpr int kFusedGrid = 152 * 2;
-constexpr int kTileGrid = 152;  // register-blocked engine: one 12-warp CTA per SM
+constexpr int kTileGrid = 152;
+// bulk point record (16 floats): point, lhs0, A of stencil points 0..6, diag, rod, batch slot
+constexpr int kRecP = 0, kRecLhs0 = 3, kRecA = 4, kRecDiag = 11, kRecRod = 12, kRecSlot = 13, kRecFloats = 16;  // register-blocked engine: one 12-warp CTA per SM
 
 // ----------------------------------------------------------------------------------------
 // workspace
@@ -43,6 +45,7 @@ struct Workspace {
   float* ju;
   float4* jx;        // [jcap] job coordinates (w unused)
   float* jg;         // [jcap] d loss / d u of the job
+  float* brec;       // [2][B][16] bulk point records, in bulk-list order (layout: kRec* below)
   float* partials;   // [2*grid][P]: rows [0, grid) general adjoint, [grid, 2*grid) fused
   float* grad;       // [P]
   int64_t nblk, nres, jcap, B;
