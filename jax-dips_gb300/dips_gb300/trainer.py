@@ -25,7 +25,7 @@ from typing import Callable
 import numpy as np
 import torch
 
-from . import _lib, levelset, nn, ops
+from . import _lib, dp, levelset, nn, ops
 from .mesh import GridState
 from .records import FVLevel, eval_callable
 
@@ -107,7 +107,7 @@ class Trainer:
     def __init__(self, lvl_gstate: GridState, tr_gstate: GridState, eval_gstate: GridState, sim_state_fn,
                  num_epochs=1000, batch_size=131072, optimizer_dict=None, model_dict=None, batching="sequential",
                  seed=0, checkpoint_dir=None, restart=False, restart_checkpoint_dir=None, use_graph=True,
-                 device="cuda"):
+                 device="cuda", multi_gpu=False):
         if not torch.cuda.is_available():
             raise RuntimeError("dips_gb300 runs on a CUDA GPU; none is available")
         _lib.load()
@@ -132,7 +132,19 @@ class Trainer:
         pts = np.asarray(tr_gstate.R, F32)
         n = pts.shape[0]
         bs = min(int(batch_size), n)
-        if batching == "sequential":
+        self.multi_gpu = bool(multi_gpu)
+        self.rank, self.world = 0, 1
+        if self.multi_gpu:
+            # one process per GPU: this rank trains on its DatasetDict device run and the
+            # gradients are summed across ranks every step (trainer.py:716-834)
+            if not torch.distributed.is_initialized():
+                raise RuntimeError("multi_gpu needs torch.distributed initialised, one process per GPU")
+            self.rank, self.world = torch.distributed.get_rank(), torch.distributed.get_world_size()
+            pts, bs, nb = dp.device_points(pts, self.world * int(batch_size), self.rank, self.world,
+                                           lambda c: self._padding_points(np.asarray(tr_gstate.R, F32), c))
+            self.batching = "sequential"
+            self.use_graph = False
+        elif batching == "sequential":
             nb, extra = n // bs, n % bs
             if extra:
                 pad = self._padding_points(pts, bs - extra)
@@ -186,6 +198,13 @@ class Trainer:
         _lib.check(lib.dips_batch_ids_device(n_ids, self.batch, self.n_batches, self.seed or 0, mode,
                                              _lib.ptr(self.opt.count), _lib.ptr(self.ids), _lib.stream_handle()),
                    "dips_batch_ids_device")
+        if self.multi_gpu:  # update_multi_gpu (trainer.py:824-834): psum of grads and loss, then Adam
+            loss, _, _ = ops.residual_forward(self.arch, self.params, lvl, self.ids, ws)
+            grad = ops.residual_backward(self.arch, self.params, lvl, self.ids, ws)
+            dp.allreduce_sum_(grad, loss)
+            self.opt.step(self.arch, self.params, grad)
+            self.loss_epoch_acc += loss
+            return
         ops.train_step(self.arch, self.params, self.opt, lvl, self.ids, ws, self.loss_dev)
         self.loss_epoch_acc += self.loss_dev
 
@@ -304,8 +323,6 @@ def setup(initial_value_fn, dirichlet_bc_fn, lvl_set_fn, mu_m_fn_, mu_p_fn_, k_m
                 seed: int = 42, use_graph: bool = True):
         if algorithm != 0:
             raise NotImplementedError("algorithm 1 (network extrapolation) is unimplemented in the reference too")
-        if multi_gpu:
-            raise NotImplementedError("one GPU per process; use dips_gb300.parallel for data parallelism")
         R = torch.as_tensor(eval_gstate.R, device="cuda")
         ev = lambda f: eval_callable(f, R)  # noqa: E731
         state = PoissonSimState(ev(lvl_set_fn), ev(initial_value_fn), ev(dirichlet_bc_fn), ev(mu_m_fn_),
@@ -316,7 +333,7 @@ def setup(initial_value_fn, dirichlet_bc_fn, lvl_set_fn, mu_m_fn_, mu_p_fn_, k_m
             tr = Trainer(lvl_gstate, tr_gstate, eval_gstate, fn, num_epochs=num_epochs, batch_size=batch_size,
                          optimizer_dict=optimizer_dict, model_dict=model_dict, batching=batching, seed=seed,
                          checkpoint_dir=checkpoint_dir, restart=restart, restart_checkpoint_dir=restart_checkpoint_dir,
-                         use_graph=use_graph)
+                         use_graph=use_graph, multi_gpu=multi_gpu)
             epoch_store, loss_epochs = tr.solve(print_rate=print_rate)
             u, gu, gn = tr.evaluate_solution_and_gradients(eval_gstate)
             new = dataclasses.replace(sim_state, solution=u, grad_solution=gu, grad_normal_solution=gn)
