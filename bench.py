@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--no-tta", action="store_true")
     ap.add_argument("--tta-lr", type=float, default=1e-2)
     ap.add_argument("--cpu-sample", type=int, default=16384)
+    ap.add_argument("--problem", default="sphere", choices=["sphere", "star"],
+                    help="sphere: phi=|x|-0.5, mu 1/10 (the 128^3 headline); star: the variable-coefficient "
+                         "star interface (mu- = 1+0.5 sin xy, mu+ = 20+5 cos z, k+ = 1)")
     return ap.parse_args()
 
 
@@ -113,7 +116,7 @@ class ClockSampler:
 # ----------------------------------------------------------------------------------------
 # reference arm: the CPU restatement of the reference's per-step work
 # ----------------------------------------------------------------------------------------
-def cpu_oracle_rate(n, sample, steps, seed=0, arch=ARCH):
+def cpu_oracle_rate(n, sample, steps, seed=0, arch=ARCH, problem="sphere"):
     import torch
 
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -121,7 +124,7 @@ def cpu_oracle_rate(n, sample, steps, seed=0, arch=ARCH):
     import nbm_oracle as O
     from dips_gb300 import mesh, problems
 
-    pr = problems.sphere_problem()
+    pr = getattr(problems, f"{problem}_problem")()
     g = mesh.uniform_grid(n)
     phi = O.perturb(np.asarray(pr["phi"](g.R.T), np.float32))
     prob = L.Problem(phi, g.x, g.y, g.z, pr)
@@ -145,9 +148,9 @@ def run_reference(args, rank, world):
     steps = max(args.steps, 1)
     sample = args.cpu_sample
     # warm-up (imports, allocator)
-    cpu_oracle_rate(args.n, 256, max(min(args.warmup, 2), 1))
+    cpu_oracle_rate(args.n, 256, max(min(args.warmup, 2), 1), problem=args.problem)
     t0 = time.perf_counter()
-    rate, times, cores = cpu_oracle_rate(args.n, sample, steps)
+    rate, times, cores = cpu_oracle_rate(args.n, sample, steps, problem=args.problem)
     wall = time.perf_counter() - t0
     line = {
         "impl": "reference",
@@ -163,7 +166,7 @@ def run_reference(args, rank, world):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"sphere {args.n}^3, DoubleMLP 3x32/3x32 tanh, h=dx; each step a sample of "
+        "config": {"workload": f"{args.problem} {args.n}^3, DoubleMLP 3x32/3x32 tanh, h=dx; each step a sample of "
                                f"{sample} points (geometry + residual + gradient, recomputed per step as the "
                                "reference does)", "global_batch": sample},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
@@ -187,7 +190,7 @@ def run_ours(args, rank, world):
     dev = f"cuda:{int(os.environ.get('LOCAL_RANK', 0))}"
     torch.cuda.set_device(dev)
     lib = _lib.load()
-    pr = problems.sphere_problem()
+    pr = getattr(problems, f"{args.problem}_problem")()
     g = mesh.uniform_grid(args.n)
     arch = nn.Arch(*ARCH)
     P = nn.n_params(arch)
@@ -327,7 +330,7 @@ def run_ours(args, rank, world):
     # ---- CPU baseline (oracle port, bounded sample)
     cpu = None
     if rank == 0:
-        rate, times, cores = cpu_oracle_rate(args.n, args.cpu_sample, 3)
+        rate, times, cores = cpu_oracle_rate(args.n, args.cpu_sample, 3, problem=args.problem)
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"3 steps x {args.cpu_sample} points of the {args.n}^3 grid (geometry + residual + "
                          f"gradient per step), {sum(times):.1f} s"}
@@ -346,7 +349,7 @@ def run_ours(args, rank, world):
             "vs_baseline": None,
             "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": f"NBM training step, sphere {args.n}^3 (phi grid {args.n}^3), DoubleMLP "
+            "config": {"workload": f"NBM training step, {args.problem} {args.n}^3 (phi grid {args.n}^3), DoubleMLP "
                                    "3x32/3x32 tanh, h=dx, minibatch drawn uniformly",
                        "global_batch": B * world, "points": int(lvl.n), "jobs_per_step": jobs_m + jobs_p,
                        "l2": "flushed (256 MB write) between timed steps", "cuda_graph": world == 1,
@@ -433,7 +436,36 @@ def time_to_target(args, lvl, g, pr, arch, dev):
         if err <= target:
             reached = t_train
             break
-    return {"target_rel_linf": target, "floor_rel_linf": floor,
+    # what the trained network adds over the discrete solution: values off the grid.  The
+    # Krylov nodal field is interpolated trilinearly (the same interpolation the level set
+    # uses); the network is evaluated on the side of the interface the point lies on.
+    from dips_gb300 import levelset
+
+    rng = np.random.default_rng(3)
+    q = torch.as_tensor(rng.uniform(-0.9, 0.9, (200000, 3)).astype(np.float32), device=dev)
+    phi_q = lvl.ls(q)
+    qn = q.T.cpu().numpy()
+    # the exact solution on the side of the interface that both methods see (the sign of the
+    # interpolated level set), so that a side mismatch within O(h^2) of the interface is not
+    # counted as an error of either method
+    side = (phi_q >= 0).cpu().numpy()
+    ex_q = torch.as_tensor(np.where(side, pr["u_p"](qn), pr["u_m"](qn)).astype(np.float32), device=dev)
+    u_nn = nn.mlp_eval(arch, params, q, phi_q)
+    u_kr = levelset.LevelSetGrid(g, kr.x.reshape(-1).float(), dev)(q)
+    near = phi_q.abs() < 2.0 * float(g.dx)
+    scale = float(ex_q.abs().max())
+
+    def rel(a, m=None):
+        d = (a - ex_q).abs() if m is None else (a - ex_q)[m].abs()
+        return float(d.max()) / scale
+
+    offgrid = {"points": int(q.shape[0]), "near_interface_points": int(near.sum()),
+               "nbm_rel_linf": rel(u_nn), "krylov_trilinear_rel_linf": rel(u_kr),
+               "nbm_rel_linf_near_interface": rel(u_nn, near),
+               "krylov_trilinear_rel_linf_near_interface": rel(u_kr, near),
+               "nbm_rel_linf_away": rel(u_nn, ~near), "krylov_trilinear_rel_linf_away": rel(u_kr, ~near),
+               "near": "|phi| < 2 dx"}
+    return {"target_rel_linf": target, "floor_rel_linf": floor, "offgrid": offgrid,
             "note": "target = max(1e-2, 1.1 x the converged discrete solution's error): 1e-2 against the exact "
                     "solution is below this discretisation's error at this grid",
             "krylov_s": t_kr, "krylov_iterations": kr.iterations, "krylov_rel_linf": kr.rel_linf,
