@@ -62,9 +62,13 @@ def parse():
     ap.add_argument("--no-tta", action="store_true")
     ap.add_argument("--tta-lr", type=float, default=1e-2)
     ap.add_argument("--cpu-sample", type=int, default=16384)
-    ap.add_argument("--problem", default="sphere", choices=["sphere", "star"],
+    ap.add_argument("--problem", default="sphere", choices=["sphere", "star", "blob"],
                     help="sphere: phi=|x|-0.5, mu 1/10 (the 128^3 headline); star: the variable-coefficient "
-                         "star interface (mu- = 1+0.5 sin xy, mu+ = 20+5 cos z, k+ = 1)")
+                         "star interface (mu- = 1+0.5 sin xy, mu+ = 20+5 cos z, k+ = 1); blob: 0.3-isosurface of "
+                         "500 Gaussians, mu 1/100, k = 0.5")
+    ap.add_argument("--arch", default="3x32", choices=["3x32", "4x64", "2x16"],
+                    help="hidden layers x width of both networks (4x64 runs on the TF32 tensor cores)")
+    ap.add_argument("--n-ls", type=int, default=0, help="level-set grid side (default: the training grid's)")
     return ap.parse_args()
 
 
@@ -116,7 +120,7 @@ class ClockSampler:
 # ----------------------------------------------------------------------------------------
 # reference arm: the CPU restatement of the reference's per-step work
 # ----------------------------------------------------------------------------------------
-def cpu_oracle_rate(n, sample, steps, seed=0, arch=ARCH, problem="sphere"):
+def cpu_oracle_rate(n, sample, steps, seed=0, arch=ARCH, problem="sphere", n_ls=0):
     import torch
 
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -126,8 +130,9 @@ def cpu_oracle_rate(n, sample, steps, seed=0, arch=ARCH, problem="sphere"):
 
     pr = getattr(problems, f"{problem}_problem")()
     g = mesh.uniform_grid(n)
-    phi = O.perturb(np.asarray(pr["phi"](g.R.T), np.float32))
-    prob = L.Problem(phi, g.x, g.y, g.z, pr)
+    gl = mesh.uniform_grid(n_ls) if n_ls else g
+    phi = O.perturb(np.asarray(pr["phi"](torch.as_tensor(gl.R.T)).numpy(), np.float32))
+    prob = L.Problem(phi, gl.x, gl.y, gl.z, pr)
     h = np.array([g.dx, g.dy, g.dz], np.float32)
     a = L.Arch(*arch)
     w = L.init_params(a, 0)
@@ -148,9 +153,11 @@ def run_reference(args, rank, world):
     steps = max(args.steps, 1)
     sample = args.cpu_sample
     # warm-up (imports, allocator)
-    cpu_oracle_rate(args.n, 256, max(min(args.warmup, 2), 1), problem=args.problem)
+    cpu_oracle_rate(args.n, 256, max(min(args.warmup, 2), 1), arch=arch_tuple(args), problem=args.problem,
+                    n_ls=args.n_ls)
     t0 = time.perf_counter()
-    rate, times, cores = cpu_oracle_rate(args.n, sample, steps, problem=args.problem)
+    rate, times, cores = cpu_oracle_rate(args.n, sample, steps, arch=arch_tuple(args), problem=args.problem,
+                                         n_ls=args.n_ls)
     wall = time.perf_counter() - t0
     line = {
         "impl": "reference",
@@ -166,7 +173,7 @@ def run_reference(args, rank, world):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"{args.problem} {args.n}^3, DoubleMLP 3x32/3x32 tanh, h=dx; each step a sample of "
+        "config": {"workload": f"{args.problem} {args.n}^3, DoubleMLP {args.arch}/{args.arch} tanh, h=dx; each step a sample of "
                                f"{sample} points (geometry + residual + gradient, recomputed per step as the "
                                "reference does)", "global_batch": sample},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
@@ -181,8 +188,16 @@ def run_reference(args, rank, world):
 # ----------------------------------------------------------------------------------------
 # our arm
 # ----------------------------------------------------------------------------------------
+def arch_tuple(args):
+    L, W = (int(v) for v in args.arch.split("x"))
+    return (L, W, L, W)
+
+
 def run_ours(args, rank, world):
     import torch
+
+    global ARCH
+    ARCH = arch_tuple(args)
 
     from dips_gb300 import _lib, krylov, levelset, mesh, nn, ops, problems
     from dips_gb300.records import FVLevel
@@ -193,12 +208,13 @@ def run_ours(args, rank, world):
     pr = getattr(problems, f"{args.problem}_problem")()
     g = mesh.uniform_grid(args.n)
     arch = nn.Arch(*ARCH)
+    gl = mesh.uniform_grid(args.n_ls) if args.n_ls else g
     P = nn.n_params(arch)
 
     # ---- set-up: level set and residual records (timed, reported as set-up)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    ls = levelset.LevelSetGrid.from_callable(g, lambda r: levelset.perturb(pr["phi"](r)), dev)
+    ls = levelset.LevelSetGrid.from_callable(gl, lambda r: levelset.perturb(pr["phi"](r)), dev)
     pts = torch.as_tensor(g.R, device=dev)
     h = np.array([g.dx, g.dy, g.dz], np.float32)
     lvl = FVLevel(ls, pr, pts, h)
@@ -286,10 +302,13 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
         phases.append(ops.phase_ms(evs))
     phase_med = {k: statistics.median(p[k] for p in phases) for k in ops.STEP_PHASES}
-    t_dom = phase_med["fused_p"] / 1e3
-    # the u+ launch runs forward + adjoint of every u+ job: the 7 stencil jobs of each bulk u+
-    # point and the u+ jobs of the other points (3 F per job; the general forward that feeds
-    # their residual is its own launch and not counted here)
+    tensor = ARCH[1] == 64
+    # the dominant launch: for 3x32 the u+ tile launch (forward + adjoint of every u+ job: the 7
+    # stencil jobs of each bulk u+ point and the u+ jobs of the other points); for 4x64 the u+
+    # tensor-core adjoint (which also recomputes the forward).  3 F per job either way; the
+    # forward that feeds the residual and the recompute are not counted.
+    dom_phase = "adjoint_p" if tensor else "fused_p"
+    t_dom = phase_med[dom_phase] / 1e3
     dom_flops = 3 * jobs_p * f_p
     # FP32 FMA peak of this GPU (measured)
     probe = torch.empty(152 * 16 * 256, dtype=torch.float32, device=dev)
@@ -302,6 +321,19 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     fp32_peak = 152 * 16 * 256 * 8 * 16 * iters * 2 / (pe0.elapsed_time(pe1) / 1e3) / 1e12
     dom_tflops = dom_flops / t_dom / 1e12
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    if tensor:  # TF32 dense tensor rate = half the BF16 dense rate on this architecture
+        bf16 = float(peaks.get("bf16_tflops", 1900.0))
+        dom_peak, peak_src = bf16 / 2, ("half of MEASURED_PEAKS.json bf16_tflops (cuBLAS bf16 burst), the TF32 dense "
+                                        "rate" if "bf16_tflops" in peaks else "fallback 1.9 PFLOP/s bf16 / 2")
+    else:
+        dom_peak, peak_src = fp32_peak, ("measured FFMA probe (dips_fp32_fma_probe) in this run; "
+                                         "MEASURED_PEAKS.json has no FP32 figure")
     step_tflops = 3 * fwd_flops / (t_total / args.steps) / 1e12
 
     # ---- e2e through the public API with host buffers
@@ -330,7 +362,8 @@ def run_ours(args, rank, world):
     # ---- CPU baseline (oracle port, bounded sample)
     cpu = None
     if rank == 0:
-        rate, times, cores = cpu_oracle_rate(args.n, args.cpu_sample, 3, problem=args.problem)
+        rate, times, cores = cpu_oracle_rate(args.n, args.cpu_sample, 3, arch=ARCH, problem=args.problem,
+                                             n_ls=args.n_ls)
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"3 steps x {args.cpu_sample} points of the {args.n}^3 grid (geometry + residual + "
                          f"gradient per step), {sum(times):.1f} s"}
@@ -349,25 +382,28 @@ def run_ours(args, rank, world):
             "vs_baseline": None,
             "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": f"NBM training step, {args.problem} {args.n}^3 (phi grid {args.n}^3), DoubleMLP "
-                                   "3x32/3x32 tanh, h=dx, minibatch drawn uniformly",
+            "config": {"workload": f"NBM training step, {args.problem} {args.n}^3 (phi grid {args.n_ls or args.n}^3), "
+                                   f"DoubleMLP {args.arch}/{args.arch} tanh ({'TF32 tensor cores' if tensor else 'FP32'}), "
+                                   "h=dx, minibatch drawn uniformly",
                        "global_batch": B * world, "points": int(lvl.n), "jobs_per_step": jobs_m + jobs_p,
                        "l2": "flushed (256 MB write) between timed steps", "cuda_graph": world == 1,
                        "setup_s": setup_s, "wall_s_timed": wall},
-            "roofline": {"bound": "fp32", "kernel": "tile::k_tile_net<u+ net, backward> (forward, bulk residual, "
-                                                    "adjoint and dW of every u+ job of the batch)",
-                         "achieved": dom_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
-                         "frac": dom_tflops / fp32_peak, "traffic": FUSED_TRAFFIC.get((args.n, B)),
+            "roofline": {"bound": "tensor" if tensor else "fp32",
+                         "kernel": ("tcnet::k_tc_adjoint<u+ net> (tcgen05 TF32: recomputed forward, adjoint and "
+                                    "dW of every u+ job)" if tensor else
+                                    "tile::k_tile_net<u+ net, backward> (forward, bulk residual, adjoint and dW of "
+                                    "every u+ job of the batch)"),
+                         "achieved": dom_tflops, "peak": dom_peak, "unit": "TFLOP/s",
+                         "frac": dom_tflops / dom_peak, "traffic": FUSED_TRAFFIC.get((args.n, B)),
                          "algorithmic": f"3 x F(u+) per u+ job, F = sum(2*in*out+out) + tanh count = {f_p}; "
-                                        f"{jobs_p} u+ jobs per launch ({bulk_p} bulk u+ points x 7 + general)",
-                         "peak_source": "measured FFMA probe (dips_fp32_fma_probe) in this run; "
-                                        "MEASURED_PEAKS.json has no FP32 figure",
+                                        f"{jobs_p} u+ jobs per launch ({bulk_p} bulk u+ points)",
+                         "peak_source": peak_src, "fp32_peak_tflops": fp32_peak,
                          "phase_ms": phase_med,
                          "step_tflops": step_tflops, "step_frac": step_tflops / fp32_peak,
                          "step_algorithmic": "3 x F x (all jobs of the batch) per step"},
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "gpu_launches": 14 * args.steps,
+            "gpu_launches": (12 if tensor else 14) * args.steps,
             "clocks": clk,
             "time_to_target": tta,
         }

@@ -106,7 +106,7 @@ __device__ __forceinline__ void block_scan4(const int64_t v[4], int64_t ex[4], i
 // A point is "bulk" when it has exactly 7 jobs (its stencil points, no cube vertices) all of
 // one network; the fused kernel handles it.
 __global__ void k_count(const int32_t* __restrict__ ids, int64_t B, int64_t n_pts, const int32_t* __restrict__ cnt,
-                        const int32_t* __restrict__ cnt_m, Workspace w) {
+                        const int32_t* __restrict__ cnt_m, int bulk_ok, Workspace w) {
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   int64_t v[4] = {0, 0, 0, 0};  // bulk u-, bulk u+, general u- jobs, general u+ jobs
   if (b < B) {
@@ -114,7 +114,7 @@ __global__ void k_count(const int32_t* __restrict__ ids, int64_t B, int64_t n_pt
     int kind = 3;                   // an out-of-range id gets no work and a NaN residual
     if (pid >= 0 && pid < n_pts) {
       const int c = cnt[pid], m = cnt_m[pid];
-      if (c == kStencil && (m == kStencil || m == 0)) {
+      if (bulk_ok && c == kStencil && (m == kStencil || m == 0)) {
         kind = m ? 1 : 2;
         v[m ? 0 : 1] = 1;
       } else {
@@ -159,6 +159,7 @@ __global__ void k_scan_blocks(Workspace w) {
     const bool over = jm_pad + jp > w.jcap;
     // on overflow no job is expanded or evaluated and every residual becomes NaN
     w.ctl->overflow = over ? 1 : 0;
+    w.ctl->engine_error = 0;
     w.ctl->nbm = over ? 0 : carry[0];
     w.ctl->nbp = over ? 0 : carry[1];
     w.ctl->jm = over ? 0 : jm;
@@ -289,7 +290,7 @@ __global__ void k_loss_final(Workspace w, int64_t B, double* __restrict__ loss_o
   for (int64_t i = threadIdx.x; i < w.nres; i += blockDim.x) v += w.lossp[i];
   for (int64_t i = threadIdx.x; i < 2 * w.fgrid; i += blockDim.x) v += w.floss[i];
   const double t = block_sum_d(v);
-  if (threadIdx.x == 0) *loss_out = t / (double)B;
+  if (threadIdx.x == 0) *loss_out = w.ctl->engine_error ? nan("") : t / (double)B;
 }
 
 // columns [0, Pm) belong to the u- network; rows_m / rows_p partial rows hold each network's
@@ -300,7 +301,7 @@ __global__ void k_grad_reduce(Workspace w, int P, int Pm, int rows_m, int rows_p
   const int rows = i < Pm ? rows_m : rows_p;
   float v = 0.0f;
   for (int c = 0; c < rows; ++c) v += w.partials[(size_t)c * P + i];
-  grad_out[i] = v;
+  grad_out[i] = w.ctl->engine_error ? nanf("") : v;
 }
 
 __global__ void k_adam(dips_adam_t hp, int P, float* __restrict__ params, const float* __restrict__ grad,
@@ -410,18 +411,21 @@ const ArchOps* arch_ops_1_1_2_10();
 const ArchOps* arch_ops_2_8_2_8();
 const ArchOps* arch_ops_2_16_2_16();
 const ArchOps* arch_ops_3_32_3_32();
+const ArchOps* arch_ops_4_64_4_64();
 
 static const ArchOps* find_arch(const dips_arch_t* a) {
   if (!a) {
     set_error("null arch");
     return nullptr;
   }
-  const ArchOps* table[] = {arch_ops_1_1_2_10(), arch_ops_2_8_2_8(), arch_ops_2_16_2_16(), arch_ops_3_32_3_32()};
+  const ArchOps* table[] = {arch_ops_1_1_2_10(), arch_ops_2_8_2_8(), arch_ops_2_16_2_16(), arch_ops_3_32_3_32(),
+                            arch_ops_4_64_4_64()};
   for (const ArchOps* o : table)
     if (o->m_layers == a->m_layers && o->m_width == a->m_width && o->p_layers == a->p_layers &&
         o->p_width == a->p_width)
       return o;
-  set_error("no kernel compiled for DoubleMLP m=%dx%d p=%dx%d (supported: 1x1/2x10, 2x8/2x8, 2x16/2x16, 3x32/3x32)",
+  set_error("no kernel compiled for DoubleMLP m=%dx%d p=%dx%d (supported: 1x1/2x10, 2x8/2x8, 2x16/2x16, 3x32/3x32, "
+            "4x64/4x64)",
             a->m_layers, a->m_width, a->p_layers, a->p_width);
   return nullptr;
 }
@@ -471,11 +475,11 @@ static int prep_ws(const dips_arch_t* arch, int64_t B, void* ws, size_t ws_bytes
   return DIPS_OK;
 }
 
-static int expand(const dips_records_t* rec, const int32_t* ids, int64_t B, Workspace& W, const Marks* mk,
-                  cudaStream_t s) {
+static int expand(const dips_records_t* rec, const int32_t* ids, int64_t B, Workspace& W, int bulk_ok,
+                  const Marks* mk, cudaStream_t s) {
   const int nblk = (int)W.nblk;
   mark(mk, kMarkStart, s);
-  k_count<<<nblk, kScanBlock, 0, s>>>(ids, B, rec->n_pts, rec->cnt, rec->cnt_m, W);
+  k_count<<<nblk, kScanBlock, 0, s>>>(ids, B, rec->n_pts, rec->cnt, rec->cnt_m, bulk_ok, W);
   k_scan_blocks<<<1, kScanBlock, 0, s>>>(W);
   k_emit<<<nblk, kScanBlock, 0, s>>>(ids, B, *rec, W);
   DIPS_CHECK_LAUNCH("batch expansion");
@@ -486,7 +490,7 @@ static int expand(const dips_records_t* rec, const int32_t* ids, int64_t B, Work
 // expansion, general forward + residual, fused bulk kernel (with or without its gradient)
 static int run_forward(const ArchOps* ops, const dips_records_t* rec, const int32_t* ids, int64_t B, Workspace& W,
                        double* loss_out, float* residual_out, bool fused_bwd, const Marks* mk, cudaStream_t s) {
-  int st = expand(rec, ids, B, W, mk, s);
+  int st = expand(rec, ids, B, W, ops->bulk_ok, mk, s);
   if (st) return st;
   st = ops->job_forward(make_ph(rec), ids, W, mk, s);
   if (st) return st;

@@ -604,6 +604,7 @@ const ArchOps* DIPS_GETTER() {
                               DIPS_WP,           DIPS_NS::A::kParams,
                               DIPS_NS::uses_tile<DIPS_NS::A::M>() ? 1 : 0,
                               DIPS_NS::uses_tile<DIPS_NS::A::P>() ? 1 : 0,
+                              1,
                               DIPS_NS::load_params,
                               DIPS_NS::job_forward, DIPS_NS::job_adjoint, DIPS_NS::bulk_fused,
                               DIPS_NS::mlp_eval};

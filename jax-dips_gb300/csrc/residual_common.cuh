@@ -22,6 +22,7 @@ struct Ctl {
   int64_t jm, jp, jm_pad, total;  // jobs of the general points: u-, u+, padded u- count, all
   int64_t overflow;               // 1 when the batch's jobs exceed the workspace's job capacity
   int64_t nbm, nbp;               // bulk points (7 jobs of one network) of the u- / u+ network
+  int64_t engine_error;           // nonzero when a tensor-core wait gave up (the loss and gradient become NaN)
 };
 
 // Step workspace, carved from one caller-owned buffer.  Bulk points go to the fused kernel
@@ -96,7 +97,8 @@ inline void mark(const Marks* m, int slot, cudaStream_t s) {
 struct ArchOps {
   int m_layers, m_width, p_layers, p_width;
   int n_params;
-  int tile_m, tile_p;  // 1: the network runs on the register-blocked engine (kTileGrid gradient rows)
+  int tile_m, tile_p;  // 1: the network's gradient comes in kTileGrid partial rows (tile engines)
+  int bulk_ok;         // 0: no bulk-point kernel; every point is expanded into jobs
   int (*load_params)(const float* params, cudaStream_t s);
   int (*job_forward)(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s);
   int (*job_adjoint)(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s);

@@ -35,6 +35,7 @@ UNITS = {
     "residual_a3_32_3_32.cu": [],
     "krylov.cu": [],
     "residual_static.cu": [],
+    "residual_tc.cu": [],
 }
 
 _lock = threading.Lock()

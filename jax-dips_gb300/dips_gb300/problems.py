@@ -218,6 +218,84 @@ def _assemble(phi, u_m, u_p, mu_m, mu_p, k_m, k_p, f_m, f_p, beta):
 
 
 # ----------------------------------------------------------------------------------------
+# irregular blob (config 5): phi = 0.3 - sum of 500 Gaussians
+# ----------------------------------------------------------------------------------------
+def blob_problem(n_gauss=500, seed=0, iso=0.3, mu_m=1.0, mu_p=100.0, k=0.5):
+    """phi = iso - sum_i exp(-|x - c_i|^2 / (2 w_i^2)), centres uniform in [-0.7, 0.7]^3, widths
+    uniform in [0.05, 0.2] (numpy default_rng(seed)); mu- = 1, mu+ = 100, k+- = 0.5;
+    u- = sin x cos y e^z, u+ = x^2 + y^2 + z^2 (the sphere problem's solution)."""
+    rng = np.random.default_rng(seed)
+    C = rng.uniform(-0.7, 0.7, (n_gauss, 3)).astype(np.float32)
+    Wd = rng.uniform(0.05, 0.2, n_gauss).astype(np.float32)
+    inv2w2 = (1.0 / (2.0 * Wd.astype(np.float64) ** 2)).astype(np.float32)
+    invw2 = (1.0 / Wd.astype(np.float64) ** 2).astype(np.float32)
+    cache = {}
+
+    def _tables(r):
+        if _is_torch(r):
+            key = str(r.device)
+            if key not in cache:
+                cache[key] = tuple(torch.as_tensor(a, device=r.device) for a in (C, inv2w2, invw2))
+            return cache[key]
+        return C, inv2w2, invw2
+
+    def _sum(r, want_grad):
+        """S(x) and (optionally) grad S, points in chunks and Gaussians in blocks of 32."""
+        c, a, b = _tables(r[0])
+        xp = _NS(r[0])
+        M = r[0].shape[0]
+        S = xp.full(0.0)
+        G = [xp.full(0.0), xp.full(0.0), xp.full(0.0)] if want_grad else None
+        step = 1 << 19
+        for p0 in range(0, M, step):
+            p1 = min(M, p0 + step)
+            x, y, z = r[0][p0:p1, None], r[1][p0:p1, None], r[2][p0:p1, None]
+            for g0 in range(0, c.shape[0], 32):
+                g1 = min(c.shape[0], g0 + 32)
+                dx, dy, dz = x - c[g0:g1, 0], y - c[g0:g1, 1], z - c[g0:g1, 2]
+                e = xp.exp(-(dx * dx + dy * dy + dz * dz) * a[g0:g1])
+                S[p0:p1] += e.sum(1)
+                if want_grad:
+                    eb = e * b[g0:g1]
+                    G[0][p0:p1] -= (eb * dx).sum(1)
+                    G[1][p0:p1] -= (eb * dy).sum(1)
+                    G[2][p0:p1] -= (eb * dz).sum(1)
+        return S, G
+
+    def phi(r):
+        S, _ = _sum(r, False)
+        return iso - S
+
+    def u_m(r):
+        x, y, z, xp = _xyz(r)
+        return xp.sin(x) * xp.cos(y) * xp.exp(z)
+
+    def u_p(r):
+        x, y, z, xp = _xyz(r)
+        return x * x + y * y + z * z
+
+    def f_m(r):  # -mu- lap u- + k u-, lap u- = -u-
+        return (mu_m + k) * u_m(r)
+
+    def f_p(r):  # -mu+ lap u+ + k u+, lap u+ = 6
+        return -6.0 * mu_p + k * u_p(r)
+
+    def beta(r):
+        x, y, z, xp = _xyz(r)
+        _, gS = _sum(r, True)
+        gx, gy, gz = -gS[0], -gS[1], -gS[2]  # grad phi = -grad S
+        gn = xp.sqrt(gx * gx + gy * gy + gz * gz)
+        nx, ny, nz = xp.safe_div(gx, gn), xp.safe_div(gy, gn), xp.safe_div(gz, gn)
+        e = xp.exp(z)
+        dn_um = xp.cos(x) * xp.cos(y) * e * nx - xp.sin(x) * xp.sin(y) * e * ny + xp.sin(x) * xp.cos(y) * e * nz
+        dn_up = 2.0 * (x * nx + y * ny + z * nz)
+        return -(mu_p * dn_up - mu_m * dn_um)
+
+    return _assemble(phi, u_m, u_p, lambda r: _xyz(r)[3].full(mu_m), lambda r: _xyz(r)[3].full(mu_p),
+                     lambda r: _xyz(r)[3].full(k), lambda r: _xyz(r)[3].full(k), f_m, f_p, beta)
+
+
+# ----------------------------------------------------------------------------------------
 # linearised Poisson-Boltzmann instances (config 4)
 # ----------------------------------------------------------------------------------------
 def lpbe_problem(centres, radii, charges, sigma=0.02, mu_m=1.0, mu_p=80.0, k_p=0.1):

@@ -42,10 +42,10 @@ def test_arch_table_and_workspace_query():
     from dips_gb300.nn import Arch, n_params
 
     lib = _lib.load()
-    for a in (Arch(1, 1, 2, 10), Arch(3, 32, 3, 32), Arch(2, 16, 2, 16), Arch(2, 8, 2, 8)):
+    for a in (Arch(1, 1, 2, 10), Arch(3, 32, 3, 32), Arch(2, 16, 2, 16), Arch(2, 8, 2, 8), Arch(4, 64, 4, 64)):
         assert lib.dips_arch_supported(a.ctype()) == 1
         assert lib.dips_num_params(a.ctype()) == n_params(a)
-    assert lib.dips_arch_supported(Arch(4, 64, 4, 64).ctype()) == 0
+    assert lib.dips_arch_supported(Arch(2, 64, 2, 64).ctype()) == 0
     small = lib.dips_step_workspace_bytes(Arch().ctype(), 1000, 7000)
     big = lib.dips_step_workspace_bytes(Arch().ctype(), 1000, 70000)
     assert 0 < small < big
