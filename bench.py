@@ -307,9 +307,11 @@ def run_ours(args, rank, world):
     # stencil jobs of each bulk u+ point and the u+ jobs of the other points); for 4x64 the u+
     # tensor-core adjoint (which also recomputes the forward).  3 F per job either way; the
     # forward that feeds the residual and the recompute are not counted.
-    dom_phase = "adjoint_p" if tensor else "fused_p"
-    t_dom = phase_med[dom_phase] / 1e3
-    dom_flops = 3 * jobs_p * f_p
+    kind = "adjoint" if tensor else "fused"
+    dom_net = "p" if phase_med[f"{kind}_p"] >= phase_med[f"{kind}_m"] else "m"
+    t_dom = phase_med[f"{kind}_{dom_net}"] / 1e3
+    dom_jobs, dom_f = (jobs_p, f_p) if dom_net == "p" else (jobs_m, f_m)
+    dom_flops = 3 * dom_jobs * dom_f
     # FP32 FMA peak of this GPU (measured)
     probe = torch.empty(152 * 16 * 256, dtype=torch.float32, device=dev)
     iters = 4096
@@ -389,14 +391,14 @@ def run_ours(args, rank, world):
                        "l2": "flushed (256 MB write) between timed steps", "cuda_graph": world == 1,
                        "setup_s": setup_s, "wall_s_timed": wall},
             "roofline": {"bound": "tensor" if tensor else "fp32",
-                         "kernel": ("tcnet::k_tc_adjoint<u+ net> (tcgen05 TF32: recomputed forward, adjoint and "
-                                    "dW of every u+ job)" if tensor else
-                                    "tile::k_tile_net<u+ net, backward> (forward, bulk residual, adjoint and dW of "
-                                    "every u+ job of the batch)"),
+                         "kernel": (f"tcnet::k_tc_adjoint<u{'+' if dom_net == 'p' else '-'} net> (tcgen05 TF32: "
+                                    "recomputed forward, adjoint and dW of every job of that network)" if tensor else
+                                    f"tile::k_tile_net<u{'+' if dom_net == 'p' else '-'} net, backward> (forward, bulk "
+                                    "residual, adjoint and dW of every job of that network)"),
                          "achieved": dom_tflops, "peak": dom_peak, "unit": "TFLOP/s",
                          "frac": dom_tflops / dom_peak, "traffic": FUSED_TRAFFIC.get((args.n, B)),
-                         "algorithmic": f"3 x F(u+) per u+ job, F = sum(2*in*out+out) + tanh count = {f_p}; "
-                                        f"{jobs_p} u+ jobs per launch ({bulk_p} bulk u+ points)",
+                         "algorithmic": f"3 x F per job of the network, F = sum(2*in*out+out) + tanh count = "
+                                        f"{dom_f}; {dom_jobs} jobs per launch (bulk points: {bulk_m} u-, {bulk_p} u+)",
                          "peak_source": peak_src, "fp32_peak_tflops": fp32_peak,
                          "phase_ms": phase_med,
                          "step_tflops": step_tflops, "step_frac": step_tflops / fp32_peak,

@@ -9,7 +9,8 @@
 //   k_tc_adjoint   forward again (the activations are recomputed, not stored between kernels),
 //                  then dL/dtheta accumulated over all jobs of the network
 //
-// One CTA of 128 threads owns a tile of 128 jobs at a time; thread t is job t and TMEM lane t.
+// One CTA of 256 threads owns a tile of 128 jobs at a time.  Job t is TMEM lane t; it is served
+// by two threads, warps w and w + 4 (w = t / 32), which take features [0, 32) and [32, 64).
 // Per hidden-hidden layer the product [128 jobs x 64] x [64 x 64] is one tcgen05.mma group
 // (M = 128, N = 64, eight K = 8 steps) whose A operand (the activations, job-major) sits in
 // TMEM and whose B operand (the weights) sits in shared memory.  The bias, tanh and the
@@ -39,8 +40,9 @@ constexpr int kParams = 2 * kNetParams;
 constexpr int kOut = 4 * W + (L - 1) * (W * W + W);  // offset of the output weights in a network
 __host__ __device__ constexpr int layer_off(int l) { return l == 0 ? 0 : 4 * W + (l - 1) * (W * W + W); }
 
-constexpr int kThreads = 128;
+constexpr int kThreads = 256;  // two threads per job: features [0, 32) and [32, 64)
 constexpr int kTile = 128;
+constexpr int kHalf = 32;
 constexpr int kGrid = kTileGrid;
 constexpr uint32_t kWaitLimit = 1u << 24;
 
@@ -59,7 +61,7 @@ __device__ __forceinline__ int foff(int r, int j) { return (r >> 3) * kSboJ + (j
 // the weight-gradient accumulators of the adjoint
 constexpr uint32_t cD = 0, cA = 64, cW2 = 128, cW3 = 200, cW4 = 272, cW1 = 344, cWO = 352;
 constexpr uint32_t kFwdCols = 128, kAdjCols = 512;
-constexpr int kFwdCtasPerSm = 4;  // 4 x 128 TMEM columns, 4 x 50 KB shared memory
+constexpr int kFwdCtasPerSm = 2;  // 2 x 256 threads at <= 128 registers
 
 // small tables (floats) shared by both kernels: W1[3][64], b[4][64], wo[64], bo
 constexpr int kSmallFloats = 3 * W + 4 * W + W + 4;
@@ -178,22 +180,22 @@ __device__ __forceinline__ void tmem_free(uint32_t base, uint32_t cols) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(base), "r"(cols));
 }
 
-// h1 = tanh(W1^T x + b1) on the FP32 pipe
-__device__ __forceinline__ void layer1(const float* small, const float x[3], float* h) {
+// h1 = tanh(W1^T x + b1) for features [f0, f0 + 32), on the FP32 pipe
+__device__ __forceinline__ void layer1(const float* small, const float x[3], float* h, int f0) {
 #pragma unroll
-  for (int o = 0; o < W; ++o) {
-    float z = small[3 * W + o];
-    z = fmaf(x[0], small[o], z);
-    z = fmaf(x[1], small[W + o], z);
-    z = fmaf(x[2], small[2 * W + o], z);
+  for (int o = 0; o < kHalf; ++o) {
+    float z = small[3 * W + f0 + o];
+    z = fmaf(x[0], small[f0 + o], z);
+    z = fmaf(x[1], small[W + f0 + o], z);
+    z = fmaf(x[2], small[2 * W + f0 + o], z);
     h[o] = tanh_f(z);
   }
 }
 
-// this thread's 64 values into its TMEM lane, columns [col, col + 64), rounded to TF32
+// this thread's 32 values into its TMEM lane, columns [col, col + 32), rounded to TF32
 __device__ __forceinline__ void to_tmem(uint32_t lane_base, uint32_t col, const float* v) {
 #pragma unroll
-  for (int c = 0; c < W; c += 16) {
+  for (int c = 0; c < kHalf; c += 16) {
     float t[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) t[q] = tf32(v[c + q]);
@@ -202,12 +204,12 @@ __device__ __forceinline__ void to_tmem(uint32_t lane_base, uint32_t col, const 
 }
 __device__ __forceinline__ void from_tmem(uint32_t lane_base, uint32_t col, float* v) {
 #pragma unroll
-  for (int c = 0; c < W; c += 16) tld16(lane_base + col + c, v + c);
+  for (int c = 0; c < kHalf; c += 16) tld16(lane_base + col + c, v + c);
 }
-// this thread's column (job t) of a feature-major matrix, rows [0, 64)
-__device__ __forceinline__ void to_fm(unsigned char* m, int t, const float* v) {
+// rows [f0, f0 + 32) of column t (this thread's job) of a feature-major matrix
+__device__ __forceinline__ void to_fm(unsigned char* m, int t, const float* v, int f0) {
 #pragma unroll
-  for (int r = 0; r < W; ++r) *reinterpret_cast<float*>(m + foff(r, t)) = tf32(v[r]);
+  for (int r = 0; r < kHalf; ++r) *reinterpret_cast<float*>(m + foff(f0 + r, t)) = tf32(v[r]);
 }
 __device__ __forceinline__ float fm_at(const unsigned char* m, int r, int t) {
   return *reinterpret_cast<const float*>(m + foff(r, t));
@@ -247,17 +249,19 @@ __device__ __forceinline__ void issue_dw(uint32_t d, const unsigned char* a, uin
 // ---- forward kernel -------------------------------------------------------------------------
 constexpr size_t kFwdSmem = 3 * kWBytes + sizeof(float) * kSmallFloats + 64;
 
-__global__ void __launch_bounds__(kThreads, 1) k_tc_forward(const float* __restrict__ params, int off, Workspace w,
-                                                            int net_p) {
+__global__ void __launch_bounds__(kThreads, kFwdCtasPerSm) k_tc_forward(const float* __restrict__ params, int off,
+                                                                        Workspace w, int net_p) {
   extern __shared__ __align__(1024) unsigned char sm[];
   unsigned char* wf = sm;
   float* small = reinterpret_cast<float*>(sm + 3 * kWBytes);
   uint64_t* bar = reinterpret_cast<uint64_t*>(small + kSmallFloats);
   uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
   __shared__ int s_abort;
-  const int t = threadIdx.x, warp = t >> 5;
+  __shared__ float s_u[kTile];  // partial output sums of the features [32, 64)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int job = 32 * (warp & 3) + lane, f0 = kHalf * (warp >> 2);
   load_weights<false>(params + off, wf, nullptr, small);
-  if (t == 0) {
+  if (threadIdx.x == 0) {
     s_abort = 0;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(1));
     asm volatile("fence.mbarrier_init.release.cluster;");
@@ -265,13 +269,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_forward(const float* __restr
   tmem_alloc(slot, kFwdCols);
   sync_for_mma();
   const uint32_t tb = *slot;
-  const uint32_t lb = tb + ((uint32_t)(32 * warp) << 16);  // this warp's TMEM lane quarter
+  const uint32_t lb = tb + ((uint32_t)(32 * (warp & 3)) << 16);  // this warp's TMEM lane quarter
   const Ctl ctl = *w.ctl;
   const int64_t jbeg = net_p ? ctl.jm_pad : 0, jend = net_p ? ctl.total : ctl.jm;
   const int64_t ntiles = (jend - jbeg + kTile - 1) / kTile;
   uint32_t phase = 0;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t j = jbeg + tile * kTile + t;
+    const int64_t j = jbeg + tile * kTile + job;
     float x[3] = {0.0f, 0.0f, 0.0f};
     if (j < jend) {
       const float4 xv = w.jx[j];
@@ -279,13 +283,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_forward(const float* __restr
       x[1] = xv.y;
       x[2] = xv.z;
     }
-    float h[W];
-    layer1(small, x, h);
+    float h[kHalf];
+    layer1(small, x, h, f0);
     for (int l = 0; l < 3; ++l) {
-      to_tmem(lb, cA, h);
+      to_tmem(lb, cA + f0, h);
       sync_for_mma();
       if (s_abort) break;
-      if (t == 0) {
+      if (threadIdx.x == 0) {
         issue_fwd(tb, wf + l * kWBytes);
         commit(bar);
       }
@@ -295,15 +299,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_forward(const float* __restr
       }
       phase ^= 1;
       fence_after();
-      from_tmem(lb, cD, h);
+      from_tmem(lb, cD + f0, h);
 #pragma unroll
-      for (int o = 0; o < W; ++o) h[o] = tanh_f(h[o] + small[3 * W + (l + 1) * W + o]);
+      for (int o = 0; o < kHalf; ++o) h[o] = tanh_f(h[o] + small[3 * W + (l + 1) * W + f0 + o]);
     }
-    if (s_abort) break;
-    float u = small[8 * W];
+    // (an abort is acted on at the next barrier, where every thread sees the flag)
+    float u = 0.0f;
 #pragma unroll
-    for (int o = 0; o < W; ++o) u = fmaf(small[7 * W + o], h[o], u);
-    if (j < jend) w.ju[j] = u;
+    for (int o = 0; o < kHalf; ++o) u = fmaf(small[7 * W + f0 + o], h[o], u);
+    if (f0) s_u[job] = u;
+    __syncthreads();
+    if (!f0 && j < jend) w.ju[j] = u + s_u[job] + small[8 * W];
   }
   fence_before();
   __syncthreads();
@@ -335,6 +341,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
   uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
   __shared__ int s_abort;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int job = 32 * (warp & 3) + lane, f0 = kHalf * (warp >> 2);
   load_weights<true>(params + off, wf, wb, small);
   // constant rows: 64 = ones (the bias input) and 65..71 = 0 in the 72-row matrices; rows 1..7
   // of GX and rows 64..71 of the 72-row matrices are never rewritten
@@ -354,7 +361,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
   tmem_alloc(slot, kAdjCols);
   sync_for_mma();
   const uint32_t tb = *slot;
-  const uint32_t lb = tb + ((uint32_t)(32 * warp) << 16);
+  const uint32_t lb = tb + ((uint32_t)(32 * (warp & 3)) << 16);
   const Ctl ctl = *w.ctl;
   const int64_t jbeg = net_p ? ctl.jm_pad : 0, jend = net_p ? ctl.total : ctl.jm;
   const int64_t ntiles = (jend - jbeg + kTile - 1) / kTile;
@@ -369,7 +376,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     fence_after();
   };
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t j = jbeg + tile * kTile + t;
+    const int64_t j = jbeg + tile * kTile + job;
     float x[3] = {0.0f, 0.0f, 0.0f};
     float g = 0.0f;
     if (j < jend) {
@@ -380,9 +387,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
       g = w.jg[j];
     }
     // ---- forward, keeping h2^T and h3^T
-    float h[W];
-    layer1(small, x, h);
-    to_tmem(lb, cA, h);
+    float h[kHalf];
+    layer1(small, x, h, f0);
+    to_tmem(lb, cA + f0, h);
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -390,11 +397,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
       commit(bar);
     }
     wait();
-    from_tmem(lb, cD, h);
+    from_tmem(lb, cD + f0, h);
 #pragma unroll
-    for (int o = 0; o < W; ++o) h[o] = tanh_f(h[o] + small[4 * W + o]);
-    to_tmem(lb, cA, h);
-    to_fm(H2, t, h);
+    for (int o = 0; o < kHalf; ++o) h[o] = tanh_f(h[o] + small[4 * W + f0 + o]);
+    to_tmem(lb, cA + f0, h);
+    to_fm(H2, job, h, f0);
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -402,11 +409,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
       commit(bar);
     }
     wait();
-    from_tmem(lb, cD, h);
+    from_tmem(lb, cD + f0, h);
 #pragma unroll
-    for (int o = 0; o < W; ++o) h[o] = tanh_f(h[o] + small[5 * W + o]);
-    to_tmem(lb, cA, h);
-    to_fm(H3, t, h);
+    for (int o = 0; o < kHalf; ++o) h[o] = tanh_f(h[o] + small[5 * W + f0 + o]);
+    to_tmem(lb, cA + f0, h);
+    to_fm(H3, job, h, f0);
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -414,15 +421,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
       commit(bar);
     }
     wait();
-    from_tmem(lb, cD, h);
+    from_tmem(lb, cD + f0, h);
 #pragma unroll
-    for (int o = 0; o < W; ++o) h[o] = tanh_f(h[o] + small[6 * W + o]);  // h4
+    for (int o = 0; o < kHalf; ++o) h[o] = tanh_f(h[o] + small[6 * W + f0 + o]);  // h4
     // ---- output layer: dWo, dbo = sum_j g_j [h4, 1]  (A = [g] replicated, B = h4^T with its ones row)
-    to_fm(Z, t, h);
-    *reinterpret_cast<float*>(GX + foff(0, t)) = tf32(g);
-    *reinterpret_cast<float*>(GX + foff(1, t)) = 0.0f;
-    *reinterpret_cast<float*>(GX + foff(2, t)) = 0.0f;
-    *reinterpret_cast<float*>(GX + foff(3, t)) = 0.0f;
+    to_fm(Z, job, h, f0);
+    if (!f0) {
+      *reinterpret_cast<float*>(GX + foff(0, job)) = tf32(g);
+      *reinterpret_cast<float*>(GX + foff(1, job)) = 0.0f;
+      *reinterpret_cast<float*>(GX + foff(2, job)) = 0.0f;
+      *reinterpret_cast<float*>(GX + foff(3, job)) = 0.0f;
+    }
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -432,9 +441,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     wait();
     // delta4 = g wo (1 - h4^2)
 #pragma unroll
-    for (int o = 0; o < W; ++o) h[o] = g * small[7 * W + o] * fmaf(-h[o], h[o], 1.0f);
-    to_tmem(lb, cA, h);
-    to_fm(Z, t, h);
+    for (int o = 0; o < kHalf; ++o) h[o] = g * small[7 * W + f0 + o] * fmaf(-h[o], h[o], 1.0f);
+    to_tmem(lb, cA + f0, h);
+    to_fm(Z, job, h, f0);
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -444,14 +453,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     }
     wait();
     // delta3 = (W4 delta4) (1 - h3^2)
-    from_tmem(lb, cD, h);
+    from_tmem(lb, cD + f0, h);
 #pragma unroll
-    for (int o = 0; o < W; ++o) {
-      const float a = fm_at(H3, o, t);
+    for (int o = 0; o < kHalf; ++o) {
+      const float a = fm_at(H3, f0 + o, job);
       h[o] *= fmaf(-a, a, 1.0f);
     }
-    to_tmem(lb, cA, h);
-    to_fm(Z, t, h);
+    to_tmem(lb, cA + f0, h);
+    to_fm(Z, job, h, f0);
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -461,17 +470,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     }
     wait();
     // delta2 = (W3 delta3) (1 - h2^2); h1 recomputed into H3
-    from_tmem(lb, cD, h);
+    from_tmem(lb, cD + f0, h);
 #pragma unroll
-    for (int o = 0; o < W; ++o) {
-      const float a = fm_at(H2, o, t);
+    for (int o = 0; o < kHalf; ++o) {
+      const float a = fm_at(H2, f0 + o, job);
       h[o] *= fmaf(-a, a, 1.0f);
     }
-    float h1[W];
-    layer1(small, x, h1);
-    to_fm(H3, t, h1);
-    to_tmem(lb, cA, h);
-    to_fm(Z, t, h);
+    float h1[kHalf];
+    layer1(small, x, h1, f0);
+    to_fm(H3, job, h1, f0);
+    to_tmem(lb, cA + f0, h);
+    to_fm(Z, job, h, f0);
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -481,14 +490,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     }
     wait();
     // delta1 = (W2 delta2) (1 - h1^2); dW1^T | db1 = delta1^T [x, y, z, 1]
-    from_tmem(lb, cD, h);
+    from_tmem(lb, cD + f0, h);
 #pragma unroll
-    for (int o = 0; o < W; ++o) h[o] *= fmaf(-h1[o], h1[o], 1.0f);
-    to_fm(Z, t, h);
-    *reinterpret_cast<float*>(GX + foff(0, t)) = tf32(x[0]);
-    *reinterpret_cast<float*>(GX + foff(1, t)) = tf32(x[1]);
-    *reinterpret_cast<float*>(GX + foff(2, t)) = tf32(x[2]);
-    *reinterpret_cast<float*>(GX + foff(3, t)) = 1.0f;
+    for (int o = 0; o < kHalf; ++o) h[o] *= fmaf(-h1[o], h1[o], 1.0f);
+    to_fm(Z, job, h, f0);
+    if (!f0) {
+      *reinterpret_cast<float*>(GX + foff(0, job)) = tf32(x[0]);
+      *reinterpret_cast<float*>(GX + foff(1, job)) = tf32(x[1]);
+      *reinterpret_cast<float*>(GX + foff(2, job)) = tf32(x[2]);
+      *reinterpret_cast<float*>(GX + foff(3, job)) = 1.0f;
+    }
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -505,7 +516,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
   fence_after();
   if (first || s_abort) {
     for (int i = t; i < kNetParams; i += blockDim.x) row[i] = 0.0f;
-  } else {
+  } else if (warp < 4) {
     // M = 64 accumulators: row o sits in lane 32*(o/16) + o%16; lanes 16..31 of each warp idle
     const int o = 16 * warp + lane;
     const bool have = lane < 16;
