@@ -230,6 +230,9 @@ def run_ours(args, rank, world):
     loss = torch.zeros((), dtype=torch.float64, device=dev)
     grad = torch.empty(P, dtype=torch.float32, device=dev)
 
+    # launch-configuration autotuner (process-wide, per device), before any graph capture
+    cta_warps = ops.autotune(arch, params, lvl, ops.batch_ids(lvl.n, B, epoch=0, batch_index=0, seed=99), ws)
+
     def step():
         _lib.check(lib.dips_batch_ids_device(lvl.n, B, nb, 7 + rank, 1, _lib.ptr(opt.count), _lib.ptr(ids),
                                              _lib.stream_handle()), "batch ids")
@@ -389,6 +392,7 @@ def run_ours(args, rank, world):
                                    "h=dx, minibatch drawn uniformly",
                        "global_batch": B * world, "points": int(lvl.n), "jobs_per_step": jobs_m + jobs_p,
                        "l2": "flushed (256 MB write) between timed steps", "cuda_graph": world == 1,
+                       "autotuned_cta_warps": cta_warps,
                        "setup_s": setup_s, "wall_s_timed": wall},
             "roofline": {"bound": "tensor" if tensor else "fp32",
                          "kernel": (f"tcnet::k_tc_adjoint<u{'+' if dom_net == 'p' else '-'} net> (tcgen05 TF32: "

@@ -188,6 +188,15 @@ int dips_train_step_profiled(const dips_arch_t* arch, const dips_adam_t* hp, flo
 int dips_train_step_noalloc(const dips_arch_t* arch, const dips_adam_t* hp, float* params, float* mu, float* nu,
                             int64_t* count, const dips_records_t* rec, const int32_t* batch_ids, int64_t batch,
                             int64_t max_jobs, double* loss_out, float* grad_out, cudaStream_t stream);
+/* Autotuner (no counterpart in the reference): runs the residual forward on this batch, then
+   times each launch configuration of the shape's tunable point kernel (for 3x32: the
+   register-blocked engine as 12 warps x 1 CTA, 6 x 2 or 4 x 3 per SM) and keeps the fastest for
+   the current device, process-wide.  Synchronises `stream`; call it before capturing a graph.
+   *choice_out (host, may be NULL) receives the warps per CTA chosen, 0 when the shape has
+   nothing to tune.  The workspace is left in an unspecified state. */
+int dips_autotune(const dips_arch_t* arch, const float* params, const dips_records_t* rec, const int32_t* batch_ids,
+                  int64_t batch, void* workspace, size_t ws_bytes, int32_t* choice_out, cudaStream_t stream);
+
 /* Batch ids of batch `index` of an epoch: a seeded bijective permutation of 0..n-1
    (uniform minibatches without replacement), written to ids[0..B).  epoch_index and
    seed select the permutation. */

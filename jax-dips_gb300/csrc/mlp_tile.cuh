@@ -24,8 +24,9 @@
 //   delta1 = (delta2 W2^T) (1 - h1^2);  dW1 += x^T delta1
 // The 32x32 weight gradients stay in registers for all tiles a warp processes (64 per lane);
 // bias, input-layer and output-layer gradients are reduce-scattered over the 8 lanes that share
-// a feature block and kept as one register each.  At the end the CTA adds its 12 warps'
-// accumulators into shared memory and writes one partial gradient row.
+// a feature block and kept as one register each.  At the end the CTA adds its warps'
+// accumulators into shared memory and writes one partial gradient row.  12 warps share an SM
+// (168 registers each) as one CTA of 12, two of 6 or three of 4; dips_autotune picks the shape.
 //
 // Tiles: bulk tiles hold 4 bulk points x 7 stencil points (lanes 0..27; lane = 7*point +
 // stencil), whose residual is formed inside the warp from the 7 network values, plus (in the
@@ -34,8 +35,7 @@
 
 namespace tile {
 
-constexpr int kWarps = 12;
-constexpr int kThreads = 32 * kWarps;
+constexpr int kWarpsPerSm = 12;  // 168 registers per thread; CTA shapes 12x1, 6x2, 4x3 (warps x CTAs)
 constexpr int kRS = 36;  // buffer row stride (floats)
 constexpr float kTanhScale = 2.8853900817779268f;  // 2 log2(e): tanh(z) = 1 - 2/(1 + 2^(kTanhScale z))
 
@@ -61,9 +61,15 @@ struct Layout {
   static constexpr int kStageFloats = 160;
   static constexpr int kWarpFloats = kStage + 2 * kStageFloats;
   static constexpr int kWarp0 = (kShared + 3) / 4 * 4;
-  static constexpr int kAcc = kWarp0 + kWarps * kWarpFloats;     // [kParams] CTA gradient accumulator
-  static constexpr int kLoss = (kAcc + N::kParams + 3) / 4 * 4;  // [kWarps] doubles
-  static constexpr size_t kBytes = sizeof(float) * (size_t)kLoss + sizeof(double) * kWarps;
+};
+
+// the CTA-level parts of the layout, for NW warps per CTA
+template <class N, int NW>
+struct CtaLayout {
+  using Lay = Layout<N>;
+  static constexpr int kAcc = Lay::kWarp0 + NW * Lay::kWarpFloats;  // [kParams] CTA gradient accumulator
+  static constexpr int kLoss = (kAcc + N::kParams + 3) / 4 * 4;     // [NW] doubles
+  static constexpr size_t kBytes = sizeof(float) * (size_t)kLoss + sizeof(double) * NW;
 };
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
@@ -377,16 +383,17 @@ __device__ __forceinline__ void flush_acc(float* cta, const Acc& a, int lane) {
 // the warp) and, with BWD, general tiles (32 jobs of the job list).  Writes the loss partial
 // floss[net_p][blockIdx.x] (and zeros the rest of that row of slots), residual_out of the bulk
 // slots, and with BWD the partial gradient row blockIdx.x (columns of this network).
-template <class N, int OFF, bool BWD>
-__global__ void __launch_bounds__(kThreads, 1) k_tile_net(PtsH ph, const int32_t* __restrict__ ids, Workspace w,
+template <class N, int OFF, bool BWD, int NW>
+__global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile_net(PtsH ph, const int32_t* __restrict__ ids, Workspace w,
                                                           dips_records_t rec, int net_p, float* __restrict__ residual_out) {
   using Lay = Layout<N>;
+  using Cta = CtaLayout<N, NW>;
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   load_weights<N, OFF>(sm);
   if (BWD)
-    for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) sm[Lay::kAcc + i] = 0.0f;
+    for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) sm[Cta::kAcc + i] = 0.0f;
   __syncthreads();
   float* wp = sm + Lay::kWarp0 + warp * Lay::kWarpFloats;
   float* X = wp + Lay::kX;
@@ -440,8 +447,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_tile_net(PtsH ph, const int32_t
     cp_commit();
   };
 
-  const int64_t stride = (int64_t)gridDim.x * kWarps;
-  int64_t tile = (int64_t)blockIdx.x * kWarps + warp;
+  const int64_t stride = (int64_t)gridDim.x * NW;
+  int64_t tile = (int64_t)blockIdx.x * NW + warp;
   issue(tile, stage0);
   int sidx = 0;
   for (; tile < nbt + ngt; tile += stride, sidx ^= 1) {
@@ -518,22 +525,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_tile_net(PtsH ph, const int32_t
   }
   cp_wait<0>();
   // loss partial of the CTA
-  double* wl = reinterpret_cast<double*>(sm + Lay::kLoss);
+  double* wl = reinterpret_cast<double*>(sm + Cta::kLoss);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
   if (lane == 0) wl[warp] = lsum;
-  if (BWD) flush_acc<N>(sm + Lay::kAcc, acc, lane);
+  if (BWD) flush_acc<N>(sm + Cta::kAcc, acc, lane);
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
-    for (int q = 0; q < kWarps; ++q) t += wl[q];
-    w.floss[net_p * w.fgrid + blockIdx.x] = t;
+    for (int q = 0; q < NW; ++q) t += wl[q];
+    w.floss[net_p * kLossSlots + blockIdx.x] = t;
+    if (blockIdx.x == 0) {
+      w.ctl->floss_n[net_p] = gridDim.x;
+      if (BWD) w.ctl->grad_rows[net_p] = gridDim.x;
+    }
   }
-  if (blockIdx.x == 0)  // the loss slots beyond this grid (sized for the per-job-thread kernels)
-    for (int i = gridDim.x + threadIdx.x; i < w.fgrid; i += blockDim.x) w.floss[net_p * w.fgrid + i] = 0.0;
   if (BWD) {
     float* row = w.partials + (size_t)blockIdx.x * w.n_params + OFF;
-    for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) row[i] = sm[Lay::kAcc + i];
+    for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) row[i] = sm[Cta::kAcc + i];
   }
 }
 

@@ -47,7 +47,7 @@ static size_t carve(Workspace* w, char* base, int64_t B, int64_t max_jobs, int P
   W.gs = (float*)take(sizeof(float) * B);
   W.blk = (int64_t*)take(sizeof(int64_t) * 4 * (W.nblk + 1));
   W.lossp = (double*)take(sizeof(double) * W.nres);
-  W.floss = (double*)take(sizeof(double) * 2 * W.fgrid);
+  W.floss = (double*)take(sizeof(double) * 2 * kLossSlots);
   W.jslot = (int32_t*)take(sizeof(int32_t) * W.jcap);
   W.jcode = (uint16_t*)take(sizeof(uint16_t) * W.jcap);
   W.jA = (float*)take(sizeof(float) * W.jcap);
@@ -160,6 +160,8 @@ __global__ void k_scan_blocks(Workspace w) {
     // on overflow no job is expanded or evaluated and every residual becomes NaN
     w.ctl->overflow = over ? 1 : 0;
     w.ctl->engine_error = 0;
+    w.ctl->floss_n[0] = w.ctl->floss_n[1] = 0;
+    w.ctl->grad_rows[0] = w.ctl->grad_rows[1] = 0;
     w.ctl->nbm = over ? 0 : carry[0];
     w.ctl->nbp = over ? 0 : carry[1];
     w.ctl->jm = over ? 0 : jm;
@@ -288,19 +290,19 @@ __global__ void k_residual(const int32_t* __restrict__ ids, int64_t B, dips_reco
 __global__ void k_loss_final(Workspace w, int64_t B, double* __restrict__ loss_out) {
   double v = 0.0;
   for (int64_t i = threadIdx.x; i < w.nres; i += blockDim.x) v += w.lossp[i];
-  for (int64_t i = threadIdx.x; i < 2 * w.fgrid; i += blockDim.x) v += w.floss[i];
+  for (int net = 0; net < 2; ++net)
+    for (int64_t i = threadIdx.x; i < w.ctl->floss_n[net]; i += blockDim.x) v += w.floss[net * kLossSlots + i];
   const double t = block_sum_d(v);
   if (threadIdx.x == 0) *loss_out = w.ctl->engine_error ? nan("") : t / (double)B;
 }
 
-// columns [0, Pm) belong to the u- network; rows_m / rows_p partial rows hold each network's
-// gradient (kTileGrid for the register-blocked engine, grid + fgrid otherwise)
-__global__ void k_grad_reduce(Workspace w, int P, int Pm, int rows_m, int rows_p, float* __restrict__ grad_out) {
+// columns [0, Pm) belong to the u- network; Ctl::grad_rows gives each network's partial rows
+__global__ void k_grad_reduce(Workspace w, int P, int Pm, float* __restrict__ grad_out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P) return;
-  const int rows = i < Pm ? rows_m : rows_p;
+  const int64_t rows = w.ctl->grad_rows[i < Pm ? 0 : 1];
   float v = 0.0f;
-  for (int c = 0; c < rows; ++c) v += w.partials[(size_t)c * P + i];
+  for (int64_t c = 0; c < rows; ++c) v += w.partials[(size_t)c * P + i];
   grad_out[i] = w.ctl->engine_error ? nanf("") : v;
 }
 
@@ -511,9 +513,7 @@ static int run_backward(const ArchOps* ops, const dips_records_t* rec, const int
   int st = ops->job_adjoint(make_ph(rec), ids, W, mk, s);
   if (st) return st;
   const int Pm = ops->n_params - net_params(ops->p_layers, ops->p_width);
-  const int legacy_rows = W.grid + W.fgrid;
-  k_grad_reduce<<<div_up(ops->n_params, 256), 256, 0, s>>>(W, ops->n_params, Pm, ops->tile_m ? kTileGrid : legacy_rows,
-                                                           ops->tile_p ? kTileGrid : legacy_rows, grad_out);
+  k_grad_reduce<<<div_up(ops->n_params, 256), 256, 0, s>>>(W, ops->n_params, Pm, grad_out);
   DIPS_CHECK_LAUNCH("gradient reduction");
   mark(mk, kMarkReduce, s);
   return DIPS_OK;
@@ -619,6 +619,31 @@ extern "C" int dips_train_step_profiled(const dips_arch_t* arch, const dips_adam
   const Marks mk = {events, n_events < kMarkCount ? n_events : (int)kMarkCount};
   return train_step(arch, hp, params, mu, nu, count, rec, batch_ids, batch, workspace, ws_bytes, loss_out, grad_out,
                     &mk, stream);
+}
+
+extern "C" int dips_autotune(const dips_arch_t* arch, const float* params, const dips_records_t* rec,
+                             const int32_t* batch_ids, int64_t batch, void* workspace, size_t ws_bytes,
+                             int32_t* choice_out, cudaStream_t stream) {
+  int st = check_rec(rec, batch);
+  if (st) return st;
+  DIPS_REQUIRE(params, DIPS_E_ARG, "dips_autotune: null params");
+  const ArchOps* ops = find_arch(arch);
+  if (!ops) return DIPS_E_UNSUPPORTED;
+  Workspace W;
+  st = prep_ws(arch, batch, workspace, ws_bytes, &W);
+  if (st) return st;
+  st = ops->load_params(params, stream);
+  if (st) return st;
+  int chosen = 0;
+  if (ops->autotune) {
+    // the forward prepares what the timed launches read (job lists, records, dL/du)
+    st = run_forward(ops, rec, batch_ids, batch, W, nullptr, nullptr, false, nullptr, stream);
+    if (st) return st;
+    st = ops->autotune(make_ph(rec), batch_ids, W, *rec, stream, &chosen);
+    if (st) return st;
+  }
+  if (choice_out) *choice_out = chosen;
+  return DIPS_OK;
 }
 
 extern "C" int dips_batch_ids(int64_t n, int64_t epoch_index, uint64_t seed, int64_t batch_index, int64_t batch,

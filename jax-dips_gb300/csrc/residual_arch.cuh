@@ -15,6 +15,9 @@
 
 #include <math.h>
 
+#include <atomic>
+#include <mutex>
+
 #include "residual_common.cuh"
 
 namespace dips {
@@ -400,7 +403,11 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_bulk_fused(PtsH ph, const 
   if (warp == 0) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
-    if (lane == 0) w.floss[net_p * w.fgrid + blockIdx.x] = lsum;
+    if (lane == 0) w.floss[net_p * kLossSlots + blockIdx.x] = lsum;
+    if (lane == 0 && blockIdx.x == 0) {
+      w.ctl->floss_n[net_p] = gridDim.x;
+      if (BWD) w.ctl->grad_rows[net_p] = w.grid + gridDim.x;  // adjoint rows, then these
+    }
   }
   if (BWD) {
     __syncthreads();
@@ -543,19 +550,52 @@ static int job_adjoint(const PtsH& ph, const int32_t* ids, const Workspace& w, c
   return DIPS_OK;
 }
 
+// CTA shape of the tile engine per device: 12 warps x 1 CTA (default), 6 x 2 or 4 x 3 per SM,
+// chosen by dips_autotune
+constexpr int kMaxDevices = 64;
+static std::atomic<int> g_tile_nw[kMaxDevices];
+static std::mutex g_tune_mu;
+
+static int current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return -1;
+  return dev;
+}
+
+static int tile_nw() {
+  const int dev = current_device();
+  const int v = dev < 0 ? 0 : g_tile_nw[dev].load(std::memory_order_relaxed);
+  return v ? v : tile::kWarpsPerSm;
+}
+
+template <class N, int OFF, bool BWD, int NW>
+static int tile_launch(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
+                       float* residual_out, int net_p, cudaStream_t s) {
+  constexpr size_t bytes = tile::CtaLayout<N, NW>::kBytes;
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(tile::k_tile_net<N, OFF, BWD, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)bytes);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(tile engine smem)");
+    attr_done = true;
+  }
+  tile::k_tile_net<N, OFF, BWD, NW><<<kTileGrid * (tile::kWarpsPerSm / NW), 32 * NW, bytes, s>>>(ph, ids, w, rec, net_p,
+                                                                                                 residual_out);
+  return DIPS_OK;
+}
+
 template <class N, int OFF, bool BWD>
 static int fused_launch(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
                         float* residual_out, int net_p, cudaStream_t s) {
   if constexpr (uses_tile<N>()) {
-    constexpr size_t bytes = tile::Layout<N>::kBytes;
-    static bool attr_done = false;
-    if (!attr_done) {
-      cudaError_t e = cudaFuncSetAttribute(tile::k_tile_net<N, OFF, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)bytes);
-      if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(tile engine smem)");
-      attr_done = true;
+    switch (tile_nw()) {
+      case 6:
+        return tile_launch<N, OFF, BWD, 6>(ph, ids, w, rec, residual_out, net_p, s);
+      case 4:
+        return tile_launch<N, OFF, BWD, 4>(ph, ids, w, rec, residual_out, net_p, s);
+      default:
+        return tile_launch<N, OFF, BWD, 12>(ph, ids, w, rec, residual_out, net_p, s);
     }
-    tile::k_tile_net<N, OFF, BWD><<<kTileGrid, tile::kThreads, bytes, s>>>(ph, ids, w, rec, net_p, residual_out);
   } else {
     constexpr size_t bytes = fused_smem_bytes<N>();
     static bool attr_done = false;
@@ -597,17 +637,62 @@ static int mlp_eval(const float* pts, const float* phi, int64_t n, float* u, flo
   return DIPS_OK;
 }
 
+
+// Times the backward launches of both networks under each CTA shape (one warm-up, then three
+// timed repetitions on the caller's stream, which is synchronised) and keeps the fastest for
+// the current device.
+static int autotune(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec, cudaStream_t s,
+                    int* chosen) {
+  *chosen = 0;
+  if constexpr (!uses_tile<typename A::M>() && !uses_tile<typename A::P>()) {
+    return DIPS_OK;
+  } else {
+    const int dev = current_device();
+    DIPS_REQUIRE(dev >= 0, DIPS_E_CUDA, "autotune: no current device");
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+      return cuda_status(cudaGetLastError(), "autotune: cudaEventCreate");
+    const int cand[3] = {12, 6, 4};
+    float best = 3.4e38f;
+    int best_nw = tile::kWarpsPerSm;
+    int st = DIPS_OK;
+    for (int c : cand) {
+      g_tile_nw[dev].store(c);
+      for (int r = 0; r < 4 && !st; ++r) {
+        if (r == 1) cudaEventRecord(e0, s);
+        st = bulk_fused(ph, ids, w, rec, nullptr, true, nullptr, s);
+      }
+      cudaEventRecord(e1, s);
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (st || e != cudaSuccess) {
+        if (!st) st = cuda_status(e, "autotune: timing");
+        break;
+      }
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) {
+        best = ms;
+        best_nw = c;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    g_tile_nw[dev].store(st ? 0 : best_nw);
+    if (!st) *chosen = best_nw;
+    return st;
+  }
+}
+
 }  // namespace DIPS_NS
 
 const ArchOps* DIPS_GETTER() {
   static const ArchOps ops = {DIPS_LM,           DIPS_WM,          DIPS_LP,
                               DIPS_WP,           DIPS_NS::A::kParams,
-                              DIPS_NS::uses_tile<DIPS_NS::A::M>() ? 1 : 0,
-                              DIPS_NS::uses_tile<DIPS_NS::A::P>() ? 1 : 0,
                               1,
                               DIPS_NS::load_params,
                               DIPS_NS::job_forward, DIPS_NS::job_adjoint, DIPS_NS::bulk_fused,
-                              DIPS_NS::mlp_eval};
+                              DIPS_NS::mlp_eval, DIPS_NS::autotune};
   return &ops;
 }
 

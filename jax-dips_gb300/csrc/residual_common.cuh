@@ -11,9 +11,10 @@ constexpr int kAdjThreads = 256;     // adjoint CTA: 8 warps
 constexpr int kAdjGrid = 152 * 2;    // two adjoint CTAs per SM (GB300 has 152 SMs)
 constexpr int kFusedThreads = 224;   // fused bulk CTA: one warp per stencil point
 constexpr int kFusedGrid = 152 * 2;
-constexpr int kTileGrid = 152;
+constexpr int kTileGrid = 152;  // register-blocked engine: 12 warps per SM (one CTA of 12 by default)
+constexpr int kLossSlots = 512;  // per-network capacity of the per-CTA loss partials
 // bulk point record (16 floats): point, lhs0, A of stencil points 0..6, diag, rod, batch slot
-constexpr int kRecP = 0, kRecLhs0 = 3, kRecA = 4, kRecDiag = 11, kRecRod = 12, kRecSlot = 13, kRecFloats = 16;  // register-blocked engine: one 12-warp CTA per SM
+constexpr int kRecP = 0, kRecLhs0 = 3, kRecA = 4, kRecDiag = 11, kRecRod = 12, kRecSlot = 13, kRecFloats = 16;
 
 // ----------------------------------------------------------------------------------------
 // workspace
@@ -23,6 +24,8 @@ struct Ctl {
   int64_t overflow;               // 1 when the batch's jobs exceed the workspace's job capacity
   int64_t nbm, nbp;               // bulk points (7 jobs of one network) of the u- / u+ network
   int64_t engine_error;           // nonzero when a tensor-core wait gave up (the loss and gradient become NaN)
+  int64_t floss_n[2];             // per-CTA loss partials written by the point kernels of each network
+  int64_t grad_rows[2];           // partial gradient rows written for each network
 };
 
 // Step workspace, carved from one caller-owned buffer.  Bulk points go to the fused kernel
@@ -39,7 +42,7 @@ struct Workspace {
   float* gs;         // [B] d loss / d lhs of general slots
   int64_t* blk;      // [4*(nblk+1)] block sums, then block offsets
   double* lossp;     // [nres] loss partials of general slots
-  double* floss;     // [2*fgrid] loss partials of the fused kernels
+  double* floss;     // [2][kLossSlots] per-CTA loss partials of the point kernels (count in Ctl::floss_n)
   int32_t* jslot;
   uint16_t* jcode;
   float* jA;
@@ -47,7 +50,7 @@ struct Workspace {
   float4* jx;        // [jcap] job coordinates (w unused)
   float* jg;         // [jcap] d loss / d u of the job
   float* brec;       // [2][B][16] bulk point records, in bulk-list order (layout: kRec* below)
-  float* partials;   // [2*grid][P]: rows [0, grid) general adjoint, [grid, 2*grid) fused
+  float* partials;   // [grid + fgrid][P] partial gradient rows (count per network in Ctl::grad_rows)
   float* grad;       // [P]
   int64_t nblk, nres, jcap, B;
   int grid, fgrid;
@@ -97,8 +100,7 @@ inline void mark(const Marks* m, int slot, cudaStream_t s) {
 struct ArchOps {
   int m_layers, m_width, p_layers, p_width;
   int n_params;
-  int tile_m, tile_p;  // 1: the network's gradient comes in kTileGrid partial rows (tile engines)
-  int bulk_ok;         // 0: no bulk-point kernel; every point is expanded into jobs
+  int bulk_ok;  // 0: no bulk-point kernel; every point is expanded into jobs
   int (*load_params)(const float* params, cudaStream_t s);
   int (*job_forward)(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s);
   int (*job_adjoint)(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s);
@@ -107,6 +109,10 @@ struct ArchOps {
   int (*bulk_fused)(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
                     float* residual_out, bool bwd, const Marks* mk, cudaStream_t s);
   int (*mlp_eval)(const float* pts, const float* phi, int64_t n, float* u, float* g, cudaStream_t s);
+  // times the shape's tunable launch configurations on a prepared workspace and keeps the
+  // fastest for the current device (NULL: nothing to tune); *chosen = the choice (0: none)
+  int (*autotune)(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec, cudaStream_t s,
+                  int* chosen);
 };
 
 }  // namespace dips

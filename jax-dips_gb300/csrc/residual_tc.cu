@@ -511,6 +511,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
   }
   // ---- partial gradient row of this CTA (columns of this network)
   float* row = w.partials + (size_t)blockIdx.x * w.n_params + off;
+  if (t == 0 && blockIdx.x == 0) w.ctl->grad_rows[net_p] = gridDim.x;
   fence_before();
   __syncthreads();
   fence_after();
@@ -642,11 +643,9 @@ static int job_adjoint(const PtsH&, const int32_t*, const Workspace& w, const Ma
   return DIPS_OK;
 }
 
-// no bulk points for this shape: only the loss slots of the bulk kernels are cleared
-static int bulk_fused(const PtsH&, const int32_t*, const Workspace& w, const dips_records_t&, float*, bool,
+// no bulk points for this shape (their loss-partial count stays 0)
+static int bulk_fused(const PtsH&, const int32_t*, const Workspace&, const dips_records_t&, float*, bool,
                       const Marks* mk, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(w.floss, 0, sizeof(double) * 2 * w.fgrid, s);
-  if (e != cudaSuccess) return cuda_status(e, "cudaMemsetAsync(loss slots)");
   mark(mk, kMarkFusedM, s);
   mark(mk, kMarkFusedP, s);
   return DIPS_OK;
@@ -664,8 +663,8 @@ static int mlp_eval(const float* pts, const float* phi, int64_t n, float* u, flo
 }  // namespace tcnet
 
 const ArchOps* arch_ops_4_64_4_64() {
-  static const ArchOps ops = {4, 64, 4, 64, tcnet::kParams, 1, 1, 0, tcnet::load_params, tcnet::job_forward,
-                              tcnet::job_adjoint, tcnet::bulk_fused, tcnet::mlp_eval};
+  static const ArchOps ops = {4, 64, 4, 64, tcnet::kParams, 0, tcnet::load_params, tcnet::job_forward,
+                              tcnet::job_adjoint, tcnet::bulk_fused, tcnet::mlp_eval, nullptr};
   return &ops;
 }
 

@@ -230,6 +230,10 @@ _SIGS = {
         [P(ArchT), P(AdamT), c_void_p, c_void_p, c_void_p, c_void_p, P(RecordsT), c_void_p, c_i64, c_i64, c_void_p,
          c_void_p, c_void_p],
     ),
+    "dips_autotune": (
+        c_i32,
+        [P(ArchT), c_void_p, P(RecordsT), c_void_p, c_i64, c_void_p, ctypes.c_size_t, P(c_i32), c_void_p],
+    ),
     "dips_batch_ids": (c_i32, [c_i64, c_i64, ctypes.c_uint64, c_i64, c_i64, c_void_p, c_void_p]),
     "dips_batch_ids_device": (c_i32, [c_i64, c_i64, c_i64, ctypes.c_uint64, c_i32, c_void_p, c_void_p, c_void_p]),
     "dips_mlp_eval": (c_i32, [P(ArchT), c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),

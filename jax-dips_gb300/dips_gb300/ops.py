@@ -107,6 +107,18 @@ def train_step(arch: Arch, params: torch.Tensor, opt: AdamState, level: FVLevel,
                "dips_train_step")
 
 
+def autotune(arch: Arch, params: torch.Tensor, level: FVLevel, batch_ids, ws: StepWorkspace) -> int:
+    """Pick the fastest launch configuration of the shape's point kernel on this batch (kept
+    process-wide for the current device); returns the warps per CTA chosen (0: nothing to tune).
+    Synchronises the stream: call it before capturing a CUDA graph."""
+    lib = _lib.load()
+    B = level.n if batch_ids is None else int(batch_ids.numel())
+    out = ctypes.c_int32(0)
+    _lib.check(lib.dips_autotune(arch.ctype(), _lib.ptr(params), level.desc, _ids_ptr(batch_ids), B, _lib.ptr(ws.buf),
+                                 ws.nbytes, ctypes.byref(out), _lib.stream_handle()), "dips_autotune")
+    return int(out.value)
+
+
 STEP_PHASES = ("expand", "forward_m", "forward_p", "residual", "fused_m", "fused_p", "loss", "adjoint_m",
                "adjoint_p", "reduce", "adam")
 

@@ -96,6 +96,9 @@ def adam_state_from_dict(n_params, optimizer_dict, device):
     raise ValueError(f"Unknown optimizer: {name}")
 
 
+_TUNED = set()
+
+
 def _levels(num_epochs):
     q = max(num_epochs // 4, 1)
     return (num_epochs - 1) // q + 1 if num_epochs > 0 else 1
@@ -210,6 +213,12 @@ class Trainer:
 
     def _make_runner(self, lvl):
         ws = ops.StepWorkspace(self.arch, self.batch, lvl.max_jobs(self.batch, distinct=True), self.device)
+        a = self.arch
+        key = (a.m_layers, a.m_width, a.p_layers, a.p_width, str(self.device))
+        if key not in _TUNED:  # launch-configuration autotuner, once per shape and device, before any capture
+            ids = ops.batch_ids(self.points.shape[0], self.batch, epoch=0, batch_index=0, seed=99, device=self.device)
+            ops.autotune(self.arch, self.params, lvl, ids, ws)
+            _TUNED.add(key)
         if not self.use_graph:
             return lambda: self._step(lvl, ws), ws
         # warm up outside the capture (sets kernel attributes), then undo its effect

@@ -168,3 +168,25 @@ def test_batch_ids_are_a_permutation():
     assert len(np.unique(seen)) == seen.size and seen.min() >= 0 and seen.max() < n
     other = ops.batch_ids(n, B, epoch=4, batch_index=0, seed=7).cpu().numpy()
     assert not np.array_equal(other, seen[:B])
+
+
+def test_autotune_choice_and_unchanged_results():
+    from dips_gb300 import ops
+
+    case = _parity.build_case("sphere", n=20, arch=(3, 32, 3, 32), level=0)
+    lg0, gg0 = case.gpu_loss_grad()
+    lvl = case.gpu_level()
+    a = case.gpu_arch()
+    params = torch.as_tensor(case.params, device="cuda")
+    ws = ops.StepWorkspace(a, lvl.n, lvl.max_jobs(lvl.n), "cuda")
+    nw = ops.autotune(a, params, lvl, None, ws)
+    assert nw in (4, 6, 12)
+    lg1, gg1 = case.gpu_loss_grad()
+    assert abs(lg1 - lg0) <= 1e-6 * abs(lg0)
+    np.testing.assert_allclose(gg1, gg0, rtol=1e-4, atol=1e-6 * np.max(np.abs(gg0)))
+    # shapes without a tunable kernel report 0
+    small = _parity.build_case("sphere", n=12, arch=(1, 1, 2, 10), level=0)
+    slvl = small.gpu_level()
+    sa = small.gpu_arch()
+    sws = ops.StepWorkspace(sa, slvl.n, slvl.max_jobs(slvl.n), "cuda")
+    assert ops.autotune(sa, torch.as_tensor(small.params, device="cuda"), slvl, None, sws) == 0
