@@ -62,10 +62,12 @@ def parse():
     ap.add_argument("--no-tta", action="store_true")
     ap.add_argument("--tta-lr", type=float, default=1e-2)
     ap.add_argument("--cpu-sample", type=int, default=16384)
-    ap.add_argument("--problem", default="sphere", choices=["sphere", "star", "blob"],
+    ap.add_argument("--problem", default="sphere", choices=["sphere", "star", "blob", "lpbe"],
                     help="sphere: phi=|x|-0.5, mu 1/10 (the 128^3 headline); star: the variable-coefficient "
                          "star interface (mu- = 1+0.5 sin xy, mu+ = 20+5 cos z, k+ = 1); blob: 0.3-isosurface of "
-                         "500 Gaussians, mu 1/100, k = 0.5")
+                         "500 Gaussians, mu 1/100, k = 0.5; lpbe: --instances linearised Poisson-Boltzmann problems "
+                         "of uneven size (sides 48..160), 2x16 networks, one graph launch per batched step")
+    ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--arch", default="3x32", choices=["3x32", "4x64", "2x16"],
                     help="hidden layers x width of both networks (4x64 runs on the TF32 tensor cores)")
     ap.add_argument("--n-ls", type=int, default=0, help="level-set grid side (default: the training grid's)")
@@ -416,6 +418,93 @@ def run_ours(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def run_instances(args, rank, world):
+    """Uneven LPBE instances trained together: one CUDA graph launch per batched step."""
+    import torch
+
+    from dips_gb300 import _lib, batch, nn, problems
+
+    dev = f"cuda:{int(os.environ.get('LOCAL_RANK', 0))}"
+    torch.cuda.set_device(dev)
+    _lib.load()
+    arch = nn.Arch(2, 16, 2, 16)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    insts = [(side, problems.lpbe_problem(c, r, q)) for side, c, r, q in problems.lpbe_instances(args.instances, seed=rank)]
+    ib = batch.InstanceBatch(insts, arch, batch=args.batch, lr=1e-3, seed=rank)
+    for _ in range(max(args.warmup, 3)):
+        ib.step()
+    ib.capture()
+    for _ in range(2):
+        ib.step()
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    for i in range(args.steps):
+        flush.zero_()
+        starts[i].record()
+        ib.step()
+        ends[i].record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    t_total = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / 1e3
+    if world > 1:
+        t = torch.tensor([t_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_total = float(t)
+    pts = ib.points_per_step
+    value = pts * world * args.steps / t_total
+    f = net_flops(2, 16)
+    jobs = 0
+    for it in ib.items:
+        ids = it.ids.long()
+        jobs += int(it.level.cnt[ids].sum())
+    step_tflops = 3 * f * jobs / (t_total / args.steps) / 1e12
+    # e2e: each instance's batch ids copied from pinned host memory, the losses read back
+    host = [torch.empty(it.batch, dtype=torch.int32).pin_memory() for it in ib.items]
+    for hbuf, it in zip(host, ib.items):
+        hbuf.numpy()[:] = np.random.default_rng(1).permutation(it.level.n)[: it.batch]
+    out = torch.empty(len(ib.items), dtype=torch.float64).pin_memory()
+    from dips_gb300 import ops as _ops
+
+    e2e_steps = max(args.steps // 2, 3)
+    torch.cuda.synchronize()
+    te0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for hbuf, it in zip(host, ib.items):
+            it.ids.copy_(hbuf, non_blocking=True)
+            _ops.train_step(arch, it.params, it.opt, it.level, it.ids, it.ws, it.loss)
+        out.copy_(torch.stack([it.loss for it in ib.items]), non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    te = time.perf_counter() - te0
+    if rank == 0:
+        sides = sorted(it.side for it in ib.items)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{len(ib.items)} linearised Poisson-Boltzmann instances, sides {sides[0]}..{sides[-1]} "
+                                   "(uniform in steps of 16), phi = min over 50-2000 spheres, DoubleMLP 2x16/2x16 tanh; "
+                                   "one CUDA graph launch per batched step (every instance's batch ids + training step)",
+                       "global_batch": pts * world, "points": int(sum(it.level.n for it in ib.items)),
+                       "batch_per_instance": args.batch, "jobs_per_step": jobs, "setup_s": setup_s,
+                       "l2": "flushed (256 MB write) between timed steps", "cuda_graph": True},
+            "roofline": {"bound": "fp32", "kernel": "whole batched step (14 launches per instance)",
+                         "achieved": step_tflops, "peak": 78.4, "unit": "TFLOP/s", "frac": step_tflops / 78.4,
+                         "traffic": None, "algorithmic": "3 x F(2x16) x jobs per step",
+                         "peak_source": "FFMA probe value measured in the headline runs"},
+            "cpu_baseline": None,
+            "e2e": {"value": pts * e2e_steps / te, "unit": UNIT, "h2d_bytes_per_step": 4 * pts,
+                    "d2h_bytes_per_step": 8 * len(ib.items)},
+            "gpu_launches": ib.kernels_per_step * args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def time_to_target(args, lvl, g, pr, arch, dev):
     import torch
 
@@ -530,6 +619,8 @@ def main():
         dist.init_process_group(backend)
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.problem == "lpbe":
+        run_instances(args, rank, world)
     else:
         run_ours(args, rank, world)
     if world > 1:

@@ -1,0 +1,103 @@
+"""Many independent interface problems of uneven size trained together.
+
+Each instance has its own level set, residual records, network parameters and Adam state (the
+reference trains one problem per ``Trainer``; examples/benchmark_LPBE runs its molecules one by
+one).  ``InstanceBatch`` captures the training steps of all instances in one CUDA graph, so
+that a batched step is one graph launch: the batch-id kernel and the fused training step of
+every instance, largest instance first, on one stream.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib, levelset, mesh, nn, ops
+from .records import FVLevel
+
+F32 = np.float32
+
+
+class Instance:
+    """One problem: its grid, level set, records at h = dx, parameters and optimizer."""
+
+    def __init__(self, side: int, problem: dict, arch: nn.Arch, batch: int, lr: float, seed: int, device="cuda"):
+        self.side = side
+        self.grid = mesh.uniform_grid(side)
+        g = self.grid
+        self.ls = levelset.LevelSetGrid.from_callable(g, lambda r: levelset.perturb(problem["phi"](r)), device)
+        pts = torch.as_tensor(g.R, device=device)
+        self.level = FVLevel(self.ls, problem, pts, np.array([g.dx, g.dy, g.dz], F32))
+        self.batch = min(int(batch), self.level.n)
+        self.n_batches = self.level.n // self.batch
+        self.params = torch.as_tensor(nn.init_params(arch, seed), device=device)
+        self.opt = ops.AdamState(nn.n_params(arch), lr=lr, decay_rate=0.9, device=device)
+        self.ws = ops.StepWorkspace(arch, self.batch, self.level.max_jobs(self.batch), device)
+        self.ids = torch.empty(self.batch, dtype=torch.int32, device=device)
+        self.loss = torch.zeros((), dtype=torch.float64, device=device)
+        self.seed = seed
+
+
+class InstanceBatch:
+    """Train ``len(instances)`` problems with one graph launch per batched step.
+
+    instances: list of (grid side, problem dict).  batch: points per instance and step (clamped
+    to the instance's size); minibatches are uniform permutations per epoch of each instance.
+    """
+
+    def __init__(self, instances, arch: nn.Arch, batch: int = 1 << 15, lr: float = 1e-3, seed: int = 0,
+                 device="cuda"):
+        if not torch.cuda.is_available():
+            raise RuntimeError("dips_gb300 runs on a CUDA GPU; none is available")
+        lib = _lib.load()
+        if not lib.dips_arch_supported(arch.ctype()):
+            raise NotImplementedError(lib.dips_last_error().decode())
+        self.arch = arch
+        self.device = device
+        self.items = [Instance(side, prob, arch, batch, lr, seed + i, device) for i, (side, prob) in enumerate(instances)]
+        self.order = sorted(range(len(self.items)), key=lambda i: -self.items[i].level.n)
+        self.losses = torch.zeros(len(self.items), dtype=torch.float64, device=device)
+        self.graph = None
+
+    def _step_all(self):
+        lib = _lib.load()
+        for i in self.order:
+            it = self.items[i]
+            _lib.check(lib.dips_batch_ids_device(it.level.n, it.batch, it.n_batches, it.seed, 1, _lib.ptr(it.opt.count),
+                                                 _lib.ptr(it.ids), _lib.stream_handle()), "dips_batch_ids_device")
+            ops.train_step(self.arch, it.params, it.opt, it.level, it.ids, it.ws, it.loss)
+            self.losses[i : i + 1].copy_(it.loss.reshape(1))
+
+    def capture(self):
+        """Warm up once (restoring the state), then capture every instance's step in one graph."""
+        saved = [(it.params.clone(), it.opt.mu.clone(), it.opt.nu.clone(), it.opt.count.clone()) for it in self.items]
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self._step_all()
+        torch.cuda.current_stream().wait_stream(s)
+        for it, (p, m, v, c) in zip(self.items, saved):
+            it.params.copy_(p)
+            it.opt.mu.copy_(m)
+            it.opt.nu.copy_(v)
+            it.opt.count.copy_(c)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self._step_all()
+        return self
+
+    def step(self):
+        """One training step of every instance (one graph launch once captured)."""
+        if self.graph is None:
+            self._step_all()
+        else:
+            self.graph.replay()
+        return self.losses
+
+    @property
+    def points_per_step(self) -> int:
+        return sum(it.batch for it in self.items)
+
+    @property
+    def kernels_per_step(self) -> int:
+        return 14 * len(self.items)
