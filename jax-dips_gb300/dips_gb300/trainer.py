@@ -278,6 +278,19 @@ class Trainer:
         return u, gu, gn
 
     # ------------------------------------------------------------------ checkpoints
+    def write_solution_vtk(self, filename="results/solution", gstate: GridState = None):
+        """u, grad u, d_n u and phi on a grid as a VTK structured grid (the reference's
+        write_vtk_manual, utils/io.py:80-88)."""
+        from . import io
+
+        gstate = gstate or self.eval_gstate
+        u, gu, gn = self.evaluate_solution_and_gradients(gstate)
+        R = torch.as_tensor(gstate.R, device=self.device)
+        shape = (gstate.x.shape[0], gstate.y.shape[0], gstate.z.shape[0])
+        fields = {"solution": u.reshape(shape), "grad_solution": gu.reshape(shape + (3,)),
+                  "grad_normal_solution": gn.reshape(shape), "phi": self.ls(R).reshape(shape)}
+        return io.write_vtk_manual(gstate, fields, filename)
+
     def save_checkpoint(self, checkpoint_dir, epoch):
         """pickle of {opt_state, params, epoch, batch_size, resolution} (trainer.py:340-351)."""
         os.makedirs(checkpoint_dir, exist_ok=True)

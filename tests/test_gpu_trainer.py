@@ -57,7 +57,7 @@ def _oracle_losses(g, pr, epochs, lr, arch):
     return np.array(losses), params
 
 
-def test_setup_init_solve_tracks_oracle():
+def test_setup_init_solve_tracks_oracle(tmp_path):
     n, epochs, lr = 14, 8, 1e-2
     g, pr, state, epoch_store, losses, tr = _run_api(n, epochs, lr)
     assert list(epoch_store) == list(range(epochs))
@@ -70,6 +70,12 @@ def test_setup_init_solve_tracks_oracle():
     assert tuple(state.solution.shape) in ((ne,), (ne, 1))
     assert tuple(state.grad_solution.shape) == (ne, 3)
     assert torch.isfinite(torch.as_tensor(state.solution)).all()
+    # the VTK dump of the evaluation grid holds the same solution (x fastest in the file)
+    from dips_gb300 import io
+
+    back = io.read_vts(tr.write_solution_vtk(str(tmp_path / "sol")))
+    sol = torch.as_tensor(state.solution).reshape(n, n, n).cpu().numpy()
+    np.testing.assert_allclose(back["solution"], sol.transpose(2, 1, 0).reshape(-1), rtol=1e-6, atol=1e-7)
 
 
 def test_training_reduces_the_solution_error():
