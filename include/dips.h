@@ -14,7 +14,8 @@
  *   params      float32 flat vector: net u- then net u+; per net and hidden layer
  *               W[in][out] row-major then b[out]; output layer W[width] then b[1].
  *               This is the haiku tree order of double_mlp/~mlp_{m,p}_fn/linear{,_1,..}
- *               (nn/mlp/MLP.py:101-139) with w before b.
+ *               (nn/mlp/MLP.py:101-139) with w before b.  With the learned preconditioner
+ *               its parameters follow, in the same per-layer order (first layer 26 x width).
  *   job code    uint16: stencil point j (0..6: ijk, i-1, i+1, j-1, j+1, k-1, k+1) times 27
  *               plus regression-cube vertex k (0..26, x fastest), bit 15 set when the
  *               u+ network evaluates the point (phi >= 0, nn/mlp/MLP.py:98).
@@ -85,10 +86,19 @@ typedef struct {
                                its cnt_m u- jobs at the start, its cnt - cnt_m u+ jobs at the end */
   const uint16_t* job_code; /* [jobs] */
   const float* job_A;       /* [jobs] lhs coefficient of the network value at the job point */
+  const float* coeff26;     /* [n][26] cell coefficients (geom_pp.py:873-901); read only by the
+                               learned preconditioner, may be NULL without it */
 } dips_records_t;
 
 typedef struct {
   int32_t m_layers, m_width, p_layers, p_width; /* DoubleMLP hidden layers and widths, tanh */
+  /* learned preconditioner (nn/preconditioner.py:10-35, trainer.py:229-243): pre_layers tanh
+     layers of width pre_width over the 26 cell coefficients, then one output y, and
+     P = 0.5 + pre_scaling * sigmoid(y) multiplies the point's residual
+     (discretization.py:339, :419-420).  pre_layers = 0 disables it; widths 8, 16 or 32,
+     1 to 3 layers. */
+  int32_t pre_layers, pre_width;
+  float pre_scaling;
 } dips_arch_t;
 
 /* optax chain: clip_by_global_norm -> scale_by_adam -> scale_by_schedule(exponential_decay)

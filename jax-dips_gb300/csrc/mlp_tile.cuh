@@ -502,8 +502,11 @@ __global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile_net(PtsH ph,
 #pragma unroll
             for (int q = 0; q < kStencil; ++q) lhs += U[kStencil * lane + q];
             const float qv = lhs / r_diag;
-            const float r = nan_to_num(qv) - r_rod;
-            gc = isfinite(qv) ? (r / Bf) / r_diag : 0.0f;
+            const float r0 = nan_to_num(qv) - r_rod;
+            const float Pv = w.pre_P ? w.pre_P[rslot] : 1.0f;  // learned preconditioner
+            const float r = Pv * r0;
+            if (w.pre_P) w.pre_r0[rslot] = r0;
+            gc = isfinite(qv) ? (r / Bf) * Pv / r_diag : 0.0f;
             lsum += 0.5 * (double)r * (double)r;
             if (residual_out) residual_out[rslot] = r;
           }

@@ -21,7 +21,7 @@ namespace dips {
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-static size_t carve(Workspace* w, char* base, int64_t B, int64_t max_jobs, int P) {
+static size_t carve(Workspace* w, char* base, int64_t B, int64_t max_jobs, int P, int pre_n) {
   size_t off = 0;
   auto take = [&](size_t bytes) {
     char* p = base ? base + off : nullptr;
@@ -55,6 +55,10 @@ static size_t carve(Workspace* w, char* base, int64_t B, int64_t max_jobs, int P
   W.jx = (float4*)take(sizeof(float4) * W.jcap);
   W.jg = (float*)take(sizeof(float) * W.jcap);
   W.brec = (float*)take(sizeof(float) * kRecFloats * 2 * B);
+  W.pre_n = pre_n;
+  W.pre_P = pre_n ? (float*)take(sizeof(float) * B) : nullptr;
+  W.pre_r0 = pre_n ? (float*)take(sizeof(float) * B) : nullptr;
+  W.pre_partials = pre_n ? (float*)take(sizeof(float) * (size_t)kPreGrid * pre_n) : nullptr;
   W.partials = (float*)take(sizeof(float) * (size_t)(W.grid + W.fgrid) * P);
   W.grad = (float*)take(sizeof(float) * P);
   if (w) *w = W;
@@ -273,9 +277,13 @@ __global__ void k_residual(const int32_t* __restrict__ ids, int64_t B, dips_reco
       for (int q = 0; q < cp; ++q) lhs = fmaf(w.jA[op + q], w.ju[op + q], lhs);
       const float diag = rec.diag[pid];
       const float qv = lhs / diag;
-      const float r = nan_to_num(qv) - rec.rod[pid];
+      const float r0 = nan_to_num(qv) - rec.rod[pid];
+      // the learned preconditioner scales both lhs/diag and rhs/diag (discretization.py:419-420)
+      const float Pv = w.pre_P ? w.pre_P[b] : 1.0f;
+      const float r = Pv * r0;
+      if (w.pre_P) w.pre_r0[b] = r0;
       // d(mean 0.5 r^2)/d lhs; nan_to_num has zero derivative where lhs/diag is not finite
-      const float gs = isfinite(qv) ? (r / (float)B) / diag : 0.0f;
+      const float gs = isfinite(qv) ? (r / (float)B) * Pv / diag : 0.0f;
       w.gs[b] = gs;
       for (int q = 0; q < cm; ++q) w.jg[om + q] = gs * w.jA[om + q];
       for (int q = 0; q < cp; ++q) w.jg[op + q] = gs * w.jA[op + q];
@@ -296,10 +304,17 @@ __global__ void k_loss_final(Workspace w, int64_t B, double* __restrict__ loss_o
   if (threadIdx.x == 0) *loss_out = w.ctl->engine_error ? nan("") : t / (double)B;
 }
 
-// columns [0, Pm) belong to the u- network; Ctl::grad_rows gives each network's partial rows
-__global__ void k_grad_reduce(Workspace w, int P, int Pm, float* __restrict__ grad_out) {
+// columns [0, Pm) belong to the u- network and [Pm, Psol) to the u+ network, with
+// Ctl::grad_rows partial rows each; columns [Psol, P) to the preconditioner (kPreGrid rows)
+__global__ void k_grad_reduce(Workspace w, int P, int Pm, int Psol, float* __restrict__ grad_out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P) return;
+  if (i >= Psol) {
+    float v = 0.0f;
+    for (int c = 0; c < kPreGrid; ++c) v += w.pre_partials[(size_t)c * w.pre_n + (i - Psol)];
+    grad_out[i] = w.ctl->engine_error ? nanf("") : v;
+    return;
+  }
   const int64_t rows = w.ctl->grad_rows[i < Pm ? 0 : 1];
   float v = 0.0f;
   for (int64_t c = 0; c < rows; ++c) v += w.partials[(size_t)c * P + i];
@@ -434,9 +449,17 @@ static const ArchOps* find_arch(const dips_arch_t* a) {
 
 static int net_params(int L, int W) { return 3 * W + W + (L - 1) * (W * W + W) + W + 1; }
 
+// parameters of the learned preconditioner (0 when it is off, -1 for an unsupported shape)
+static int arch_pre_params(const dips_arch_t* a) {
+  if (!a || a->pre_layers <= 0) return 0;
+  return pre_supported(a->pre_layers, a->pre_width) ? pre_num_params(a->pre_layers, a->pre_width) : -1;
+}
+
 static int arch_params(const dips_arch_t* a) {
   if (!a || a->m_layers < 1 || a->p_layers < 1 || a->m_width < 1 || a->p_width < 1) return -1;
-  return net_params(a->m_layers, a->m_width) + net_params(a->p_layers, a->p_width);
+  const int pre = arch_pre_params(a);
+  if (pre < 0) return -1;
+  return net_params(a->m_layers, a->m_width) + net_params(a->p_layers, a->p_width) + pre;
 }
 
 static int check_rec(const dips_records_t* rec, int64_t B) {
@@ -460,7 +483,8 @@ static int prep_ws(const dips_arch_t* arch, int64_t B, void* ws, size_t ws_bytes
   const int P = arch_params(arch);
   DIPS_REQUIRE(P > 0, DIPS_E_ARG, "invalid arch");
   DIPS_REQUIRE(ws != nullptr, DIPS_E_ARG, "null workspace");
-  const size_t fixed = carve(nullptr, nullptr, B, 0, P);
+  const int pre_n = arch_pre_params(arch);
+  const size_t fixed = carve(nullptr, nullptr, B, 0, P, pre_n);
   DIPS_REQUIRE(ws_bytes >= fixed + 256, DIPS_E_WORKSPACE, "workspace too small: %zu < %zu", ws_bytes, fixed + 256);
   char* base = (char*)(((uintptr_t)ws + 255) & ~(uintptr_t)255);
   const size_t avail = ws_bytes - (size_t)(base - (char*)ws);
@@ -468,12 +492,12 @@ static int prep_ws(const dips_arch_t* arch, int64_t B, void* ws, size_t ws_bytes
   int64_t lo = 0, hi = (int64_t)(avail / 14) + 1;
   while (lo + 1 < hi) {
     const int64_t mid = (lo + hi) / 2;
-    if (carve(nullptr, nullptr, B, mid, P) <= avail)
+    if (carve(nullptr, nullptr, B, mid, P, pre_n) <= avail)
       lo = mid;
     else
       hi = mid;
   }
-  carve(W, base, B, lo, P);
+  carve(W, base, B, lo, P, pre_n);
   return DIPS_OK;
 }
 
@@ -490,10 +514,15 @@ static int expand(const dips_records_t* rec, const int32_t* ids, int64_t B, Work
 }
 
 // expansion, general forward + residual, fused bulk kernel (with or without its gradient)
-static int run_forward(const ArchOps* ops, const dips_records_t* rec, const int32_t* ids, int64_t B, Workspace& W,
-                       double* loss_out, float* residual_out, bool fused_bwd, const Marks* mk, cudaStream_t s) {
+static int run_forward(const ArchOps* ops, const dips_arch_t* arch, const float* params, const dips_records_t* rec,
+                       const int32_t* ids, int64_t B, Workspace& W, double* loss_out, float* residual_out,
+                       bool fused_bwd, const Marks* mk, cudaStream_t s) {
   int st = expand(rec, ids, B, W, ops->bulk_ok, mk, s);
   if (st) return st;
+  if (W.pre_n) {  // the preconditioner's value per slot, read by every residual kernel
+    st = precond_forward(*arch, params + ops->n_params, *rec, ids, B, W, s);
+    if (st) return st;
+  }
   st = ops->job_forward(make_ph(rec), ids, W, mk, s);
   if (st) return st;
   k_residual<<<(int)W.nres, 256, 0, s>>>(ids, B, *rec, W, residual_out);
@@ -508,12 +537,18 @@ static int run_forward(const ArchOps* ops, const dips_records_t* rec, const int3
 }
 
 // general adjoint and the reduction of all partial gradient rows
-static int run_backward(const ArchOps* ops, const dips_records_t* rec, const int32_t* ids, Workspace& W,
-                        float* grad_out, const Marks* mk, cudaStream_t s) {
+static int run_backward(const ArchOps* ops, const dips_arch_t* arch, const float* params, const dips_records_t* rec,
+                        const int32_t* ids, int64_t B, Workspace& W, float* grad_out, const Marks* mk,
+                        cudaStream_t s) {
   int st = ops->job_adjoint(make_ph(rec), ids, W, mk, s);
   if (st) return st;
+  if (W.pre_n) {
+    st = precond_backward(*arch, params + ops->n_params, *rec, ids, B, W, s);
+    if (st) return st;
+  }
   const int Pm = ops->n_params - net_params(ops->p_layers, ops->p_width);
-  k_grad_reduce<<<div_up(ops->n_params, 256), 256, 0, s>>>(W, ops->n_params, Pm, grad_out);
+  const int P = ops->n_params + W.pre_n;
+  k_grad_reduce<<<div_up(P, 256), 256, 0, s>>>(W, P, Pm, ops->n_params, grad_out);
   DIPS_CHECK_LAUNCH("gradient reduction");
   mark(mk, kMarkReduce, s);
   return DIPS_OK;
@@ -530,7 +565,7 @@ extern "C" int32_t dips_arch_supported(const dips_arch_t* arch) { return find_ar
 extern "C" size_t dips_step_workspace_bytes(const dips_arch_t* arch, int64_t batch, int64_t max_jobs) {
   const int P = arch_params(arch);
   if (P <= 0 || batch <= 0 || max_jobs < 0) return 0;
-  return carve(nullptr, nullptr, batch, max_jobs, P) + 256;
+  return carve(nullptr, nullptr, batch, max_jobs, P, arch_pre_params(arch)) + 256;
 }
 
 extern "C" int dips_residual_fwd(const dips_arch_t* arch, const float* params, const dips_records_t* rec,
@@ -546,7 +581,7 @@ extern "C" int dips_residual_fwd(const dips_arch_t* arch, const float* params, c
   if (st) return st;
   st = ops->load_params(params, stream);
   if (st) return st;
-  return run_forward(ops, rec, batch_ids, batch, W, loss_out, residual_out, false, nullptr, stream);
+  return run_forward(ops, arch, params, rec, batch_ids, batch, W, loss_out, residual_out, false, nullptr, stream);
 }
 
 extern "C" int dips_residual_bwd(const dips_arch_t* arch, const float* params, const dips_records_t* rec,
@@ -565,7 +600,7 @@ extern "C" int dips_residual_bwd(const dips_arch_t* arch, const float* params, c
   // the bulk points' gradient comes from the fused kernel, run again with its backward half
   st = ops->bulk_fused(make_ph(rec), batch_ids, W, *rec, nullptr, true, nullptr, stream);
   if (st) return st;
-  return run_backward(ops, rec, batch_ids, W, grad_out, nullptr, stream);
+  return run_backward(ops, arch, params, rec, batch_ids, batch, W, grad_out, nullptr, stream);
 }
 
 extern "C" int dips_adam_step(const dips_arch_t* arch, const dips_adam_t* hp, float* params, const float* grad,
@@ -591,12 +626,12 @@ static int train_step(const dips_arch_t* arch, const dips_adam_t* hp, float* par
   if (st) return st;
   st = ops->load_params(params, stream);
   if (st) return st;
-  st = run_forward(ops, rec, batch_ids, batch, W, loss_out, nullptr, true, mk, stream);
+  st = run_forward(ops, arch, params, rec, batch_ids, batch, W, loss_out, nullptr, true, mk, stream);
   if (st) return st;
   float* g = grad_out ? grad_out : W.grad;
-  st = run_backward(ops, rec, batch_ids, W, g, mk, stream);
+  st = run_backward(ops, arch, params, rec, batch_ids, batch, W, g, mk, stream);
   if (st) return st;
-  k_adam<<<1, 1024, 0, stream>>>(*hp, ops->n_params, params, g, mu, nu, count);
+  k_adam<<<1, 1024, 0, stream>>>(*hp, ops->n_params + W.pre_n, params, g, mu, nu, count);
   DIPS_CHECK_LAUNCH("dips_train_step adam");
   mark(mk, kMarkAdam, stream);
   return DIPS_OK;
@@ -637,7 +672,7 @@ extern "C" int dips_autotune(const dips_arch_t* arch, const float* params, const
   int chosen = 0;
   if (ops->autotune) {
     // the forward prepares what the timed launches read (job lists, records, dL/du)
-    st = run_forward(ops, rec, batch_ids, batch, W, nullptr, nullptr, false, nullptr, stream);
+    st = run_forward(ops, arch, params, rec, batch_ids, batch, W, nullptr, nullptr, false, nullptr, stream);
     if (st) return st;
     st = ops->autotune(make_ph(rec), batch_ids, W, *rec, stream, &chosen);
     if (st) return st;

@@ -389,11 +389,14 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_bulk_fused(PtsH ph, const 
       for (int j = 0; j < kStencil; ++j) lhs += sU[j * 32 + lane];
       const float diag = rec.diag[pid];
       const float qv = lhs / diag;
-      const float r = nan_to_num(qv) - rec.rod[pid];
-      gc = isfinite(qv) ? (r / Bf) / diag : 0.0f;
+      const float r0 = nan_to_num(qv) - rec.rod[pid];
+      const float Pv = w.pre_P ? w.pre_P[slot] : 1.0f;  // learned preconditioner
+      const float r = Pv * r0;
+      gc = isfinite(qv) ? (r / Bf) * Pv / diag : 0.0f;
       if (warp == 0) {
         lsum += 0.5 * (double)r * (double)r;
         if (residual_out) residual_out[slot] = r;
+        if (w.pre_P) w.pre_r0[slot] = r0;
       }
     }
     __syncthreads();  // sU is rewritten by the next group

@@ -13,6 +13,9 @@ constexpr int kFusedThreads = 224;   // fused bulk CTA: one warp per stencil poi
 constexpr int kFusedGrid = 152 * 2;
 constexpr int kTileGrid = 152;  // register-blocked engine: 12 warps per SM (one CTA of 12 by default)
 constexpr int kLossSlots = 512;  // per-network capacity of the per-CTA loss partials
+constexpr int kPreGrid = 304;    // CTAs of the preconditioner's backward (partial rows)
+constexpr int kPreIn = 26;       // preconditioner input: the cell coefficients
+
 // bulk point record (16 floats): point, lhs0, A of stencil points 0..6, diag, rod, batch slot
 constexpr int kRecP = 0, kRecLhs0 = 3, kRecA = 4, kRecDiag = 11, kRecRod = 12, kRecSlot = 13, kRecFloats = 16;
 
@@ -50,11 +53,15 @@ struct Workspace {
   float4* jx;        // [jcap] job coordinates (w unused)
   float* jg;         // [jcap] d loss / d u of the job
   float* brec;       // [2][B][16] bulk point records, in bulk-list order (layout: kRec* below)
+  float* pre_P;      // [B] learned preconditioner value per slot; NULL when it is off
+  float* pre_r0;     // [B] residual before preconditioning (its backward reads it)
+  float* pre_partials;  // [kPreGrid][pre_n] partial gradient rows of the preconditioner
   float* partials;   // [grid + fgrid][P] partial gradient rows (count per network in Ctl::grad_rows)
   float* grad;       // [P]
   int64_t nblk, nres, jcap, B;
   int grid, fgrid;
   int n_params;      // row stride of partials
+  int pre_n;         // preconditioner parameters (0 when it is off); they follow the networks'
 };
 
 struct PtsH {
@@ -114,5 +121,13 @@ struct ArchOps {
   int (*autotune)(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec, cudaStream_t s,
                   int* chosen);
 };
+
+// learned preconditioner (implemented in precond.cu)
+int pre_num_params(int layers, int width);
+bool pre_supported(int layers, int width);
+int precond_forward(const dips_arch_t& a, const float* pre_params, const dips_records_t& rec, const int32_t* ids,
+                    int64_t B, const Workspace& w, cudaStream_t s);
+int precond_backward(const dips_arch_t& a, const float* pre_params, const dips_records_t& rec, const int32_t* ids,
+                     int64_t B, const Workspace& w, cudaStream_t s);
 
 }  // namespace dips

@@ -36,6 +36,7 @@ UNITS = {
     "krylov.cu": [],
     "residual_static.cu": [],
     "residual_tc.cu": [],
+    "precond.cu": [],
 }
 
 _lock = threading.Lock()
@@ -165,11 +166,13 @@ class RecordsT(ctypes.Structure):
         ("job_off", c_void_p),
         ("job_code", c_void_p),
         ("job_A", c_void_p),
+        ("coeff26", c_void_p),
     ]
 
 
 class ArchT(ctypes.Structure):
-    _fields_ = [("m_layers", c_i32), ("m_width", c_i32), ("p_layers", c_i32), ("p_width", c_i32)]
+    _fields_ = [("m_layers", c_i32), ("m_width", c_i32), ("p_layers", c_i32), ("p_width", c_i32),
+                ("pre_layers", c_i32), ("pre_width", c_i32), ("pre_scaling", c_f32)]
 
 
 class AdamT(ctypes.Structure):

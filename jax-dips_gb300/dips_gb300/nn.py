@@ -28,9 +28,15 @@ class Arch:
     m_width: int = 1
     p_layers: int = 2
     p_width: int = 10
+    # learned preconditioner (nn/preconditioner.py:10-35): tanh layers over the 26 cell
+    # coefficients, P = 0.5 + pre_scaling * sigmoid(out); 0 layers = off
+    pre_layers: int = 0
+    pre_width: int = 0
+    pre_scaling: float = 1.0
 
     def ctype(self):
-        return _lib.ArchT(self.m_layers, self.m_width, self.p_layers, self.p_width)
+        return _lib.ArchT(self.m_layers, self.m_width, self.p_layers, self.p_width, self.pre_layers, self.pre_width,
+                          self.pre_scaling)
 
     def net(self, which):
         return (self.m_layers, self.m_width) if which == "m" else (self.p_layers, self.p_width)
@@ -45,8 +51,16 @@ def layer_shapes(layers, width, d_in=3):
     return shapes
 
 
+PRE_IN = 26  # the preconditioner's input: the cell coefficients (geom_pp.py:873-901)
+
+
+def pre_shapes(arch: Arch):
+    return layer_shapes(arch.pre_layers, arch.pre_width, PRE_IN) if arch.pre_layers > 0 else []
+
+
 def n_params(arch: Arch) -> int:
-    return sum(a * b + b for w in ("m", "p") for a, b in layer_shapes(*arch.net(w)))
+    nets = sum(a * b + b for w in ("m", "p") for a, b in layer_shapes(*arch.net(w)))
+    return nets + sum(a * b + b for a, b in pre_shapes(arch))
 
 
 def arch_from_model_dict(model_dict: dict) -> Arch:
@@ -58,8 +72,15 @@ def arch_from_model_dict(model_dict: dict) -> Arch:
         act = mlp.get(key, "jnp.tanh")
         if act not in _TANH_NAMES:
             raise NotImplementedError(f"{key}={act!r}: only tanh activations have a CUDA kernel")
+    pre = model_dict.get("preconditioner") or {}
+    pl, pw, ps = 0, 0, 1.0
+    if pre.get("enable", False):
+        widths = [int(v) for v in pre.get("layer_widths", [])]
+        if not widths or len(set(widths)) != 1:
+            raise NotImplementedError(f"preconditioner layer_widths {widths}: one width for every layer is supported")
+        pl, pw, ps = len(widths), widths[0], float(pre.get("scaling_coeff", 1.0))
     return Arch(int(mlp.get("hidden_layers_m", 1)), int(mlp.get("hidden_dim_m", 1)),
-                int(mlp.get("hidden_layers_p", 2)), int(mlp.get("hidden_dim_p", 10)))
+                int(mlp.get("hidden_layers_p", 2)), int(mlp.get("hidden_dim_p", 10)), pl, pw, ps)
 
 
 def init_params(arch: Arch, seed: int = 0) -> np.ndarray:
@@ -79,6 +100,11 @@ def init_params(arch: Arch, seed: int = 0) -> np.ndarray:
             # truncated standard normal on [-2, 2] has std 0.87962566...
             parts.append((w * std / 0.87962566103423978).astype(np.float32).ravel())
             parts.append(np.zeros(b, np.float32))
+    # preconditioner: flax Dense with glorot_uniform kernels and zero biases (preconditioner.py:18-35)
+    for a, b in pre_shapes(arch):
+        lim = np.sqrt(6.0 / (a + b))
+        parts.append(rng.uniform(-lim, lim, (a, b)).astype(np.float32).ravel())
+        parts.append(np.zeros(b, np.float32))
     return np.concatenate(parts).astype(np.float32)
 
 
@@ -103,7 +129,14 @@ def params_to_tree(flat, arch: Arch) -> dict:
             bb = flat[off:off + b]
             off += b
             tree[next(names)] = {"w": w, "b": bb}
-    tree["preconditioner"] = {}
+    pre = {}
+    for li, (a, b) in enumerate(pre_shapes(arch)):
+        k = flat[off:off + a * b].reshape(a, b)
+        off += a * b
+        bb = flat[off:off + b]
+        off += b
+        pre[f"Dense_{li}"] = {"kernel": k, "bias": bb}
+    tree["preconditioner"] = {"params": pre} if pre else {}
     return tree
 
 
@@ -114,6 +147,11 @@ def tree_to_params(tree: dict, arch: Arch, device=None) -> torch.Tensor:
                                      else tree[name]["w"]).reshape(-1))
         parts.append(torch.as_tensor(np.asarray(tree[name]["b"]) if not torch.is_tensor(tree[name]["b"])
                                      else tree[name]["b"]).reshape(-1))
+    pre = (tree.get("preconditioner") or {}).get("params", {})
+    for li in range(len(pre_shapes(arch))):
+        for key in ("kernel", "bias"):
+            v = pre[f"Dense_{li}"][key]
+            parts.append(torch.as_tensor(np.asarray(v) if not torch.is_tensor(v) else v).reshape(-1))
     out = torch.cat([p.to(torch.float32).cpu() for p in parts])
     return out.to(device) if device is not None else out
 

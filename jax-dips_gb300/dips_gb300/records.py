@@ -134,7 +134,7 @@ class FVLevel:
         self.max_cnt = int(self.cnt.max()) if n else 0
         self.desc = _lib.RecordsT(
             P(self.pts), n, (_lib.c_f32 * 3)(*[float(v) for v in self.h]), P(self.lhs0), P(self.diag), P(self.rod),
-            P(self.cnt), P(self.cnt_m), P(self.job_off), P(self.job_code), P(self.job_A),
+            P(self.cnt), P(self.cnt_m), P(self.job_off), P(self.job_code), P(self.job_A), P(self.coeff26),
         )
 
     def max_jobs(self, batch: int, distinct: bool = True) -> int:

@@ -118,10 +118,7 @@ class Trainer:
         self.fn = sim_state_fn
         self.lvl_gstate, self.tr_gstate, self.eval_gstate = lvl_gstate, tr_gstate, eval_gstate
         model_dict = dict(model_dict or DEFAULT_MODEL)
-        pre = model_dict.get("preconditioner", {"enable": False}) or {"enable": False}
-        if pre.get("enable", False):
-            raise NotImplementedError("the learned preconditioner is not on the GB300 path yet")
-        self.arch = nn.arch_from_model_dict(model_dict)
+        self.arch = nn.arch_from_model_dict(model_dict)  # includes the learned preconditioner if enabled
         if not _lib.load().dips_arch_supported(self.arch.ctype()):
             raise NotImplementedError(_lib.load().dips_last_error().decode())
         self.num_epochs = int(num_epochs)
@@ -190,7 +187,8 @@ class Trainer:
             fns = {"mu_m": self.fn.mu_m_fn, "mu_p": self.fn.mu_p_fn, "k_m": self.fn.k_m_fn, "k_p": self.fn.k_p_fn,
                    "f_m": self.fn.f_m_fn, "f_p": self.fn.f_p_fn, "alpha": self.fn.alpha_fn, "beta": self.fn.beta_fn,
                    "g": self.fn.dir_bc_fn}
-            self._level_cache[k] = FVLevel(self.ls, fns, self.points, h)
+            # the learned preconditioner reads the 26 cell coefficients of each point
+            self._level_cache[k] = FVLevel(self.ls, fns, self.points, h, keep_geometry=self.arch.pre_layers > 0)
         return self._level_cache[k]
 
     # ------------------------------------------------------------------ step

@@ -41,6 +41,10 @@ class Arch:
     m_width: int = 1
     p_layers: int = 2
     p_width: int = 10
+    # learned preconditioner (nn/preconditioner.py:10-35); 0 layers = off
+    pre_layers: int = 0
+    pre_width: int = 0
+    pre_scaling: float = 1.0
 
     def net(self, which):
         return (self.m_layers, self.m_width) if which == "m" else (self.p_layers, self.p_width)
@@ -56,12 +60,16 @@ def net_sizes(layers, width, d_in=3):
     return shapes
 
 
+def pre_sizes(arch: Arch):
+    return net_sizes(arch.pre_layers, arch.pre_width, 26) if arch.pre_layers > 0 else []
+
+
 def n_params(arch: Arch):
     tot = 0
     for which in ("m", "p"):
         for a, b in net_sizes(*arch.net(which)):
             tot += a * b + b
-    return tot
+    return tot + sum(a * b + b for a, b in pre_sizes(arch))
 
 
 def unflatten(flat, arch: Arch):
@@ -76,6 +84,14 @@ def unflatten(flat, arch: Arch):
             off += b
             layers.append((W, bb))
         out[which] = layers
+    pre = []
+    for a, b in pre_sizes(arch):
+        W = flat[off:off + a * b].reshape(a, b)
+        off += a * b
+        bb = flat[off:off + b]
+        off += b
+        pre.append((W, bb))
+    out["pre"] = pre
     assert off == flat.shape[0]
     return out
 
@@ -229,7 +245,13 @@ def residual(flat_params, arch: Arch, rg: ResidualGeometry, dtype=torch.float32)
     lhs = torch.where(bnd, u_s[:, 0] * V, lhs)
     diag = torch.where(bnd, V.expand(N), diag)
     rhs = torch.where(bnd, T(rg.g) * V, rhs)
-    return torch.nan_to_num(lhs / diag) - torch.nan_to_num(rhs / diag)
+    r = torch.nan_to_num(lhs / diag) - torch.nan_to_num(rhs / diag)
+    if arch.pre_layers > 0:
+        # precond = 0.5 + s * sigmoid(Dense(tanh(...)(coeffs_))) multiplies lhs/diag and rhs/diag
+        # (discretization.py:339, :419-420; nn/preconditioner.py:21-35)
+        P = 0.5 + arch.pre_scaling * torch.sigmoid(mlp(net["pre"], T(rg.coeffs)))
+        r = P * r
+    return r
 
 
 def loss(flat_params, arch: Arch, rg: ResidualGeometry, dtype=torch.float32):
@@ -263,6 +285,10 @@ def init_params(arch: Arch, seed=0):
                 w[bad] = rng.standard_normal(int(bad.sum()))
             parts.append((w * std / 0.87962566103423978).astype(F32).ravel())
             parts.append(np.zeros(b, F32))
+    for a, b in pre_sizes(arch):  # flax Dense: glorot_uniform kernels, zero biases (preconditioner.py:18-35)
+        lim = np.sqrt(6.0 / (a + b))
+        parts.append(rng.uniform(-lim, lim, (a, b)).astype(F32).ravel())
+        parts.append(np.zeros(b, F32))
     return np.concatenate(parts).astype(F32)
 
 

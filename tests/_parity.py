@@ -90,7 +90,7 @@ class Case:
         from dips_gb300.nn import Arch
 
         a = self.arch
-        return Arch(a.m_layers, a.m_width, a.p_layers, a.p_width)
+        return Arch(a.m_layers, a.m_width, a.p_layers, a.p_width, a.pre_layers, a.pre_width, a.pre_scaling)
 
     def gpu_batch_ids(self):
         import torch

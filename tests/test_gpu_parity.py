@@ -190,3 +190,28 @@ def test_autotune_choice_and_unchanged_results():
     sa = small.gpu_arch()
     sws = ops.StepWorkspace(sa, slvl.n, slvl.max_jobs(slvl.n), "cuda")
     assert ops.autotune(sa, torch.as_tensor(small.params, device="cuda"), slvl, None, sws) == 0
+
+
+@pytest.mark.parametrize(
+    "name,n,arch,level,batch",
+    [
+        ("sphere", 16, (1, 1, 2, 10, 2, 16, 1.0), 0, None),
+        ("star", 16, (3, 32, 3, 32, 1, 32, 1.0), 1, None),
+        ("star", 20, (2, 16, 2, 16, 3, 8, 2.0), 0, 2000),
+    ],
+)
+def test_learned_preconditioner_loss_and_gradient(name, n, arch, level, batch):
+    """P(coeffs) = 0.5 + s sigmoid(MLP(coeffs)) multiplies each residual (discretization.py:339,
+    :419-420); its parameters follow the networks' in the flat vector and get their gradient too."""
+    case = _parity.build_case(name, n=n, arch=arch, level=level, batch=batch, batch_seed=3)
+    lg, gg = case.gpu_loss_grad()
+    lr, gr = case.oracle_loss_grad()
+    assert abs(lg - lr) <= LOSS_RTOL * abs(lr), (lg, lr)
+    _grad_close(gg, gr)
+    from dips_gb300 import nn
+
+    a = case.gpu_arch()
+    npre = nn.n_params(a) - nn.n_params(nn.Arch(a.m_layers, a.m_width, a.p_layers, a.p_width))
+    assert npre > 0
+    gp, rp = np.asarray(gg)[-npre:], np.asarray(gr)[-npre:]
+    assert np.linalg.norm(gp - rp) <= GRAD_RTOL * np.linalg.norm(rp)

@@ -23,7 +23,7 @@ def _problem():
     return _parity.make_problem("sphere")
 
 
-def _run_api(n, epochs, lr):
+def _run_api(n, epochs, lr, pre=None):
     pr = _problem()
     g = mesh.uniform_grid(n)
     phi = lambda r: levelset.perturb(pr["phi"](r))  # noqa: E731  (the caller perturbs, as the examples do)
@@ -31,14 +31,15 @@ def _run_api(n, epochs, lr):
                             pr["f_p"], pr["alpha"], pr["beta"])
     opt = {"optimizer_name": "custom", "learning_rate": lr, "sched": {"scheduler_name": "exponential", "decay_rate": 0.9}}
     model = {"model_type": "mlp", "mlp": {"hidden_layers_m": 1, "hidden_dim_m": 1, "activation_m": "jnp.tanh",
-                                          "hidden_layers_p": 2, "hidden_dim_p": 10, "activation_p": "jnp.tanh"}}
+                                          "hidden_layers_p": 2, "hidden_dim_p": 10, "activation_p": "jnp.tanh"},
+             "preconditioner": pre or {"enable": False}}
     state, solve_fn = init_fn(lvl_gstate=g, tr_gstate=g, eval_gstate=g, num_epochs=epochs, batch_size=n ** 3,
                               optimizer_dict=opt, model_dict=model, print_rate=0, seed=42)
     state, epoch_store, loss_epochs = solve_fn(state)
     return g, pr, state, epoch_store, np.asarray(loss_epochs), solve_fn.trainer
 
 
-def _oracle_losses(g, pr, epochs, lr, arch):
+def _oracle_losses(g, pr, epochs, lr, arch, oarch=None):
     phi = O.perturb(np.asarray(pr["phi"](g.R.T), F32))
     prob = L.Problem(phi, g.x, g.y, g.z, pr)
     params = nn.init_params(arch, 42)
@@ -51,7 +52,7 @@ def _oracle_losses(g, pr, epochs, lr, arch):
             h = np.array([g.dx, g.dy, g.dz], F32) * F32(0.5**k)
             rg = L.ResidualGeometry(prob, g.R, h)
             cur = k
-        loss, grad = L.loss_and_grad(params, L.Arch(1, 1, 2, 10), rg)
+        loss, grad = L.loss_and_grad(params, oarch or L.Arch(1, 1, 2, 10), rg)
         losses.append(float(loss))
         params = adam.update(params, np.asarray(grad, F32))
     return np.array(losses), params
@@ -93,3 +94,17 @@ def test_training_reduces_the_solution_error():
     print(msg)
     assert losses[-1] < 0.2 * losses[0], msg
     assert err < 0.5 * err0, msg
+
+
+def test_learned_preconditioner_through_the_api():
+    """model_dict["preconditioner"] = {enable, layer_widths, scaling_coeff} (trainer.py:229-243):
+    the preconditioner's parameters are trained with the networks and the per-epoch losses follow
+    the oracle's loop with the same preconditioner."""
+    n, epochs, lr = 12, 6, 1e-2
+    pre = {"enable": True, "layer_widths": [16, 16], "scaling_coeff": 1.0}
+    g, pr, state, _, losses, tr = _run_api(n, epochs, lr, pre)
+    assert (tr.arch.pre_layers, tr.arch.pre_width) == (2, 16)
+    tree = nn.params_to_tree(tr.params.cpu(), tr.arch)
+    assert sorted(tree["preconditioner"]["params"]) == ["Dense_0", "Dense_1", "Dense_2"]
+    ref, _ = _oracle_losses(g, pr, epochs, lr, tr.arch, L.Arch(1, 1, 2, 10, 2, 16, 1.0))
+    np.testing.assert_allclose(losses, ref, rtol=5e-4)
