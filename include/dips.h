@@ -125,6 +125,10 @@ int dips_phi_ghost_layer(const float* phi, int32_t nx, int32_t ny, int32_t nz, f
 /* Trilinear interpolation of the ghosted cube at n points (multilinear_interpolation). */
 int dips_phi_trilinear(const dips_levelset_t* ls, const float* pts, int64_t n, float* out,
                        cudaStream_t stream);
+/* Non-oscillatory quadratic interpolant of the same ghosted field at n points: the trilinear
+   value minus 0.5 t (1 - t) min|second difference| per axis over the cell's corners
+   (nonoscillatory_quadratic_interpolation, domain/interpolate.py:572-759). */
+int dips_phi_quadratic(const dips_levelset_t* ls, const float* pts, int64_t n, float* out, cudaStream_t stream);
 
 /* ---- geometry: replaces geometry/geometric_integrations_per_point.py:201-1009 and
         solvers/poisson/discretization.py:164-519 (the parameter-independent part) ------- */

@@ -546,6 +546,16 @@ __global__ void k_trilinear(LevelSet L0, const float* __restrict__ pts, int64_t 
   }
 }
 
+__global__ void k_quadratic(LevelSet L0, const float* __restrict__ pts, int64_t n, float* __restrict__ out) {
+  LevelSet L = L0;
+  levelset_init(L);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float p[3];
+    load_point(pts, i, p);
+    out[i] = quad_at(L, p[0], p[1], p[2]);
+  }
+}
+
 struct H3 {
   float v[3];
 };
@@ -857,6 +867,19 @@ extern "C" int dips_phi_trilinear(const dips_levelset_t* ls, const float* pts, i
   if (st) return st;
   k_trilinear<<<grid_for(n, 256), 256, 0, stream>>>(L, pts, n, out);
   DIPS_CHECK_LAUNCH("dips_phi_trilinear");
+  return DIPS_OK;
+}
+
+extern "C" int dips_phi_quadratic(const dips_levelset_t* ls, const float* pts, int64_t n, float* out,
+                                  cudaStream_t stream) {
+  DIPS_REQUIRE(n >= 0, DIPS_E_ARG, "dips_phi_quadratic: negative n");
+  if (n == 0) return DIPS_OK;
+  DIPS_REQUIRE(pts && out, DIPS_E_ARG, "dips_phi_quadratic: null pointer");
+  LevelSet L;
+  int st = make_ls(ls, &L, stream);
+  if (st) return st;
+  k_quadratic<<<grid_for(n, 256), 256, 0, stream>>>(L, pts, n, out);
+  DIPS_CHECK_LAUNCH("dips_phi_quadratic");
   return DIPS_OK;
 }
 

@@ -90,4 +90,46 @@ __device__ __forceinline__ float phi_at(const LevelSet& L, float xp, float yp, f
 
 __device__ __forceinline__ float phi_at(const LevelSet& L, const float x[3]) { return phi_at(L, x[0], x[1], x[2]); }
 
+// Value of the ghosted field at (i, j, k) with every index clamped into the cube (the
+// reference's out-of-range gathers clamp), and its second difference along one axis.
+__device__ __forceinline__ float field_at(const LevelSet& L, int i, int j, int k) {
+  i = min(max(i, 0), L.n0 - 1);
+  j = min(max(j, 0), L.n1 - 1);
+  k = min(max(k, 0), L.n2 - 1);
+  return __ldg(L.g + ((int64_t)i * L.n1 + j) * L.n2 + k);
+}
+__device__ __forceinline__ float second_diff(const LevelSet& L, int i, int j, int k, int di, int dj, int dk) {
+  // c[+1] - 2 c[0] + c[-1], left to right
+  return __fadd_rn(__fsub_rn(field_at(L, i + di, j + dj, k + dk), __fmul_rn(2.0f, field_at(L, i, j, k))),
+                   field_at(L, i - di, j - dj, k - dk));
+}
+
+// Non-oscillatory quadratic interpolant (Min & Gibou 2007 eqs. 12-13 as the reference writes it,
+// interpolate.py:572-759): the trilinear value minus, per axis, 0.5 t (1 - t) times the smallest
+// |second difference| along that axis over the cell's 8 corners.
+__device__ __forceinline__ float quad_at(const LevelSet& L, float xp, float yp, float zp) {
+  const int i = ll_index(xp, L.xg[0], L.dx0, L.n0);
+  const int j = ll_index(yp, L.yg[0], L.dy0, L.n1);
+  const int k = ll_index(zp, L.zg[0], L.dz0, L.n2);
+  const float xd = __fdiv_rn(__fsub_rn(xp, L.xg[i]), __fsub_rn(L.xg[i + 1], L.xg[i]));
+  const float yd = __fdiv_rn(__fsub_rn(yp, L.yg[j]), __fsub_rn(L.yg[j + 1], L.yg[j]));
+  const float zd = __fdiv_rn(__fsub_rn(zp, L.zg[k]), __fsub_rn(L.zg[k + 1], L.zg[k]));
+  float mx = INFINITY, my = INFINITY, mz = INFINITY;
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        mx = fminf(mx, fabsf(second_diff(L, i + a, j + b, k + c, 1, 0, 0)));
+        my = fminf(my, fabsf(second_diff(L, i + a, j + b, k + c, 0, 1, 0)));
+        mz = fminf(mz, fabsf(second_diff(L, i + a, j + b, k + c, 0, 0, 1)));
+      }
+  float v = phi_at(L, xp, yp, zp);
+  v = __fsub_rn(v, __fmul_rn(__fmul_rn(__fmul_rn(mx, 0.5f), xd), __fsub_rn(1.0f, xd)));
+  v = __fsub_rn(v, __fmul_rn(__fmul_rn(__fmul_rn(my, 0.5f), yd), __fsub_rn(1.0f, yd)));
+  v = __fsub_rn(v, __fmul_rn(__fmul_rn(__fmul_rn(mz, 0.5f), zd), __fsub_rn(1.0f, zd)));
+  return v;
+}
+
 }  // namespace dips

@@ -191,6 +191,7 @@ _SIGS = {
     "dips_fp32_fma_probe": (c_i32, [c_void_p, c_i32, c_i32, c_void_p]),
     "dips_phi_ghost_layer": (c_i32, [c_void_p, c_i32, c_i32, c_i32, c_void_p, c_void_p]),
     "dips_phi_trilinear": (c_i32, [P(LevelSetT), c_void_p, c_i64, c_void_p, c_void_p]),
+    "dips_phi_quadratic": (c_i32, [P(LevelSetT), c_void_p, c_i64, c_void_p, c_void_p]),
     "dips_geometry_classify": (
         c_i32,
         [P(LevelSetT), c_void_p, c_i64, P(c_f32), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],

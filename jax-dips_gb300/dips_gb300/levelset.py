@@ -65,6 +65,17 @@ class LevelSetGrid:
         vals = torch.as_tensor(phi_fn(R.T), device=device, dtype=torch.float32)
         return cls(gstate, vals.reshape(-1), device)
 
+    def quadratic(self, pts: torch.Tensor) -> torch.Tensor:
+        """Non-oscillatory quadratic interpolation at points (n, 3) (interpolate.py:572-759)."""
+        lib = _lib.load()
+        pts = pts.to(torch.float32).contiguous()
+        out = torch.empty(pts.shape[0], dtype=torch.float32, device=pts.device)
+        _lib.check(
+            lib.dips_phi_quadratic(self.desc, _lib.ptr(pts), pts.shape[0], _lib.ptr(out), _lib.stream_handle()),
+            "dips_phi_quadratic",
+        )
+        return out
+
     def __call__(self, pts: torch.Tensor) -> torch.Tensor:
         """Trilinear interpolation at points (n, 3)."""
         lib = _lib.load()

@@ -172,6 +172,43 @@ class Trilinear:
         c = c0 * (one - zd) + c1 * zd
         return c.astype(F32).reshape(shp)
 
+    def quadratic(self, pts):
+        """``nonoscillatory_quadratic_interpolation`` (interpolate.py:572-759), float32: the
+        trilinear value minus 0.5 t (1 - t) min|second difference| per axis over the cell's 8
+        corners; out-of-range neighbour indices clamp into the ghosted cube (jax gathers clamp)."""
+        pts = np.asarray(pts, F32)
+        shp = pts.shape[:-1]
+        pts = pts.reshape(-1, 3)
+        xp, yp, zp = pts[:, 0], pts[:, 1], pts[:, 2]
+        xx, yy, zz, g = self.xx, self.yy, self.zz, self.gh
+        n0, n1, n2 = g.shape
+        i = self._index(xp, xx)
+        j = self._index(yp, yy)
+        k = self._index(zp, zz)
+
+        def at(a, b, c):
+            return g[np.clip(a, 0, n0 - 1), np.clip(b, 0, n1 - 1), np.clip(c, 0, n2 - 1)]
+
+        two, half, one = F32(2.0), F32(0.5), F32(1.0)
+        mins = []
+        for di, dj, dk in ((1, 0, 0), (0, 1, 0), (0, 0, 1)):
+            m = None
+            for a in (0, 1):
+                for b in (0, 1):
+                    for c in (0, 1):
+                        I, J, K = i + a, j + b, k + c
+                        d2 = (at(I + di, J + dj, K + dk) - two * at(I, J, K)) + at(I - di, J - dj, K - dk)
+                        m = np.abs(d2) if m is None else np.minimum(m, np.abs(d2))
+            mins.append(m)
+        xd = (xp - xx[i]) / (xx[i + 1] - xx[i])
+        yd = (yp - yy[j]) / (yy[j + 1] - yy[j])
+        zd = (zp - zz[k]) / (zz[k + 1] - zz[k])
+        v = self(pts).reshape(-1)
+        v = v - mins[0] * half * xd * (one - xd)
+        v = v - mins[1] * half * yd * (one - yd)
+        v = v - mins[2] * half * zd * (one - zd)
+        return v.astype(F32).reshape(shp)
+
 
 # ----------------------------------------------------------------------------------------
 # small fp32 helpers restating jnp semantics

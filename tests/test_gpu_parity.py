@@ -215,3 +215,16 @@ def test_learned_preconditioner_loss_and_gradient(name, n, arch, level, batch):
     assert npre > 0
     gp, rp = np.asarray(gg)[-npre:], np.asarray(gr)[-npre:]
     assert np.linalg.norm(gp - rp) <= GRAD_RTOL * np.linalg.norm(rp)
+
+
+def test_quadratic_interpolation_bit_exact():
+    from dips_gb300 import levelset, mesh
+
+    g = mesh.uniform_grid(23)
+    rng = np.random.default_rng(9)
+    vals = rng.standard_normal(23 ** 3).astype(F32)
+    T = O.Trilinear(vals, g.x, g.y, g.z)
+    ls = levelset.LevelSetGrid(g, vals)
+    pts = rng.uniform(-1.3, 1.3, (20000, 3)).astype(F32)  # inside, near and beyond the box
+    got = ls.quadratic(torch.as_tensor(pts, device="cuda")).cpu().numpy()
+    np.testing.assert_array_equal(got, T.quadratic(pts))

@@ -112,3 +112,22 @@ def test_h_schedule_and_sequential_batches():
     assert [O.h_level(200, e) for e in (0, 49, 50, 149, 150, 199)] == [0, 0, 1, 2, 3, 3]
     assert O.sequential_batches(32768, 262144) == (1, 32768, 0)
     assert O.sequential_batches(1000, 300) == (4, 300, 200)
+
+
+def test_quadratic_interpolation_reproduces_a_convex_quadratic():
+    """The non-oscillatory quadratic interpolant (interpolate.py:572-759) subtracts
+    0.5 t (1 - t) min|D2| per axis from the trilinear value; for x^2 + y^2 + z^2 (second
+    differences 2 dx^2 everywhere) that cancels the trilinear error exactly."""
+    from dips_gb300 import mesh
+
+    g = mesh.uniform_grid(17)
+    X, Y, Z = np.meshgrid(g.x, g.y, g.z, indexing="ij")
+    vals = (X * X + Y * Y + Z * Z).astype(np.float32)
+    T = O.Trilinear(vals.reshape(-1), g.x, g.y, g.z)
+    rng = np.random.default_rng(2)
+    p = rng.uniform(-0.8, 0.8, (4000, 3)).astype(np.float32)
+    exact = (p ** 2).sum(1)
+    q = T.quadratic(p)
+    t = T(p)
+    assert np.max(np.abs(q - exact)) < 2e-5
+    assert np.max(np.abs(t - exact)) > 100 * np.max(np.abs(q - exact))
