@@ -99,6 +99,13 @@ def adam_state_from_dict(n_params, optimizer_dict, device):
 _TUNED = set()
 
 
+def _to_numpy(tree):
+    """Nested dict of tensors -> nested dict of numpy arrays (checkpoint contents)."""
+    if isinstance(tree, dict):
+        return {k: _to_numpy(v) for k, v in tree.items()}
+    return np.asarray(tree.detach().cpu() if torch.is_tensor(tree) else tree)
+
+
 def _levels(num_epochs):
     q = max(num_epochs // 4, 1)
     return (num_epochs - 1) // q + 1 if num_epochs > 0 else 1
@@ -295,8 +302,7 @@ class Trainer:
         state = {
             "opt_state": {"mu": self.opt.mu.cpu().numpy(), "nu": self.opt.nu.cpu().numpy(),
                           "count": int(self.opt.count.item())},
-            "params": {k: ({kk: np.asarray(vv.cpu()) for kk, vv in v.items()} if v else {})
-                       for k, v in nn.params_to_tree(self.params, self.arch).items()},
+            "params": _to_numpy(nn.params_to_tree(self.params, self.arch)),
             "epoch": int(epoch),
             "batch_size": int(self.batch),
             "resolution": f"{self.h0[0]}, {self.h0[1]}, {self.h0[2]}",
