@@ -68,6 +68,10 @@ def parse():
                          "500 Gaussians, mu 1/100, k = 0.5; lpbe: --instances linearised Poisson-Boltzmann problems "
                          "of uneven size (sides 48..160), 2x16 networks, one graph launch per batched step")
     ap.add_argument("--instances", type=int, default=64)
+    ap.add_argument("--c1", action="store_true",
+                    help="configuration 1 end to end through trainer.setup/init_fn/solve_fn: sphere 32^3, "
+                         "DoubleMLP 1x1/2x10, full batch, 200 epochs, lr 1e-3 decaying 0.9; CPU oracle timed "
+                         "on a few epochs")
     ap.add_argument("--arch", default="3x32", choices=["3x32", "4x64", "2x16"],
                     help="hidden layers x width of both networks (4x64 runs on the TF32 tensor cores)")
     ap.add_argument("--n-ls", type=int, default=0, help="level-set grid side (default: the training grid's)")
@@ -505,6 +509,64 @@ def run_instances(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def run_c1(args, rank, world):
+    """Configuration 1 through the reference-facing API, timed end to end (the GPU solve), with
+    the oracle's per-epoch CPU time beside it."""
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import nbm_loss as L
+    import nbm_oracle as O
+    from dips_gb300 import levelset, mesh, nn, problems, trainer
+
+    if rank != 0:
+        return
+    pr = problems.sphere_problem()
+    n, epochs = 32, 200
+    g = mesh.uniform_grid(n)
+    phi = lambda r: levelset.perturb(pr["phi"](r))  # noqa: E731
+    init_fn = trainer.setup(pr["u_p"], pr["g"], phi, pr["mu_m"], pr["mu_p"], pr["k_m"], pr["k_p"], pr["f_m"],
+                            pr["f_p"], pr["alpha"], pr["beta"])
+    opt = {"optimizer_name": "custom", "learning_rate": 1e-3, "sched": {"scheduler_name": "exponential",
+                                                                        "decay_rate": 0.9}}
+    model = {"model_type": "mlp", "mlp": {"hidden_layers_m": 1, "hidden_dim_m": 1, "activation_m": "jnp.tanh",
+                                          "hidden_layers_p": 2, "hidden_dim_p": 10, "activation_p": "jnp.tanh"}}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    state, solve_fn = init_fn(lvl_gstate=g, tr_gstate=g, eval_gstate=g, num_epochs=epochs, batch_size=n ** 3,
+                              optimizer_dict=opt, model_dict=model, print_rate=0, seed=0, checkpoint_dir="")
+    state, _, losses = solve_fn(state)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ex = np.asarray(pr["exact"](g.R.T), np.float32)
+    u = torch.as_tensor(state.solution).reshape(-1).cpu().numpy()
+    err = float(np.max(np.abs(u - ex)) / np.max(np.abs(ex)))
+    # CPU: the oracle's training step on the full batch (geometry per level + loss + gradient)
+    phi_np = O.perturb(np.asarray(pr["phi"](g.R.T), np.float32))
+    prob = L.Problem(phi_np, g.x, g.y, g.z, pr)
+    a = L.Arch(1, 1, 2, 10)
+    w = L.init_params(a, 0)
+    tg0 = time.perf_counter()
+    rg = L.ResidualGeometry(prob, g.R, np.array([g.dx, g.dy, g.dz], np.float32))
+    t_geo = time.perf_counter() - tg0
+    cpu_ep = []
+    for _ in range(3):
+        tc = time.perf_counter()
+        L.loss_and_grad(w, a, rg)
+        cpu_ep.append(time.perf_counter() - tc)
+    cpu_est = 4 * t_geo + epochs * statistics.median(cpu_ep)
+    line = {"metric": "configuration 1 end to end (trainer.setup -> init_fn -> solve_fn)", "value": wall, "unit": "s",
+            "n_gpus": 1, "steps": epochs, "warmup": 0, "ms_per_step": 1e3 * wall / epochs, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "sphere 32^3, DoubleMLP 1x1/2x10, full batch (32768), 200 epochs, h halved at "
+                                   "epochs 50/100/150, chained Adam lr 1e-3 decay 0.9",
+                       "final_loss": float(losses[-1]), "first_loss": float(losses[0]), "rel_linf": err},
+            "cpu_baseline": {"value": cpu_est, "unit": "s", "cores": torch.get_num_threads(), "kind": "port",
+                             "sample": f"geometry of one level {t_geo:.2f} s (x4 levels) + loss/gradient "
+                                       f"{statistics.median(cpu_ep):.3f} s per epoch (x{epochs}), measured on 3 epochs"}}
+    print(json.dumps(line), flush=True)
+
+
 def time_to_target(args, lvl, g, pr, arch, dev):
     import torch
 
@@ -619,6 +681,8 @@ def main():
         dist.init_process_group(backend)
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.c1:
+        run_c1(args, rank, world)
     elif args.problem == "lpbe":
         run_instances(args, rank, world)
     else:
