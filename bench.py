@@ -38,7 +38,7 @@ ARCH = (3, 32, 3, 32)
 
 # DRAM bytes (read + write) of one launch of the dominant kernel, keyed by (grid side, batch),
 # from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum); absent until captured.
-FUSED_TRAFFIC = {(128, 1 << 18): 19_930_000}
+FUSED_TRAFFIC = {}
 
 
 def net_flops(layers, width):
@@ -312,15 +312,21 @@ def run_ours(args, rank, world):
         phases.append(ops.phase_ms(evs))
     phase_med = {k: statistics.median(p[k] for p in phases) for k in ops.STEP_PHASES}
     tensor = ARCH[1] == 64
-    # the dominant launch: for 3x32 the u+ tile launch (forward + adjoint of every u+ job: the 7
-    # stencil jobs of each bulk u+ point and the u+ jobs of the other points); for 4x64 the u+
-    # tensor-core adjoint (which also recomputes the forward).  3 F per job either way; the
-    # forward that feeds the residual and the recompute are not counted.
-    kind = "adjoint" if tensor else "fused"
-    dom_net = "p" if phase_med[f"{kind}_p"] >= phase_med[f"{kind}_m"] else "m"
-    t_dom = phase_med[f"{kind}_{dom_net}"] / 1e3
-    dom_jobs, dom_f = (jobs_p, f_p) if dom_net == "p" else (jobs_m, f_m)
-    dom_flops = 3 * dom_jobs * dom_f
+    # the dominant launch: for 3x32 the tile engine's training launch, one launch for both
+    # networks (forward + adjoint + dW of every job: the 7 stencil jobs of each bulk point and the
+    # jobs of the other points); for 4x64 the u+ tensor-core adjoint (which also recomputes the
+    # forward).  3 F per job either way; the forward that feeds the residual and the recompute
+    # are not counted.
+    if tensor:
+        dom_net = "p" if phase_med["adjoint_p"] >= phase_med["adjoint_m"] else "m"
+        t_dom = phase_med[f"adjoint_{dom_net}"] / 1e3
+        dom_jobs, dom_f = (jobs_p, f_p) if dom_net == "p" else (jobs_m, f_m)
+        dom_flops = 3 * dom_jobs * dom_f
+    else:
+        dom_net = "both"
+        t_dom = (phase_med["fused_m"] + phase_med["fused_p"]) / 1e3
+        dom_jobs, dom_f = jobs_m + jobs_p, f_m
+        dom_flops = 3 * fwd_flops
     # FP32 FMA peak of this GPU (measured)
     probe = torch.empty(152 * 16 * 256, dtype=torch.float32, device=dev)
     iters = 4096
@@ -403,11 +409,11 @@ def run_ours(args, rank, world):
             "roofline": {"bound": "tensor" if tensor else "fp32",
                          "kernel": (f"tcnet::k_tc_adjoint<u{'+' if dom_net == 'p' else '-'} net> (tcgen05 TF32: "
                                     "recomputed forward, adjoint and dW of every job of that network)" if tensor else
-                                    f"tile::k_tile_net<u{'+' if dom_net == 'p' else '-'} net, backward> (forward, bulk "
-                                    "residual, adjoint and dW of every job of that network)"),
+                                    "tile::k_tile<3x32, kTrain> (one launch for both networks: forward, bulk "
+                                    "residual, adjoint and dW of every job)"),
                          "achieved": dom_tflops, "peak": dom_peak, "unit": "TFLOP/s",
                          "frac": dom_tflops / dom_peak, "traffic": FUSED_TRAFFIC.get((args.n, B)),
-                         "algorithmic": f"3 x F per job of the network, F = sum(2*in*out+out) + tanh count = "
+                         "algorithmic": f"3 x F per job, F = sum(2*in*out+out) + tanh count = "
                                         f"{dom_f}; {dom_jobs} jobs per launch (bulk points: {bulk_m} u-, {bulk_p} u+)",
                          "peak_source": peak_src, "fp32_peak_tflops": fp32_peak,
                          "phase_ms": phase_med,
@@ -415,7 +421,7 @@ def run_ours(args, rank, world):
                          "step_algorithmic": "3 x F x (all jobs of the batch) per step"},
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "gpu_launches": (12 if tensor else 14) * args.steps,
+            "gpu_launches": (12 if tensor else 10) * args.steps,
             "clocks": clk,
             "time_to_target": tta,
         }

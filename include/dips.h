@@ -156,6 +156,17 @@ int dips_geometry_assemble(const dips_levelset_t* ls, const float* pts, int64_t 
                            float* rod, int32_t* cnt, int32_t* cnt_m, uint16_t* job_code, float* job_A,
                            float* coeff26, float* beta_int, cudaStream_t stream);
 
+/* Derivative of the records along a direction in coefficient space (no counterpart in the
+   reference, which would take jax.jvp of its assembly): dco holds the derivative of every
+   coefficient sample of `co` along the direction (same layout; NULL arrays are zero, e.g. only
+   mu_p_face, mu_p_s and mu_p_r set to 1 for d/d mu+ of a constant mu+).  Writes d lhs0, d diag,
+   d rod [n] and d job_A [jobs] (job order of dips_geometry_assemble).  The geometry and the
+   discrete branches are the records' own, so this is the exact derivative of the records. */
+int dips_geometry_assemble_tangent(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
+                                   const uint32_t* flags, const int64_t* tri_off, const int64_t* xs_off,
+                                   const int64_t* job_off, const dips_coeffs_t* co, const dips_coeffs_t* dco,
+                                   float* d_lhs0, float* d_diag, float* d_rod, float* d_job_A, cudaStream_t stream);
+
 /* ---- residual, loss, adjoint, optimizer: replace Trainer.loss (trainer.py:892-912),
         value_and_grad in Trainer.update (:783-789) and the optax chain ---------------- */
 int32_t dips_num_params(const dips_arch_t* arch);
@@ -173,6 +184,14 @@ int dips_residual_fwd(const dips_arch_t* arch, const float* params, const dips_r
 int dips_residual_bwd(const dips_arch_t* arch, const float* params, const dips_records_t* rec,
                       const int32_t* batch_ids, int64_t batch, void* workspace, size_t ws_bytes,
                       float* grad_out, cudaStream_t stream);
+/* d loss / d theta of the dips_residual_fwd loss along a coefficient direction theta, the
+   params fixed (the gradient of the total loss with respect to a physical coefficient such as
+   mu+): trec carries the tangent records from dips_geometry_assemble_tangent in its lhs0, diag,
+   rod and job_A fields (its other fields are ignored).  dloss_out: device double.  Not for
+   arch with the learned preconditioner (DIPS_E_UNSUPPORTED). */
+int dips_loss_coeff_tangent(const dips_arch_t* arch, const float* params, const dips_records_t* rec,
+                            const dips_records_t* trec, const int32_t* batch_ids, int64_t batch, void* workspace,
+                            size_t ws_bytes, double* dloss_out, cudaStream_t stream);
 /* One chained-Adam update of params (in place) from grad; mu, nu: [num_params];
    count: device int64 step counter (incremented). */
 int dips_adam_step(const dips_arch_t* arch, const dips_adam_t* hp, float* params, const float* grad,
@@ -204,7 +223,7 @@ int dips_train_step_noalloc(const dips_arch_t* arch, const dips_adam_t* hp, floa
                             int64_t max_jobs, double* loss_out, float* grad_out, cudaStream_t stream);
 /* Autotuner (no counterpart in the reference): runs the residual forward on this batch, then
    times each launch configuration of the shape's tunable point kernel (for 3x32: the
-   register-blocked engine as 12 warps x 1 CTA, 6 x 2 or 4 x 3 per SM) and keeps the fastest for
+   register-blocked engine, one CTA per SM of 12, 10 or 8 warps) and keeps the fastest for
    the current device, process-wide.  Synchronises `stream`; call it before capturing a graph.
    *choice_out (host, may be NULL) receives the warps per CTA chosen, 0 when the shape has
    nothing to tune.  The workspace is left in an unspecified state. */

@@ -44,12 +44,12 @@ __host__ __device__ inline bool job_net_p(uint16_t c) { return (c & 0x8000) != 0
 // Stencil point j of point p at spacing h, with the reference's float32 operations
 // (discretization.py:347-353): the shifted coordinate is p[a] -/+ h[a].
 __device__ __forceinline__ void stencil_point(const float p[3], const float h[3], int j, float s[3]) {
-  s[0] = p[0];
-  s[1] = p[1];
-  s[2] = p[2];
-  if (j > 0) {
-    int a = (j - 1) >> 1;
-    s[a] = ((j - 1) & 1) ? __fadd_rn(p[a], h[a]) : __fsub_rn(p[a], h[a]);
+  // selects over the three axes (no run-time array index, which would put p, h and s in local
+  // memory); p - h is computed as p + (-h), the same rounded value
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const bool moved = j > 0 && ((j - 1) >> 1) == a;
+    s[a] = moved ? __fadd_rn(p[a], ((j - 1) & 1) ? h[a] : -h[a]) : p[a];
   }
 }
 

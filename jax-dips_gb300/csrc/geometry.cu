@@ -638,12 +638,24 @@ __global__ void k_queries(LevelSet L0, const float* __restrict__ pts, int64_t n,
   }
 }
 
+// tangent sample (0 where the direction leaves that coefficient unchanged)
+__device__ __forceinline__ float tsample(const float* a, int64_t i) { return a ? a[i] : 0.0f; }
+
+// Records of each point (discretization.py:356-424 with the extrapolation of :464-513).
+// With TAN the kernel writes, instead of the records, their derivative along a direction in
+// coefficient space: dco holds d(sample) of every coefficient sample (NULL arrays: zero) and
+// lhs0_out, diag_out, rod_out, A_out receive d lhs0, d diag, d rod and d A (same job order as
+// the records; code_out, cnt_out, cntm_out, coeff26_out, beta_int_out are not written).  The
+// geometry is the same in both modes and the branches (which phase is extrapolated, which cube
+// vertices have a weight) are the records' own, so the tangent is the exact derivative of the
+// records as a function of the coefficients.
+template <bool TAN>
 __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n, H3 hh, const uint32_t* __restrict__ flags,
                            const int64_t* __restrict__ tri_off, const int64_t* __restrict__ xs_off,
-                           const int64_t* __restrict__ job_off, dips_coeffs_t co, float* __restrict__ lhs0_out,
-                           float* __restrict__ diag_out, float* __restrict__ rod_out, int32_t* __restrict__ cnt_out,
-                           int32_t* __restrict__ cntm_out, uint16_t* __restrict__ code_out, float* __restrict__ A_out,
-                           float* __restrict__ coeff26_out, float* __restrict__ beta_int_out) {
+                           const int64_t* __restrict__ job_off, dips_coeffs_t co, dips_coeffs_t dco,
+                           float* __restrict__ lhs0_out, float* __restrict__ diag_out, float* __restrict__ rod_out,
+                           int32_t* __restrict__ cnt_out, int32_t* __restrict__ cntm_out, uint16_t* __restrict__ code_out,
+                           float* __restrict__ A_out, float* __restrict__ coeff26_out, float* __restrict__ beta_int_out) {
   LevelSet L = L0;
   levelset_init(L);
   const float* h = hh.v;
@@ -655,31 +667,37 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
     int64_t wm = job_off[i];          // u- jobs from the front
     int64_t wp = job_off[i + 1] - 1;  // u+ jobs from the back
     int nm = 0, np = 0;
+    // A: the job's coefficient, or its tangent
     auto emit = [&](int j, int k, bool netp, float A) {
-      uint16_t c = job_code(j, k, netp);
+      const int64_t o = netp ? wp : wm;
+      if (!TAN) code_out[o] = job_code(j, k, netp);
+      A_out[o] = A;
       if (netp) {
-        code_out[wp] = c;
-        A_out[wp] = A;
         --wp;
         ++np;
       } else {
-        code_out[wm] = c;
-        A_out[wm] = A;
         ++wm;
         ++nm;
       }
     };
     Cell cell;
     cell_eval(L, p, h, cell);
-    float mm[6], mp[6];
+    float mm[6], mp[6], tmm[6], tmp[6];
     for (int q = 0; q < 6; ++q) {
       mm[q] = co.mu_m_face[6 * i + q];
       mp[q] = co.mu_p_face[6 * i + q];
+      tmm[q] = TAN ? tsample(dco.mu_m_face, 6 * i + q) : 0.0f;
+      tmp[q] = TAN ? tsample(dco.mu_p_face, 6 * i + q) : 0.0f;
     }
-    float c26[26];
+    float c26[26], t26[26];
     face_coefficients(cell, p, h, mm, mp, c26);
+    if (TAN) {
+      // the face fluxes (entries 0..11) are linear in the face mu's; the rest is geometry
+      face_coefficients(cell, p, h, tmm, tmp, t26);
+      for (int q = 12; q < 26; ++q) t26[q] = 0.0f;
+    }
     // interface integral of beta (integrate_over_interface_at_point, geom_pp.py:383-420)
-    float bint = 0.0f;
+    float bint = 0.0f, tbint = 0.0f;
     if (cell.crossed == 0) {
       const float b0 = co.beta_origin;
       const float pad_mean = __fdiv_rn(__fadd_rn(__fadd_rn(b0, b0), b0), 3.0f);
@@ -694,6 +712,9 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
           if (q < nt) {
             float a = tri_area(tri[q][0], tri[q][1], tri[q][2]);
             float b1 = co.beta_tri[o], b2 = co.beta_tri[o + 1], b3 = co.beta_tri[o + 2];
+            if (TAN)
+              tbint += a * (tsample(dco.beta_tri, o) + tsample(dco.beta_tri, o + 1) + tsample(dco.beta_tri, o + 2)) /
+                       3.0f;
             o += 3;
             term = __fmul_rn(a, __fdiv_rn(__fadd_rn(__fadd_rn(b1, b2), b3), 3.0f));
           } else {
@@ -704,49 +725,68 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
         }
       }
     }
-    if (coeff26_out)
+    if (!TAN && coeff26_out)
       for (int q = 0; q < 26; ++q) coeff26_out[26 * i + q] = c26[q];
-    if (beta_int_out) beta_int_out[i] = bint;
+    if (!TAN && beta_int_out) beta_int_out[i] = bint;
 
     if (f & 1u) {  // box boundary: lhs = u*V, rhs = g*V (discretization.py:389-393, :410-411)
       const bool net = (f >> kFlagNetS) & 1u;
-      emit(0, kCubeCentre, net, V);
+      emit(0, kCubeCentre, net, TAN ? 0.0f : V);
       lhs0_out[i] = 0.0f;
-      diag_out[i] = V;
-      rod_out[i] = nan_to_num(__fdiv_rn(__fmul_rn(co.g[i], V), V));
-      cnt_out[i] = nm + np;
-      cntm_out[i] = nm;
+      if (TAN) {
+        diag_out[i] = 0.0f;
+        rod_out[i] = isfinite(__fdiv_rn(__fmul_rn(co.g[i], V), V)) ? tsample(dco.g, i) : 0.0f;
+      } else {
+        diag_out[i] = V;
+        rod_out[i] = nan_to_num(__fdiv_rn(__fmul_rn(co.g[i], V), V));
+        cnt_out[i] = nm + np;
+        cntm_out[i] = nm;
+      }
       continue;
     }
     const float Vm = c26[12], Vp = c26[13];
     const float km = co.k_m[i], kp = co.k_p[i];
-    float se = c26[0], so = c26[1];
+    const float tkm = TAN ? tsample(dco.k_m, i) : 0.0f, tkp = TAN ? tsample(dco.k_p, i) : 0.0f;
+    float se = c26[0], so = c26[1], tse = t26[0], tso = t26[1];
     for (int q = 1; q < 6; ++q) {
       se = __fadd_rn(se, c26[2 * q]);
       so = __fadd_rn(so, c26[2 * q + 1]);
+      if (TAN) {
+        tse += t26[2 * q];
+        tso += t26[2 * q + 1];
+      }
     }
     const float diag =
         __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(kp, Vp), __fmul_rn(km, Vm)), se), so);
     float rhs = __fadd_rn(__fmul_rn(co.f_m[i], Vm), __fmul_rn(co.f_p[i], Vp));
     rhs = __fadd_rn(rhs, bint);
-    float Am[kStencil], Ap[kStencil];
+    float tdiag = 0.0f, trhs = 0.0f;
+    if (TAN) {
+      tdiag = tkp * Vp + tkm * Vm + tse + tso;
+      trhs = tsample(dco.f_m, i) * Vm + tsample(dco.f_p, i) * Vp + tbint;
+    }
+    float Am[kStencil], Ap[kStencil], tAm[kStencil], tAp[kStencil];
     Am[0] = __fadd_rn(__fmul_rn(km, Vm), se);
     Ap[0] = __fadd_rn(__fmul_rn(kp, Vp), so);
+    tAm[0] = tkm * Vm + tse;
+    tAp[0] = tkp * Vp + tso;
     for (int j = 1; j < kStencil; ++j) {
       Am[j] = -c26[2 * (j - 1)];
       Ap[j] = -c26[2 * (j - 1) + 1];
+      tAm[j] = -t26[2 * (j - 1)];
+      tAp[j] = -t26[2 * (j - 1) + 1];
     }
-    float lhs0 = 0.0f;
+    float lhs0 = 0.0f, tlhs0 = 0.0f;
     int64_t ox = xs_off[i];
     for (int j = 0; j < kStencil; ++j) {
       const int cj = dec_crossed(f, kFlagCrossedS + 2 * j);
       const bool netj = (f >> (kFlagNetS + j)) & 1u;
       if (cj == -1) {
-        emit(j, kCubeCentre, netj, Am[j]);
+        emit(j, kCubeCentre, netj, TAN ? tAm[j] : Am[j]);
         continue;
       }
       if (cj == 1) {
-        emit(j, kCubeCentre, netj, Ap[j]);
+        emit(j, kCubeCentre, netj, TAN ? tAp[j] : Ap[j]);
         continue;
       }
       // interface stencil point: extrapolate the other phase (discretization.py:464-513)
@@ -764,6 +804,9 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
       const float mus_m = co.mu_m_s[ox], mus_p = co.mu_p_s[ox];
       const float alpha = co.alpha_r[ox], beta = co.beta_r[ox];
       const float mur_m = co.mu_m_r[ox], mur_p = co.mu_p_r[ox];
+      const float tmus_m = TAN ? tsample(dco.mu_m_s, ox) : 0.0f, tmus_p = TAN ? tsample(dco.mu_p_s, ox) : 0.0f;
+      const float talpha = TAN ? tsample(dco.alpha_r, ox) : 0.0f, tbeta = TAN ? tsample(dco.beta_r, ox) : 0.0f;
+      const float tmur_m = TAN ? tsample(dco.mu_m_r, ox) : 0.0f, tmur_p = TAN ? tsample(dco.mu_p_r, ox) : 0.0f;
       ++ox;
       const bool mbig = mus_m > mus_p;
       const float delta = R.phi_s;
@@ -776,55 +819,82 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
       for (int k = 0; k < 27; ++k)
         C[k] = __fadd_rn(__fadd_rn(__fmul_rn(R.n[0], D[0][k]), __fmul_rn(R.n[1], D[1][k])), __fmul_rn(R.n[2], D[2][k]));
       // zeta^-_pqm = ((mu+ - mu-)/mu+) phi C^- ; zeta^+_pqm = ((mu+ - mu-)/mu-) phi C^+
-      const float fac = __fmul_rn(__fdiv_rn(__fsub_rn(mus_p, mus_m), mbig ? mus_p : mus_m), delta);
+      const float mden = mbig ? mus_p : mus_m, tmden = mbig ? tmus_p : tmus_m;
+      const float fac = __fmul_rn(__fdiv_rn(__fsub_rn(mus_p, mus_m), mden), delta);
+      const float tfac = TAN ? delta * ((tmus_p - tmus_m) / mden - (mus_p - mus_m) * tmden / (mden * mden)) : 0.0f;
       float Z[27];
-      float zsum = 0.0f;
+      float zsum = 0.0f, csum_off = 0.0f;
       for (int k = 0; k < 27; ++k) {
         Z[k] = __fmul_rn(fac, C[k]);
         zsum = (k == 0) ? Z[k] : __fadd_rn(zsum, Z[k]);
+        if (k != kCubeCentre) csum_off += C[k];
       }
       const float zeta = -__fsub_rn(zsum, Z[kCubeCentre]);
+      const float tzeta = -tfac * csum_off;
       // gamma^-_pqm = zeta^-_pqm / (1 - zeta^-); gamma^+_pqm = zeta^+_pqm / (1 + zeta^+)
       const bool use_gamma = (mbig && pos) || (!mbig && !pos);
       float G[27];
       float g;
+      float tg = tzeta, den = 1.0f, tden = 0.0f;
       if (use_gamma) {
-        const float den = mbig ? __fsub_rn(1.0f, zeta) : __fadd_rn(1.0f, zeta);
+        den = mbig ? __fsub_rn(1.0f, zeta) : __fadd_rn(1.0f, zeta);
+        tden = mbig ? -tzeta : tzeta;
         float gsum = 0.0f;
+        tg = 0.0f;
         for (int k = 0; k < 27; ++k) {
           G[k] = __fdiv_rn(Z[k], den);
           gsum = (k == 0) ? G[k] : __fadd_rn(gsum, G[k]);
+          if (TAN && k != kCubeCentre) tg -= (tfac * C[k]) / den - Z[k] * tden / (den * den);
         }
         g = -__fsub_rn(gsum, G[kCubeCentre]);
       } else {
         for (int k = 0; k < 27; ++k) G[k] = Z[k];
         g = zeta;
       }
+      // tangent of G[k]
+      auto tG = [&](int k) -> float {
+        return use_gamma ? (tfac * C[k]) / den - Z[k] * tden / (den * den) : tfac * C[k];
+      };
       // constant term of the extrapolated value
-      const float bmu = __fdiv_rn(beta, mbig ? mur_p : mur_m);
+      const float mur = mbig ? mur_p : mur_m, tmur = mbig ? tmur_p : tmur_m;
+      const float bmu = __fdiv_rn(beta, mur);
       const float jump = __fadd_rn(alpha, __fmul_rn(delta, bmu));
-      float K;
-      if (mbig)
+      const float tjump = talpha + delta * (tbeta / mur - beta * tmur / (mur * mur));
+      float K, tK;
+      if (mbig) {
         K = pos ? __fmul_rn(__fmul_rn(-1.0f, __fsub_rn(1.0f, g)), jump) : jump;
-      else
+        tK = pos ? tg * jump - (1.0f - g) * tjump : tjump;
+      } else {
         K = pos ? __fmul_rn(-1.0f, jump) : __fmul_rn(__fsub_rn(1.0f, g), jump);
+        tK = pos ? -tjump : -tg * jump + (1.0f - g) * tjump;
+      }
       const float Ax = pos ? Am[j] : Ap[j];  // coefficient of the extrapolated component
       const float Ao = pos ? Ap[j] : Am[j];  // coefficient of u itself
+      const float tAx = pos ? tAm[j] : tAp[j], tAo = pos ? tAp[j] : tAm[j];
       const float wc = __fadd_rn(__fsub_rn(__fmul_rn(Ax, __fadd_rn(__fsub_rn(1.0f, g), G[kCubeCentre])),
                                            __fmul_rn(Ax, G[kCubeCentre])),
                                  Ao);
-      emit(j, kCubeCentre, netj, wc);
+      // d wc: Ax (1 - g) + Ao as a function (the G[centre] terms cancel)
+      emit(j, kCubeCentre, netj, TAN ? tAx * (1.0f - g) - Ax * tg + tAo : wc);
       for (int k = 0; k < 27; ++k) {
         if (k == kCubeCentre || G[k] == 0.0f) continue;
-        emit(j, k, R.phi_v[k] >= 0.0f, -__fmul_rn(Ax, G[k]));
+        emit(j, k, R.phi_v[k] >= 0.0f, TAN ? -(tAx * G[k] + Ax * tG(k)) : -__fmul_rn(Ax, G[k]));
       }
       lhs0 = __fadd_rn(lhs0, __fmul_rn(Ax, K));
+      if (TAN) tlhs0 += tAx * K + Ax * tK;
     }
-    lhs0_out[i] = lhs0;
-    diag_out[i] = diag;
-    rod_out[i] = nan_to_num(__fdiv_rn(rhs, diag));
-    cnt_out[i] = nm + np;
-    cntm_out[i] = nm;
+    if (TAN) {
+      const float q = __fdiv_rn(rhs, diag);
+      lhs0_out[i] = tlhs0;
+      diag_out[i] = tdiag;
+      rod_out[i] = isfinite(q) ? (trhs - q * tdiag) / diag : 0.0f;
+    } else {
+      lhs0_out[i] = lhs0;
+      diag_out[i] = diag;
+      rod_out[i] = nan_to_num(__fdiv_rn(rhs, diag));
+      cnt_out[i] = nm + np;
+      cntm_out[i] = nm;
+    }
   }
 }
 
@@ -934,8 +1004,31 @@ extern "C" int dips_geometry_assemble(const dips_levelset_t* ls, const float* pt
   LevelSet L;
   int st = make_ls(ls, &L, stream);
   if (st) return st;
-  k_assemble<<<grid_for(n, 64), 64, 0, stream>>>(L, pts, n, make_h(h), flags, tri_off, xs_off, job_off, *co, lhs0,
-                                                 diag, rod, cnt, cnt_m, job_code, job_A, coeff26, beta_int);
+  dips_coeffs_t none{};
+  k_assemble<false><<<grid_for(n, 64), 64, 0, stream>>>(L, pts, n, make_h(h), flags, tri_off, xs_off, job_off, *co,
+                                                        none, lhs0, diag, rod, cnt, cnt_m, job_code, job_A, coeff26,
+                                                        beta_int);
   DIPS_CHECK_LAUNCH("dips_geometry_assemble");
+  return DIPS_OK;
+}
+
+extern "C" int dips_geometry_assemble_tangent(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
+                                              const uint32_t* flags, const int64_t* tri_off, const int64_t* xs_off,
+                                              const int64_t* job_off, const dips_coeffs_t* co, const dips_coeffs_t* dco,
+                                              float* d_lhs0, float* d_diag, float* d_rod, float* d_job_A,
+                                              cudaStream_t stream) {
+  DIPS_REQUIRE(n >= 0 && h && co && dco, DIPS_E_ARG, "dips_geometry_assemble_tangent: bad n, h or coeffs");
+  if (n == 0) return DIPS_OK;
+  DIPS_REQUIRE(pts && flags && tri_off && xs_off && job_off && d_lhs0 && d_diag && d_rod && d_job_A, DIPS_E_ARG,
+               "dips_geometry_assemble_tangent: null pointer");
+  DIPS_REQUIRE(co->mu_m_face && co->mu_p_face && co->k_m && co->k_p && co->f_m && co->f_p && co->g, DIPS_E_ARG,
+               "dips_geometry_assemble_tangent: null dense coefficient pointer");
+  LevelSet L;
+  int st = make_ls(ls, &L, stream);
+  if (st) return st;
+  k_assemble<true><<<grid_for(n, 64), 64, 0, stream>>>(L, pts, n, make_h(h), flags, tri_off, xs_off, job_off, *co,
+                                                       *dco, d_lhs0, d_diag, d_rod, nullptr, nullptr, nullptr, d_job_A,
+                                                       nullptr, nullptr);
+  DIPS_CHECK_LAUNCH("dips_geometry_assemble_tangent");
   return DIPS_OK;
 }

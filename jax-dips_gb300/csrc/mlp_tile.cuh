@@ -35,7 +35,7 @@
 
 namespace tile {
 
-constexpr int kWarpsPerSm = 12;  // 168 registers per thread; CTA shapes 12x1, 6x2, 4x3 (warps x CTAs)
+constexpr int kWarpsPerSm = 12;  // 168 registers per thread; one CTA per SM of 12 (default), 10 or 8 warps
 constexpr int kRS = 36;  // buffer row stride (floats)
 constexpr float kTanhScale = 2.8853900817779268f;  // 2 log2(e): tanh(z) = 1 - 2/(1 + 2^(kTanhScale z))
 
@@ -49,7 +49,9 @@ struct Layout {
   static constexpr int kW1 = kWT + 2 * W * W;   // [3][8*ob + t] = c * W_1[c][ob + 4t]
   static constexpr int kB = kW1 + 3 * W;        // [3][8*ob + t] = c * b_l[ob + 4t]
   static constexpr int kWO = kB + 3 * W;        // [8*ob + t] = w_o[ob + 4t]
-  static constexpr int kShared = kWO + W;
+  static constexpr int kBO = kWO + W;           // b_o
+  static constexpr int kShared = kBO + 4;
+  static constexpr int kNetW = (kShared + 3) / 4 * 4;  // one network's tables; u- then u+
   // warp-private region
   static constexpr int kX = 0;                  // [4][32] job coordinates (x, y, z, unused)
   static constexpr int kA = kX + 4 * 32;        // [32][kRS]
@@ -60,16 +62,17 @@ struct Layout {
   static constexpr int kStage = kAv + 32;       // [2][160] inputs of the current and the next tile
   static constexpr int kStageFloats = 160;
   static constexpr int kWarpFloats = kStage + 2 * kStageFloats;
-  static constexpr int kWarp0 = (kShared + 3) / 4 * 4;
+  static constexpr int kWarp0 = 2 * kNetW;
 };
 
 // the CTA-level parts of the layout, for NW warps per CTA
 template <class N, int NW>
 struct CtaLayout {
   using Lay = Layout<N>;
-  static constexpr int kAcc = Lay::kWarp0 + NW * Lay::kWarpFloats;  // [kParams] CTA gradient accumulator
-  static constexpr int kLoss = (kAcc + N::kParams + 3) / 4 * 4;     // [NW] doubles
-  static constexpr size_t kBytes = sizeof(float) * (size_t)kLoss + sizeof(double) * NW;
+  static constexpr int kAccStride = (N::kParams + 3) / 4 * 4;
+  static constexpr int kAcc = Lay::kWarp0 + NW * Lay::kWarpFloats;  // [2][kParams] CTA gradient accumulators
+  static constexpr int kLoss = kAcc + 2 * kAccStride;                 // [NW][2] doubles
+  static constexpr size_t kBytes = sizeof(float) * (size_t)kLoss + sizeof(double) * 2 * NW;
 };
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
@@ -234,7 +237,7 @@ struct Acc {
 // One tile: forward of the 32 jobs whose coordinates are in X, then (with BWD) the backward
 // with dL/du from G.  EPI(u[4]) runs between the two: it receives this lane's 4 network
 // values (jobs jc..jc+3) and must leave G filled for the warp (it may synchronise the warp).
-template <class N, int OFF, bool BWD, class Epi>
+template <class N, bool BWD, class Epi>
 __device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc& acc, int lane, Epi epi) {
   using Lay = Layout<N>;
   const int jbl = lane & 7, ob = lane >> 3, jc = 4 * jbl, bc = 8 * ob;
@@ -262,7 +265,7 @@ __device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc& acc, i
   // output layer, reduced over the 4 feature blocks
   const float4 wo0 = ld4(sm + Lay::kWO + bc), wo1 = ld4(sm + Lay::kWO + bc + 4);
   const float wo[8] = {wo0.x, wo0.y, wo0.z, wo0.w, wo1.x, wo1.y, wo1.z, wo1.w};
-  const float bo = c_w[OFF + N::kOut + 32];
+  const float bo = sm[Lay::kBO];
   float u[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
@@ -338,23 +341,28 @@ __device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc& acc, i
   __syncwarp();  // the next tile overwrites X, G and both buffers
 }
 
-// Copy network N's weights (flat layout at params + OFF) into the CTA's permuted tables.
-template <class N, int OFF>
-__device__ __forceinline__ void load_weights(float* sm) {
+// Copy network N's weights (flat layout at params + OFF, global memory) into the CTA's permuted
+// tables.  Global rather than constant-bank loads: the permuted reads differ across a warp,
+// which the constant cache would serialise.
+template <class N>
+__device__ __forceinline__ void load_weights(float* sm, const float* __restrict__ params, int OFF) {
   using Lay = Layout<N>;
   const float c = kTanhScale;
+  const float* pw = params + OFF;
   for (int e = threadIdx.x; e < 2 * 32 * 32; e += blockDim.x) {
     const int l = e >> 10, r = e & 1023, k = r >> 5, col = r & 31, hi = col >> 3, t = col & 7;
-    const int off = OFF + N::layer_off(l + 1);
-    sm[Lay::kWF + e] = c * c_w[off + k * 32 + hi + 4 * t];
-    sm[Lay::kWT + e] = c_w[off + (hi + 4 * t) * 32 + k];
+    const float* wl = pw + (l ? N::layer_off(2) : N::layer_off(1));
+    sm[Lay::kWF + e] = c * __ldg(wl + k * 32 + hi + 4 * t);
+    sm[Lay::kWT + e] = __ldg(wl + (hi + 4 * t) * 32 + k);
   }
   for (int e = threadIdx.x; e < 3 * 32; e += blockDim.x) {
     const int row = e >> 5, col = e & 31, f = (col >> 3) + 4 * (col & 7);
-    sm[Lay::kW1 + e] = c * c_w[OFF + row * 32 + f];
-    sm[Lay::kB + e] = c * c_w[OFF + N::layer_off(row) + (row == 0 ? 3 : 32) * 32 + f];
+    const int boff = row == 0 ? N::layer_off(0) + 3 * 32 : (row == 1 ? N::layer_off(1) : N::layer_off(2)) + 32 * 32;
+    sm[Lay::kW1 + e] = c * __ldg(pw + row * 32 + f);
+    sm[Lay::kB + e] = c * __ldg(pw + boff + f);
   }
-  for (int e = threadIdx.x; e < 32; e += blockDim.x) sm[Lay::kWO + e] = c_w[OFF + N::kOut + (e >> 3) + 4 * (e & 7)];
+  for (int e = threadIdx.x; e < 32; e += blockDim.x) sm[Lay::kWO + e] = __ldg(pw + N::kOut + (e >> 3) + 4 * (e & 7));
+  if (threadIdx.x == 0) sm[Lay::kBO] = __ldg(pw + N::kOut + 32);
 }
 
 // Add a warp's accumulators into the CTA accumulator (flat layout of network N).
@@ -379,21 +387,53 @@ __device__ __forceinline__ void flush_acc(float* cta, const Acc& a, int lane) {
   if (lane == 0) atomicAdd(cta + N::kOut + 32, a.bo);
 }
 
-// One launch per network: bulk tiles (4 points x 7 stencil jobs, residual and loss formed in
-// the warp) and, with BWD, general tiles (32 jobs of the job list).  Writes the loss partial
-// floss[net_p][blockIdx.x] (and zeros the rest of that row of slots), residual_out of the bulk
-// slots, and with BWD the partial gradient row blockIdx.x (columns of this network).
-template <class N, int OFF, bool BWD, int NW>
-__global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile_net(PtsH ph, const int32_t* __restrict__ ids, Workspace w,
-                                                          dips_records_t rec, int net_p, float* __restrict__ residual_out) {
+// Launch modes of the engine.  One launch covers both networks (u- tiles first, then u+).
+enum TileMode {
+  kTrain = 0,           // bulk tiles (forward, residual, loss, backward) and general tiles (backward)
+  kForwardBulk = 1,     // bulk tiles: forward, residual and loss only
+};
+
+// One launch for both networks.  Bulk tiles hold 4 points x 7 stencil jobs (residual and loss
+// formed in the warp); general tiles hold 32 jobs of the job list.  Writes the per-CTA loss
+// partials floss[net][blockIdx.x], residual_out of the bulk slots and, in kTrain, the partial
+// gradient row blockIdx.x (both networks' columns).
+template <class N, int MODE, int NW>
+__global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile(PtsH ph, const int32_t* __restrict__ ids, Workspace w,
+                                                                   dips_records_t rec, int off_p,
+                                                                   float* __restrict__ residual_out) {
   using Lay = Layout<N>;
   using Cta = CtaLayout<N, NW>;
+  constexpr bool BWD = MODE == kTrain;
   extern __shared__ float4 smem4[];
   float* sm = reinterpret_cast<float*>(smem4);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  load_weights<N, OFF>(sm);
+  load_weights<N>(sm, w.params, 0);
+  load_weights<N>(sm + Lay::kNetW, w.params, off_p);
   if (BWD)
-    for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) sm[Cta::kAcc + i] = 0.0f;
+    for (int i = threadIdx.x; i < 2 * Cta::kAccStride; i += blockDim.x) sm[Cta::kAcc + i] = 0.0f;
+  // per network (u- then u+): bulk points, bulk tiles, job range [jb, je) and the first job of
+  // the general tiles (after the jobs the bulk tiles' spare lanes carry); tiles [0, s_tiles[0])
+  // belong to u-, [s_tiles[0], s_tiles[1]) to u+
+  __shared__ int64_t s_net[2][5];
+  __shared__ int64_t s_tiles[2];
+  enum { kNb = 0, kNbt = 1, kJb = 2, kJe = 3, kGf = 4 };
+  if (threadIdx.x == 0) {
+    const Ctl& c = *w.ctl;
+    int64_t t = 0;
+    for (int q = 0; q < 2; ++q) {
+      const int64_t nb = q ? c.nbp : c.nbm, jb = q ? c.jm_pad : 0, je = q ? c.total : c.jm;
+      const int64_t nbt = (nb + 3) / 4;
+      const int64_t rest = je - jb - 4 * nbt;
+      const int64_t ngt = MODE == kForwardBulk || rest <= 0 ? 0 : (rest + 31) / 32;
+      s_net[q][kNb] = nb;
+      s_net[q][kNbt] = nbt;
+      s_net[q][kJb] = jb;
+      s_net[q][kJe] = je;
+      s_net[q][kGf] = jb + (MODE == kTrain ? 4 * nbt : 0);
+      t += nbt + ngt;
+      s_tiles[q] = t;
+    }
+  }
   __syncthreads();
   float* wp = sm + Lay::kWarp0 + warp * Lay::kWarpFloats;
   float* X = wp + Lay::kX;
@@ -401,48 +441,51 @@ __global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile_net(PtsH ph,
   float* U = wp + Lay::kU;
   float* Av = wp + Lay::kAv;
   Acc acc;
+  auto clear = [&]() {
 #pragma unroll
-  for (int r = 0; r < 4; ++r)
+    for (int r = 0; r < 4; ++r)
 #pragma unroll
-    for (int t = 0; t < 8; ++t) acc.w3[r][t] = acc.w2[r][t] = 0.0f;
-  acc.wo = acc.b3 = acc.b2 = acc.b1 = acc.w10 = acc.w11 = acc.w12 = acc.bo = 0.0f;
+      for (int t = 0; t < 8; ++t) acc.w3[r][t] = acc.w2[r][t] = 0.0f;
+    acc.wo = acc.b3 = acc.b2 = acc.b1 = acc.w10 = acc.w11 = acc.w12 = acc.bo = 0.0f;
+  };
+  clear();
 
-  const Ctl ctl = *w.ctl;
-  const int64_t nb = net_p ? ctl.nbp : ctl.nbm;
-  const float* recs = w.brec + (size_t)(net_p ? w.B : 0) * kRecFloats;
-  const int64_t jbeg = net_p ? ctl.jm_pad : 0;
-  const int64_t jend = net_p ? ctl.total : ctl.jm;
-  const int64_t nbt = (nb + 3) / 4;
-  const int64_t nrest = jend - jbeg - 4 * nbt;  // general jobs beyond the bulk tiles' spare lanes
-  const int64_t ngt = BWD && nrest > 0 ? (nrest + 31) / 32 : 0;
+  const int64_t tiles_m = s_tiles[0], tiles = s_tiles[1];
+  const volatile int64_t(*sn)[5] = s_net;  // read per tile, not held in registers
   const float Bf = (float)w.B;
   const int jc = 4 * (lane & 7);
   const bool lead = (lane >> 3) == 0;  // lanes holding u of jobs jc..jc+3 after the reduction
-  double lsum = 0.0;
+  double lsum0 = 0.0, lsum1 = 0.0;
 
   // Stage layout.  Bulk tile: 4 point records [0, 64), spare-lane coordinates [64, 80) and
   // dL/du [80, 84).  General tile: coordinates [0, 128), dL/du [128, 160).
   float* stage0 = wp + Lay::kStage;
   auto issue = [&](int64_t t, float* st) {
-    if (t < nbt) {
-      if (lane < 16) {
-        const int64_t pidx = t * 4 + (lane >> 2);
-        const bool ok = pidx < nb;
-        cp_async16(st + 4 * lane, recs + (ok ? pidx : 0) * kRecFloats + 4 * (lane & 3), ok);
-      } else if (BWD && lane < 20) {
-        const int64_t j = jbeg + 4 * t + (lane - 16);
-        const bool ok = j < jend;
-        cp_async16(st + 64 + 4 * (lane - 16), w.jx + (ok ? j : 0), ok);
-      } else if (BWD && lane < 24) {
-        const int64_t j = jbeg + 4 * t + (lane - 20);
-        const bool ok = j < jend;
-        cp_async4(st + 80 + (lane - 20), w.jg + (ok ? j : 0), ok);
+    if (t < tiles) {
+      const int net = t >= tiles_m ? 1 : 0;
+      const int64_t lt = net ? t - tiles_m : t;
+      const int64_t nb = sn[net][kNb], jb = sn[net][kJb], je = sn[net][kJe], nbt = sn[net][kNbt];
+      if (lt < nbt) {
+        const float* recs = w.brec + (size_t)(net ? w.B : 0) * kRecFloats;
+        if (lane < 16) {
+          const int64_t pidx = lt * 4 + (lane >> 2);
+          const bool ok = pidx < nb;
+          cp_async16(st + 4 * lane, recs + (ok ? pidx : 0) * kRecFloats + 4 * (lane & 3), ok);
+        } else if (BWD && lane < 20) {
+          const int64_t j = jb + 4 * lt + (lane - 16);
+          const bool ok = j < je;
+          cp_async16(st + 64 + 4 * (lane - 16), w.jx + (ok ? j : 0), ok);
+        } else if (BWD && lane < 24) {
+          const int64_t j = jb + 4 * lt + (lane - 20);
+          const bool ok = j < je;
+          cp_async4(st + 80 + (lane - 20), w.jg + (ok ? j : 0), ok);
+        }
+      } else {
+        const int64_t j = sn[net][kGf] + (lt - nbt) * 32 + lane;
+        const bool ok = j < je;
+        cp_async16(st + 4 * lane, w.jx + (ok ? j : 0), ok);
+        if (BWD) cp_async4(st + 128 + lane, w.jg + (ok ? j : 0), ok);
       }
-    } else if (t < nbt + ngt) {
-      const int64_t j = jbeg + 4 * nbt + (t - nbt) * 32 + lane;
-      const bool ok = j < jend;
-      cp_async16(st + 4 * lane, w.jx + (ok ? j : 0), ok);
-      cp_async4(st + 128 + lane, w.jg + (ok ? j : 0), ok);
     }
     cp_commit();
   };
@@ -451,22 +494,35 @@ __global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile_net(PtsH ph,
   int64_t tile = (int64_t)blockIdx.x * NW + warp;
   issue(tile, stage0);
   int sidx = 0;
-  for (; tile < nbt + ngt; tile += stride, sidx ^= 1) {
+  int cur = -1;  // network of the accumulators
+  for (; tile < tiles; tile += stride, sidx ^= 1) {
     issue(tile + stride, stage0 + (sidx ^ 1) * Lay::kStageFloats);
     cp_wait<1>();  // this tile's copies have landed
     __syncwarp();
+    const int net = tile < tiles_m ? 0 : 1;
+    const int64_t lt = net ? tile - tiles_m : tile;
+    const int64_t nb = sn[net][kNb], nbt = sn[net][kNbt];
+    if (BWD && net != cur) {  // tiles come in increasing order: at most one switch, u- to u+
+      if (cur >= 0) {
+        flush_acc<N>(sm + Cta::kAcc + cur * Cta::kAccStride, acc, lane);
+        clear();
+      }
+      cur = net;
+    }
+    const float* wsm = sm + net * Lay::kNetW;
     const float* st = stage0 + sidx * Lay::kStageFloats;
-    if (tile < nbt) {
+    if (lt < nbt) {
       // ---- bulk tile: lane = 7 * point + stencil point; with BWD, lanes 28..31 carry four
       // general jobs (their dL/du is known) instead of idling
       const int pl = lane / kStencil, s = lane - kStencil * pl;
       float x[3] = {0.0f, 0.0f, 0.0f};
       float A = 0.0f;
       if (lane < 4 * kStencil) {
-        if (tile * 4 + pl < nb) {
+        if (lt * 4 + pl < nb) {
           const float* r = st + pl * kRecFloats;
           const float p[3] = {r[kRecP], r[kRecP + 1], r[kRecP + 2]};
-          stencil_point(p, ph.h, s, x);
+          const float hh[3] = {ph.h[0], ph.h[1], ph.h[2]};  // registers, not a local copy of ph
+          stencil_point(p, hh, s, x);
           A = r[kRecA + s];
         }
       } else if (BWD) {
@@ -479,7 +535,7 @@ __global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile_net(PtsH ph,
       // the residual's point records, for lanes 0..3 (point `lane` of the tile)
       int32_t rslot = -1;
       float r_lhs0 = 0.0f, r_diag = 1.0f, r_rod = 0.0f;
-      if (lane < 4 && tile * 4 + lane < nb) {
+      if (lane < 4 && lt * 4 + lane < nb) {
         const float* r = st + lane * kRecFloats;
         rslot = __float_as_int(r[kRecSlot]);
         r_lhs0 = r[kRecLhs0];
@@ -491,7 +547,7 @@ __global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile_net(PtsH ph,
       X[64 + lane] = x[2];
       Av[lane] = A;
       __syncwarp();
-      run_tile<N, OFF, BWD>(sm, wp, acc, lane, [&](const float (&u)[4]) {
+      run_tile<N, BWD>(wsm, wp, acc, lane, [&](const float (&u)[4]) {
         if (lead) st4(U + jc, u[0] * Av[jc], u[1] * Av[jc + 1], u[2] * Av[jc + 2], u[3] * Av[jc + 3]);
         __syncwarp();
         // lanes 0..3: residual of point `lane`; then dL/du of its 7 jobs
@@ -507,7 +563,11 @@ __global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile_net(PtsH ph,
             const float r = Pv * r0;
             if (w.pre_P) w.pre_r0[rslot] = r0;
             gc = isfinite(qv) ? (r / Bf) * Pv / r_diag : 0.0f;
-            lsum += 0.5 * (double)r * (double)r;
+            const double l = 0.5 * (double)r * (double)r;
+            if (net)
+              lsum1 += l;
+            else
+              lsum0 += l;
             if (residual_out) residual_out[rslot] = r;
           }
           if (BWD) {
@@ -517,35 +577,43 @@ __global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile_net(PtsH ph,
         }
       });
     } else {
-      // ---- general tile: 32 jobs of the job list (after those carried by the bulk tiles)
+      // ---- general tile (kTrain only): 32 jobs of the job list, dL/du known from the residual
       X[lane] = st[4 * lane];
       X[32 + lane] = st[4 * lane + 1];
       X[64 + lane] = st[4 * lane + 2];
       G[lane] = st[128 + lane];
       __syncwarp();
-      run_tile<N, OFF, BWD>(sm, wp, acc, lane, [](const float (&)[4]) {});
+      run_tile<N, BWD>(wsm, wp, acc, lane, [](const float (&)[4]) {});
     }
   }
   cp_wait<0>();
-  // loss partial of the CTA
+  // loss partials of the CTA, per network
   double* wl = reinterpret_cast<double*>(sm + Cta::kLoss);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
-  if (lane == 0) wl[warp] = lsum;
-  if (BWD) flush_acc<N>(sm + Cta::kAcc, acc, lane);
+  for (int q = 0; q < 2; ++q) {
+    double v = q ? lsum1 : lsum0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) wl[2 * warp + q] = v;
+  }
+  if (BWD && cur >= 0) flush_acc<N>(sm + Cta::kAcc + cur * Cta::kAccStride, acc, lane);
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 2) {
+    const int q = threadIdx.x;
     double t = 0.0;
-    for (int q = 0; q < NW; ++q) t += wl[q];
-    w.floss[net_p * kLossSlots + blockIdx.x] = t;
+    for (int k = 0; k < NW; ++k) t += wl[2 * k + q];
+    w.floss[q * kLossSlots + blockIdx.x] = t;
     if (blockIdx.x == 0) {
-      w.ctl->floss_n[net_p] = gridDim.x;
-      if (BWD) w.ctl->grad_rows[net_p] = gridDim.x;
+      w.ctl->floss_n[q] = gridDim.x;
+      if (BWD) w.ctl->grad_rows[q] = gridDim.x;
     }
   }
   if (BWD) {
-    float* row = w.partials + (size_t)blockIdx.x * w.n_params + OFF;
-    for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) row[i] = sm[Cta::kAcc + i];
+    float* row = w.partials + (size_t)blockIdx.x * w.n_params;
+    for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) {
+      row[i] = sm[Cta::kAcc + i];
+      row[off_p + i] = sm[Cta::kAcc + Cta::kAccStride + i];
+    }
   }
 }
 

@@ -120,7 +120,8 @@ __global__ void k_count(const int32_t* __restrict__ ids, int64_t B, int64_t n_pt
       const int c = cnt[pid], m = cnt_m[pid];
       if (bulk_ok && c == kStencil && (m == kStencil || m == 0)) {
         kind = m ? 1 : 2;
-        v[m ? 0 : 1] = 1;
+        v[0] = m ? 1 : 0;  // selects, not a run-time index (which would put v in local memory)
+        v[1] = m ? 0 : 1;
       } else {
         kind = 0;
         v[2] = m;
@@ -177,10 +178,10 @@ __global__ void k_scan_blocks(Workspace w) {
 
 __global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, dips_records_t rec, Workspace w) {
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const Ctl ctl = *w.ctl;
-  if (ctl.overflow) return;
+  if (w.ctl->overflow) return;
+  const int64_t jm = w.ctl->jm, jm_pad = w.ctl->jm_pad;
   if (b == 0) {  // padding jobs between the u- and u+ segments
-    for (int64_t j = ctl.jm; j < ctl.jm_pad; ++j) {
+    for (int64_t j = jm; j < jm_pad; ++j) {
       w.jslot[j] = -1;
       w.jcode[j] = job_code(0, kCubeCentre, false);
       w.jA[j] = 0.0f;
@@ -188,9 +189,7 @@ __global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, dips_records_
       w.jg[j] = 0.0f;
     }
   }
-  if (b >= B) return;
-  const int kind = w.bk[b];
-  if (kind == 3) return;
+  const int kind = b < B ? w.bk[b] : 3;
   if (kind == 1 || kind == 2) {
     const int net = kind - 1;
     const int64_t pos = net * B + w.ob[b] + w.blk[4 * blockIdx.x + net];
@@ -214,27 +213,52 @@ __global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, dips_records_
     r4[1] = make_float4(A[0], A[1], A[2], A[3]);
     r4[2] = make_float4(A[4], A[5], A[6], rec.diag[pid]);
     r4[3] = make_float4(rec.rod[pid], __int_as_float((int32_t)b), 0.0f, 0.0f);
-    return;
   }
-  const int64_t pid = batch_pid(ids, b);
-  const int64_t om = w.om[b] + w.blk[4 * blockIdx.x + 2];
-  const int64_t op = w.op[b] + w.blk[4 * blockIdx.x + 3] + ctl.jm_pad;
-  w.om[b] = om;
-  w.op[b] = op;
-  const int cm = w.cm[b], cp = w.cp[b];
-  const int64_t src_m = rec.job_off[pid];
-  const int64_t src_p = rec.job_off[pid + 1] - cp;
-  const float p[3] = {rec.pts[3 * pid], rec.pts[3 * pid + 1], rec.pts[3 * pid + 2]};
-  for (int q = 0; q < cm + cp; ++q) {
-    const int64_t dst = q < cm ? om + q : op + (q - cm);
-    const int64_t src = q < cm ? src_m + q : src_p + (q - cm);
-    const uint16_t code = rec.job_code[src];
-    float x[3];
-    job_coords(p, rec.h, code, x);
-    w.jslot[dst] = (int32_t)b;
-    w.jcode[dst] = code;
-    w.jA[dst] = rec.job_A[src];
-    w.jx[dst] = make_float4(x[0], x[1], x[2], 0.0f);
+  // general points: their u- jobs go to [om, om + cm), their u+ jobs to [op, op + cp); the
+  // source jobs are the first cm and the last cp of [job_off[pid], job_off[pid + 1]) (the
+  // capacity may exceed the count).  A point has up to 7 x 28 jobs, so each warp expands its
+  // general points one at a time with the 32 lanes taking the jobs.
+  const bool gen = kind == 0;
+  int64_t om = 0, op = 0, src = 0, srcp = 0;
+  int cm = 0, n = 0;
+  float p0 = 0.0f, p1 = 0.0f, p2 = 0.0f;
+  if (gen) {
+    const int64_t pid = batch_pid(ids, b);
+    om = w.om[b] + w.blk[4 * blockIdx.x + 2];
+    op = w.op[b] + w.blk[4 * blockIdx.x + 3] + jm_pad;
+    w.om[b] = om;
+    w.op[b] = op;
+    cm = w.cm[b];
+    n = cm + w.cp[b];
+    src = rec.job_off[pid];
+    srcp = rec.job_off[pid + 1] - n;  // job q >= cm comes from srcp + q (the last n - cm slots)
+    p0 = rec.pts[3 * pid];
+    p1 = rec.pts[3 * pid + 1];
+    p2 = rec.pts[3 * pid + 2];
+  }
+  const int lane = threadIdx.x & 31;
+  const float h[3] = {rec.h[0], rec.h[1], rec.h[2]};
+  unsigned todo = __ballot_sync(0xffffffffu, gen);
+  while (todo) {
+    const int l = __ffs(todo) - 1;
+    todo &= todo - 1;
+    const int64_t g_om = __shfl_sync(0xffffffffu, om, l), g_op = __shfl_sync(0xffffffffu, op, l);
+    const int64_t g_src = __shfl_sync(0xffffffffu, src, l), g_srcp = __shfl_sync(0xffffffffu, srcp, l);
+    const int g_cm = __shfl_sync(0xffffffffu, cm, l), g_n = __shfl_sync(0xffffffffu, n, l);
+    const int32_t g_b = (int32_t)__shfl_sync(0xffffffffu, b, l);
+    const float p[3] = {__shfl_sync(0xffffffffu, p0, l), __shfl_sync(0xffffffffu, p1, l),
+                        __shfl_sync(0xffffffffu, p2, l)};
+    for (int q = lane; q < g_n; q += 32) {
+      const int64_t dst = q < g_cm ? g_om + q : g_op + (q - g_cm);
+      const int64_t sq = (q < g_cm ? g_src : g_srcp) + q;
+      const uint16_t code = rec.job_code[sq];
+      float x[3];
+      job_coords(p, h, code, x);
+      w.jslot[dst] = g_b;
+      w.jcode[dst] = code;
+      w.jA[dst] = rec.job_A[sq];
+      w.jx[dst] = make_float4(x[0], x[1], x[2], 0.0f);
+    }
   }
 }
 
@@ -258,36 +282,51 @@ __device__ __forceinline__ double block_sum_d(double v) {
   return t;
 }
 
+// One warp handles its general points one at a time, the 32 lanes splitting the point's jobs
+// (up to 7 x 28): lhs = lhs0 + sum_j A_j u_j, r = P (lhs/diag - rhs/diag), dL/du_j = dL/dlhs A_j.
 __global__ void k_residual(const int32_t* __restrict__ ids, int64_t B, dips_records_t rec, Workspace w,
                            float* __restrict__ residual_out) {
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
   const bool overflow = w.ctl->overflow != 0;
+  const int kind = b < B ? (overflow ? 3 : w.bk[b]) : -1;
   double l = 0.0;
-  if (b < B) {
-    const int kind = overflow ? 3 : w.bk[b];
-    if (kind == 3) {
-      if (residual_out) residual_out[b] = nanf("");
-      l = nan("");
-    } else if (kind == 0) {
-      const int64_t pid = batch_pid(ids, b);
-      float lhs = rec.lhs0[pid];
-      const int64_t om = w.om[b], op = w.op[b];
-      const int cm = w.cm[b], cp = w.cp[b];
-      for (int q = 0; q < cm; ++q) lhs = fmaf(w.jA[om + q], w.ju[om + q], lhs);
-      for (int q = 0; q < cp; ++q) lhs = fmaf(w.jA[op + q], w.ju[op + q], lhs);
-      const float diag = rec.diag[pid];
-      const float qv = lhs / diag;
-      const float r0 = nan_to_num(qv) - rec.rod[pid];
-      // the learned preconditioner scales both lhs/diag and rhs/diag (discretization.py:419-420)
-      const float Pv = w.pre_P ? w.pre_P[b] : 1.0f;
-      const float r = Pv * r0;
-      if (w.pre_P) w.pre_r0[b] = r0;
-      // d(mean 0.5 r^2)/d lhs; nan_to_num has zero derivative where lhs/diag is not finite
-      const float gs = isfinite(qv) ? (r / (float)B) * Pv / diag : 0.0f;
-      w.gs[b] = gs;
-      for (int q = 0; q < cm; ++q) w.jg[om + q] = gs * w.jA[om + q];
-      for (int q = 0; q < cp; ++q) w.jg[op + q] = gs * w.jA[op + q];
-      if (residual_out) residual_out[b] = r;
+  if (kind == 3) {
+    if (residual_out) residual_out[b] = nanf("");
+    l = nan("");
+  }
+  unsigned todo = __ballot_sync(0xffffffffu, kind == 0);
+  while (todo) {
+    const int owner = __ffs(todo) - 1;
+    todo &= todo - 1;
+    const int64_t gb = __shfl_sync(0xffffffffu, b, owner);
+    const int64_t om = w.om[gb], op = w.op[gb];
+    const int cm = w.cm[gb], n = cm + w.cp[gb];
+    float part = 0.0f;
+    for (int q = lane; q < n; q += 32) {
+      const int64_t j = q < cm ? om + q : op + (q - cm);
+      part = fmaf(w.jA[j], w.ju[j], part);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    const int64_t pid = batch_pid(ids, gb);
+    const float lhs = rec.lhs0[pid] + part;
+    const float diag = rec.diag[pid];
+    const float qv = lhs / diag;
+    const float r0 = nan_to_num(qv) - rec.rod[pid];
+    // the learned preconditioner scales both lhs/diag and rhs/diag (discretization.py:419-420)
+    const float Pv = w.pre_P ? w.pre_P[gb] : 1.0f;
+    const float r = Pv * r0;
+    // d(mean 0.5 r^2)/d lhs; nan_to_num has zero derivative where lhs/diag is not finite
+    const float gs = isfinite(qv) ? (r / (float)B) * Pv / diag : 0.0f;
+    for (int q = lane; q < n; q += 32) {
+      const int64_t j = q < cm ? om + q : op + (q - cm);
+      w.jg[j] = gs * w.jA[j];
+    }
+    if (lane == owner) {
+      w.gs[gb] = gs;
+      if (w.pre_P) w.pre_r0[gb] = r0;
+      if (residual_out) residual_out[gb] = r;
       l = 0.5 * (double)r * (double)r;
     }
   }
@@ -319,6 +358,63 @@ __global__ void k_grad_reduce(Workspace w, int P, int Pm, int Psol, float* __res
   float v = 0.0f;
   for (int64_t c = 0; c < rows; ++c) v += w.partials[(size_t)c * P + i];
   grad_out[i] = w.ctl->engine_error ? nanf("") : v;
+}
+
+// d loss / d theta along a direction theta in coefficient space, the networks held fixed: with
+// trec holding d lhs0, d diag, d rod and d A of the records (dips_geometry_assemble_tangent),
+//   d r = (d lhs0 + sum_j dA_j u_j) / diag - (lhs / diag) d diag / diag - d rod
+// (the first two terms vanish where lhs / diag is not finite, as nan_to_num's derivative does),
+// d loss = sum_b (r_b / B) d r_b.  Every batch point is general here (the expansion ran with
+// bulk points off), so ju holds u of all its jobs.  One warp per point at a time, the lanes
+// splitting its jobs as in k_residual.
+__global__ void k_coeff_dot(const int32_t* __restrict__ ids, int64_t B, dips_records_t rec, dips_records_t trec,
+                            Workspace w) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool overflow = w.ctl->overflow != 0;
+  const int kind = b < B ? (overflow ? 3 : w.bk[b]) : -1;
+  double l = kind == 3 ? nan("") : 0.0;
+  unsigned todo = __ballot_sync(0xffffffffu, kind == 0);
+  while (todo) {
+    const int owner = __ffs(todo) - 1;
+    todo &= todo - 1;
+    const int64_t gb = __shfl_sync(0xffffffffu, b, owner);
+    const int64_t om = w.om[gb], op = w.op[gb];
+    const int cm = w.cm[gb], n = cm + w.cp[gb];
+    const int64_t pid = batch_pid(ids, gb);
+    const int64_t srcm = rec.job_off[pid], srcp = rec.job_off[pid + 1] - n;
+    float part = 0.0f, tpart = 0.0f;
+    for (int q = lane; q < n; q += 32) {
+      const int64_t j = q < cm ? om + q : op + (q - cm);
+      const int64_t src = (q < cm ? srcm : srcp) + q;
+      const float u = w.ju[j];
+      part = fmaf(w.jA[j], u, part);
+      tpart = fmaf(trec.job_A[src], u, tpart);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      part += __shfl_xor_sync(0xffffffffu, part, o);
+      tpart += __shfl_xor_sync(0xffffffffu, tpart, o);
+    }
+    if (lane == owner) {
+      const float lhs = rec.lhs0[pid] + part;
+      const float diag = rec.diag[pid];
+      const float qv = lhs / diag;
+      const float r = nan_to_num(qv) - rec.rod[pid];
+      double dr = -(double)trec.rod[pid];
+      if (isfinite(qv)) dr += ((double)trec.lhs0[pid] + tpart - (double)qv * trec.diag[pid]) / diag;
+      l = (double)r / (double)B * dr;
+    }
+  }
+  const double t = block_sum_d(l);
+  if (threadIdx.x == 0) w.lossp[blockIdx.x] = t;
+}
+
+__global__ void k_coeff_final(Workspace w, double* __restrict__ out) {
+  double v = 0.0;
+  for (int64_t i = threadIdx.x; i < w.nres; i += blockDim.x) v += w.lossp[i];
+  const double t = block_sum_d(v);
+  if (threadIdx.x == 0) *out = t;
 }
 
 __global__ void k_adam(dips_adam_t hp, int P, float* __restrict__ params, const float* __restrict__ grad,
@@ -479,7 +575,7 @@ static PtsH make_ph(const dips_records_t* rec) {
   return ph;
 }
 
-static int prep_ws(const dips_arch_t* arch, int64_t B, void* ws, size_t ws_bytes, Workspace* W) {
+static int prep_ws(const dips_arch_t* arch, const float* params, int64_t B, void* ws, size_t ws_bytes, Workspace* W) {
   const int P = arch_params(arch);
   DIPS_REQUIRE(P > 0, DIPS_E_ARG, "invalid arch");
   DIPS_REQUIRE(ws != nullptr, DIPS_E_ARG, "null workspace");
@@ -498,6 +594,7 @@ static int prep_ws(const dips_arch_t* arch, int64_t B, void* ws, size_t ws_bytes
       hi = mid;
   }
   carve(W, base, B, lo, P, pre_n);
+  W->params = params;
   return DIPS_OK;
 }
 
@@ -577,7 +674,7 @@ extern "C" int dips_residual_fwd(const dips_arch_t* arch, const float* params, c
   const ArchOps* ops = find_arch(arch);
   if (!ops) return DIPS_E_UNSUPPORTED;
   Workspace W;
-  st = prep_ws(arch, batch, workspace, ws_bytes, &W);
+  st = prep_ws(arch, params, batch, workspace, ws_bytes, &W);
   if (st) return st;
   st = ops->load_params(params, stream);
   if (st) return st;
@@ -593,7 +690,7 @@ extern "C" int dips_residual_bwd(const dips_arch_t* arch, const float* params, c
   const ArchOps* ops = find_arch(arch);
   if (!ops) return DIPS_E_UNSUPPORTED;
   Workspace W;
-  st = prep_ws(arch, batch, workspace, ws_bytes, &W);
+  st = prep_ws(arch, params, batch, workspace, ws_bytes, &W);
   if (st) return st;
   st = ops->load_params(params, stream);
   if (st) return st;
@@ -601,6 +698,33 @@ extern "C" int dips_residual_bwd(const dips_arch_t* arch, const float* params, c
   st = ops->bulk_fused(make_ph(rec), batch_ids, W, *rec, nullptr, true, nullptr, stream);
   if (st) return st;
   return run_backward(ops, arch, params, rec, batch_ids, batch, W, grad_out, nullptr, stream);
+}
+
+extern "C" int dips_loss_coeff_tangent(const dips_arch_t* arch, const float* params, const dips_records_t* rec,
+                                       const dips_records_t* trec, const int32_t* batch_ids, int64_t batch,
+                                       void* workspace, size_t ws_bytes, double* dloss_out, cudaStream_t stream) {
+  int st = check_rec(rec, batch);
+  if (st) return st;
+  DIPS_REQUIRE(arch && params && dloss_out && trec, DIPS_E_ARG, "null arch, params, trec or dloss_out");
+  DIPS_REQUIRE(trec->lhs0 && trec->diag && trec->rod && trec->job_A, DIPS_E_ARG, "null tangent record array");
+  DIPS_REQUIRE(arch->pre_layers == 0, DIPS_E_UNSUPPORTED,
+               "dips_loss_coeff_tangent: the learned preconditioner's dependence on the coefficients is not "
+               "differentiated");
+  const ArchOps* ops = find_arch(arch);
+  if (!ops) return DIPS_E_UNSUPPORTED;
+  Workspace W;
+  st = prep_ws(arch, params, batch, workspace, ws_bytes, &W);
+  if (st) return st;
+  st = ops->load_params(params, stream);
+  if (st) return st;
+  st = expand(rec, batch_ids, batch, W, 0, nullptr, stream);  // every point general: u of all jobs
+  if (st) return st;
+  st = ops->job_forward(make_ph(rec), batch_ids, W, nullptr, stream);
+  if (st) return st;
+  k_coeff_dot<<<(int)W.nres, 256, 0, stream>>>(batch_ids, batch, *rec, *trec, W);
+  k_coeff_final<<<1, 256, 0, stream>>>(W, dloss_out);
+  DIPS_CHECK_LAUNCH("dips_loss_coeff_tangent");
+  return DIPS_OK;
 }
 
 extern "C" int dips_adam_step(const dips_arch_t* arch, const dips_adam_t* hp, float* params, const float* grad,
@@ -622,7 +746,7 @@ static int train_step(const dips_arch_t* arch, const dips_adam_t* hp, float* par
   const ArchOps* ops = find_arch(arch);
   if (!ops) return DIPS_E_UNSUPPORTED;
   Workspace W;
-  st = prep_ws(arch, batch, workspace, ws_bytes, &W);
+  st = prep_ws(arch, params, batch, workspace, ws_bytes, &W);
   if (st) return st;
   st = ops->load_params(params, stream);
   if (st) return st;
@@ -665,7 +789,7 @@ extern "C" int dips_autotune(const dips_arch_t* arch, const float* params, const
   const ArchOps* ops = find_arch(arch);
   if (!ops) return DIPS_E_UNSUPPORTED;
   Workspace W;
-  st = prep_ws(arch, batch, workspace, ws_bytes, &W);
+  st = prep_ws(arch, params, batch, workspace, ws_bytes, &W);
   if (st) return st;
   st = ops->load_params(params, stream);
   if (st) return st;

@@ -512,7 +512,71 @@ static int load_params(const float* params, cudaStream_t s) {
   return e == cudaSuccess ? DIPS_OK : cuda_status(e, "cudaMemcpyToSymbolAsync(params)");
 }
 
+template <class N>
+constexpr bool uses_tile() {
+  return N::kW == 32 && N::kL == 3;
+}
+// both networks on the register-blocked tile engine, one launch per phase
+constexpr bool kTileArch = uses_tile<typename A::M>() && uses_tile<typename A::P>();
+
+// CTA width of the tile engine per device (one CTA per SM): 12 warps (default), 10 or 8,
+// chosen by dips_autotune
+constexpr int kMaxDevices = 64;
+static std::atomic<int> g_tile_nw[kMaxDevices];
+static std::mutex g_tune_mu;
+
+static int current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return -1;
+  return dev;
+}
+
+static int tile_nw() {
+  const int dev = current_device();
+  const int v = dev < 0 ? 0 : g_tile_nw[dev].load(std::memory_order_relaxed);
+  return v ? v : tile::kWarpsPerSm;
+}
+
+template <class N, int MODE, int NW>
+static int tile_launch_nw(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
+                          float* residual_out, cudaStream_t s) {
+  static_assert(N::kParams == A::P::kParams, "tile engine: both networks of one shape");
+  constexpr size_t bytes = tile::CtaLayout<N, NW>::kBytes;
+  static_assert(bytes <= 227 * 1024, "tile engine: shared memory");
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(tile::k_tile<N, MODE, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)bytes);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(tile engine smem)");
+    attr_done = true;
+  }
+  tile::k_tile<N, MODE, NW><<<kTileGrid, 32 * NW, bytes, s>>>(ph, ids, w, rec, A::kOffP, residual_out);
+  return DIPS_OK;
+}
+
+// (TILE is a template parameter so that the engine is instantiated for tile archs only)
+template <int MODE, bool TILE = kTileArch>
+static int tile_launch(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
+                       float* residual_out, cudaStream_t s) {
+  if constexpr (TILE) {
+    using N = typename A::M;
+    switch (tile_nw()) {
+      case 10:
+        return tile_launch_nw<N, MODE, 10>(ph, ids, w, rec, residual_out, s);
+      case 8:
+        return tile_launch_nw<N, MODE, 8>(ph, ids, w, rec, residual_out, s);
+      default:
+        return tile_launch_nw<N, MODE, 12>(ph, ids, w, rec, residual_out, s);
+    }
+  } else {
+    ::dips::set_error("tile engine: network shape without the engine");
+    return DIPS_E_UNSUPPORTED;
+  }
+}
+
 static int job_forward(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s) {
+  // one thread per job with the weights as constant-bank operands: for the few general jobs of
+  // a batch this has more parallelism than the tile engine's 32-job tiles
   k_job_forward<typename A::M, 0><<<152 * 24, 256, 0, s>>>(ph, ids, w, 0);
   mark(mk, kMarkFwdM, s);
   k_job_forward<typename A::P, A::kOffP><<<152 * 24, 256, 0, s>>>(ph, ids, w, 1);
@@ -535,88 +599,42 @@ static int adjoint_launch(const PtsH& ph, const int32_t* ids, const Workspace& w
   return DIPS_OK;
 }
 
-template <class N>
-constexpr bool uses_tile() {
-  return N::kW == 32 && N::kL == 3;
-}
-
 static int job_adjoint(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s) {
-  // networks on the register-blocked engine had their general jobs done by the bulk launch
+  // on the tile engine the general jobs' backward is part of the bulk launch
   int st = DIPS_OK;
-  if constexpr (!uses_tile<typename A::M>()) st = adjoint_launch<typename A::M, 0>(ph, ids, w, 0, s);
+  if constexpr (!kTileArch) st = adjoint_launch<typename A::M, 0>(ph, ids, w, 0, s);
   if (st) return st;
   mark(mk, kMarkAdjM, s);
-  if constexpr (!uses_tile<typename A::P>()) st = adjoint_launch<typename A::P, A::kOffP>(ph, ids, w, 1, s);
+  if constexpr (!kTileArch) st = adjoint_launch<typename A::P, A::kOffP>(ph, ids, w, 1, s);
   if (st) return st;
   mark(mk, kMarkAdjP, s);
   DIPS_CHECK_LAUNCH("job adjoint");
   return DIPS_OK;
 }
 
-// CTA shape of the tile engine per device: 12 warps x 1 CTA (default), 6 x 2 or 4 x 3 per SM,
-// chosen by dips_autotune
-constexpr int kMaxDevices = 64;
-static std::atomic<int> g_tile_nw[kMaxDevices];
-static std::mutex g_tune_mu;
-
-static int current_device() {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return -1;
-  return dev;
-}
-
-static int tile_nw() {
-  const int dev = current_device();
-  const int v = dev < 0 ? 0 : g_tile_nw[dev].load(std::memory_order_relaxed);
-  return v ? v : tile::kWarpsPerSm;
-}
-
-template <class N, int OFF, bool BWD, int NW>
-static int tile_launch(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
-                       float* residual_out, int net_p, cudaStream_t s) {
-  constexpr size_t bytes = tile::CtaLayout<N, NW>::kBytes;
-  static bool attr_done = false;
-  if (!attr_done) {
-    cudaError_t e = cudaFuncSetAttribute(tile::k_tile_net<N, OFF, BWD, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)bytes);
-    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(tile engine smem)");
-    attr_done = true;
-  }
-  tile::k_tile_net<N, OFF, BWD, NW><<<kTileGrid * (tile::kWarpsPerSm / NW), 32 * NW, bytes, s>>>(ph, ids, w, rec, net_p,
-                                                                                                 residual_out);
-  return DIPS_OK;
-}
-
 template <class N, int OFF, bool BWD>
 static int fused_launch(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
                         float* residual_out, int net_p, cudaStream_t s) {
-  if constexpr (uses_tile<N>()) {
-    switch (tile_nw()) {
-      case 6:
-        return tile_launch<N, OFF, BWD, 6>(ph, ids, w, rec, residual_out, net_p, s);
-      case 4:
-        return tile_launch<N, OFF, BWD, 4>(ph, ids, w, rec, residual_out, net_p, s);
-      default:
-        return tile_launch<N, OFF, BWD, 12>(ph, ids, w, rec, residual_out, net_p, s);
-    }
-  } else {
-    constexpr size_t bytes = fused_smem_bytes<N>();
-    static bool attr_done = false;
-    if (!attr_done) {
-      cudaError_t e = cudaFuncSetAttribute(k_bulk_fused<N, OFF, A::kParams, BWD>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-      if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(fused smem)");
-      attr_done = true;
-    }
-    k_bulk_fused<N, OFF, A::kParams, BWD><<<w.fgrid, kFusedThreads, bytes, s>>>(ph, ids, w, rec, net_p, residual_out);
+  constexpr size_t bytes = fused_smem_bytes<N>();
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(k_bulk_fused<N, OFF, A::kParams, BWD>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(fused smem)");
+    attr_done = true;
   }
+  k_bulk_fused<N, OFF, A::kParams, BWD><<<w.fgrid, kFusedThreads, bytes, s>>>(ph, ids, w, rec, net_p, residual_out);
   return DIPS_OK;
 }
 
 static int bulk_fused(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
                       float* residual_out, bool bwd, const Marks* mk, cudaStream_t s) {
   int st;
-  if (bwd) {
+  if constexpr (kTileArch) {
+    mark(mk, kMarkFusedM, s);
+    st = bwd ? tile_launch<tile::kTrain>(ph, ids, w, rec, residual_out, s)
+             : tile_launch<tile::kForwardBulk>(ph, ids, w, rec, residual_out, s);
+  } else if (bwd) {
     st = fused_launch<typename A::M, 0, true>(ph, ids, w, rec, residual_out, 0, s);
     if (!st) mark(mk, kMarkFusedM, s);
     if (!st) st = fused_launch<typename A::P, A::kOffP, true>(ph, ids, w, rec, residual_out, 1, s);
@@ -641,13 +659,13 @@ static int mlp_eval(const float* pts, const float* phi, int64_t n, float* u, flo
 }
 
 
-// Times the backward launches of both networks under each CTA shape (one warm-up, then three
+// Times the training launch of the tile engine under each CTA width (one warm-up, then three
 // timed repetitions on the caller's stream, which is synchronised) and keeps the fastest for
 // the current device.
 static int autotune(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec, cudaStream_t s,
                     int* chosen) {
   *chosen = 0;
-  if constexpr (!uses_tile<typename A::M>() && !uses_tile<typename A::P>()) {
+  if constexpr (!kTileArch) {
     return DIPS_OK;
   } else {
     const int dev = current_device();
@@ -656,7 +674,7 @@ static int autotune(const PtsH& ph, const int32_t* ids, const Workspace& w, cons
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
       return cuda_status(cudaGetLastError(), "autotune: cudaEventCreate");
-    const int cand[3] = {12, 6, 4};
+    const int cand[3] = {12, 10, 8};
     float best = 3.4e38f;
     int best_nw = tile::kWarpsPerSm;
     int st = DIPS_OK;

@@ -58,6 +58,7 @@ struct Workspace {
   float* pre_partials;  // [kPreGrid][pre_n] partial gradient rows of the preconditioner
   float* partials;   // [grid + fgrid][P] partial gradient rows (count per network in Ctl::grad_rows)
   float* grad;       // [P]
+  const float* params;  // the call's parameters (device): u- net, u+ net, preconditioner
   int64_t nblk, nres, jcap, B;
   int grid, fgrid;
   int n_params;      // row stride of partials

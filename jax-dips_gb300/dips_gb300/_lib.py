@@ -207,6 +207,17 @@ _SIGS = {
         + [c_void_p] * 9
         + [c_void_p],
     ),
+    "dips_geometry_assemble_tangent": (
+        c_i32,
+        [P(LevelSetT), c_void_p, c_i64, P(c_f32), c_void_p, c_void_p, c_void_p, c_void_p, P(CoeffsT), P(CoeffsT)]
+        + [c_void_p] * 4
+        + [c_void_p],
+    ),
+    "dips_loss_coeff_tangent": (
+        c_i32,
+        [P(ArchT), c_void_p, P(RecordsT), P(RecordsT), c_void_p, c_i64, c_void_p, ctypes.c_size_t, c_void_p,
+         c_void_p],
+    ),
     "dips_num_params": (c_i32, [P(ArchT)]),
     "dips_arch_supported": (c_i32, [P(ArchT)]),
     "dips_step_workspace_bytes": (ctypes.c_size_t, [P(ArchT), c_i64, c_i64]),

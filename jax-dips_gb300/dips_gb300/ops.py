@@ -57,6 +57,22 @@ def residual_backward(arch: Arch, params: torch.Tensor, level: FVLevel, batch_id
     return grad
 
 
+def loss_coefficient_derivative(arch: Arch, params: torch.Tensor, level: FVLevel, tangent, batch_ids=None,
+                                ws: StepWorkspace = None) -> torch.Tensor:
+    """d loss / d theta (device float64 scalar) of the residual_forward loss along the
+    coefficient direction of ``tangent`` (``level.coefficient_tangent({...})``), the params
+    fixed; e.g. the gradient of the total loss with respect to a constant mu+."""
+    lib = _lib.load()
+    B = level.n if batch_ids is None else int(batch_ids.numel())
+    if ws is None or not ws.fits(arch, B, level.max_jobs(B)):
+        ws = StepWorkspace(arch, B, level.max_jobs(B), params.device)
+    out = torch.empty((), dtype=torch.float64, device=params.device)
+    _lib.check(lib.dips_loss_coeff_tangent(arch.ctype(), _lib.ptr(params), level.desc, tangent.desc,
+                                           _ids_ptr(batch_ids), B, _lib.ptr(ws.buf), ws.nbytes, _lib.ptr(out),
+                                           _lib.stream_handle()), "dips_loss_coeff_tangent")
+    return out
+
+
 class ResidualLoss(torch.autograd.Function):
     """loss = mean(0.5 * (lhs/diag - rhs/diag)^2) over a batch, differentiable in params."""
 

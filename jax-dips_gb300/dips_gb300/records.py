@@ -93,6 +93,7 @@ class FVLevel:
             offs[2 * a + 1, a] = hv[a]
         offs = half * offs
         faces = (self.pts[:, None, :] + offs[None]).reshape(-1, 3)
+        self._face_offs = offs
         vals = {}
         vals["mu_m_face"] = eval_callable(fn["mu_m"], faces)
         vals["mu_p_face"] = eval_callable(fn["mu_p"], faces)
@@ -130,6 +131,8 @@ class FVLevel:
         self.flags = flags if keep_geometry else None
         self.n_tri, self.n_xs = (n_tri, n_xs) if keep_geometry else (None, None)
         self._vals = vals if keep_geometry else None
+        # what the coefficient tangent needs: the query points and offsets, the coefficients
+        self._geo = (tri_off, xs_off, tri_pts, xs_pts, xr_pts, co, beta0) if keep_geometry else None
         self.n_jobs = int(self.cnt.sum())
         self.max_cnt = int(self.cnt.max()) if n else 0
         self.desc = _lib.RecordsT(
@@ -137,7 +140,68 @@ class FVLevel:
             P(self.cnt), P(self.cnt_m), P(self.job_off), P(self.job_code), P(self.job_A), P(self.coeff26),
         )
 
+    def coefficient_tangent(self, dfns: dict) -> "TangentRecords":
+        """Derivative of the records along a direction in coefficient space.
+
+        ``dfns`` maps coefficient names (mu_m, mu_p, k_m, k_p, f_m, f_p, g, alpha, beta) to
+        callables r -> the derivative of that coefficient at r along the direction; absent names
+        do not change.  ``{"mu_p": lambda r: 1.0}`` is d/d mu+ of a constant mu+.  Needs a level
+        built with keep_geometry=True."""
+        if self._geo is None:
+            raise ValueError("coefficient_tangent needs FVLevel(..., keep_geometry=True)")
+        unknown = set(dfns) - {"mu_m", "mu_p", "k_m", "k_p", "f_m", "f_p", "g", "alpha", "beta"}
+        if unknown:
+            raise ValueError(f"unknown coefficient names {sorted(unknown)}")
+        lib = _lib.load()
+        tri_off, xs_off, tri_pts, xs_pts, xr_pts, co, _ = self._geo
+        faces = (self.pts[:, None, :] + self._face_offs[None]).reshape(-1, 3)
+        where = {"mu_m_face": ("mu_m", faces), "mu_p_face": ("mu_p", faces), "k_m": ("k_m", self.pts),
+                 "k_p": ("k_p", self.pts), "f_m": ("f_m", self.pts), "f_p": ("f_p", self.pts), "g": ("g", self.pts),
+                 "beta_tri": ("beta", tri_pts), "mu_m_s": ("mu_m", xs_pts), "mu_p_s": ("mu_p", xs_pts),
+                 "alpha_r": ("alpha", xr_pts), "beta_r": ("beta", xr_pts), "mu_m_r": ("mu_m", xr_pts),
+                 "mu_p_r": ("mu_p", xr_pts)}
+        keep = {}
+        ptrs = []
+        for field, _ in _lib.CoeffsT._fields_[:-1]:
+            name, at = where[field]
+            if name in dfns and at.shape[0] > 0:
+                keep[field] = eval_callable(dfns[name], at)
+                ptrs.append(_lib.ptr(keep[field]))
+            else:
+                ptrs.append(None)
+        dco = _lib.CoeffsT(*ptrs, 0.0)
+        t = TangentRecords(self)
+        P = _lib.ptr
+        _lib.check(
+            lib.dips_geometry_assemble_tangent(self.ls.desc, P(self.pts), self.n, self._hc(), P(self.flags),
+                                               P(tri_off), P(xs_off), P(self.job_off), co, dco, P(t.lhs0),
+                                               P(t.diag), P(t.rod), P(t.job_A), _lib.stream_handle()),
+            "dips_geometry_assemble_tangent",
+        )
+        return t
+
+    def _hc(self):
+        return (_lib.c_f32 * 3)(*[float(v) for v in self.h])
+
     def max_jobs(self, batch: int, distinct: bool = True) -> int:
         """Upper bound of the jobs of a batch of ``batch`` points (distinct points: <= all jobs)."""
         bound = batch * self.max_cnt
         return min(bound, self.n_jobs) if distinct else bound
+
+
+class TangentRecords:
+    """d lhs0, d diag, d rod (per point) and d job_A (per job) of a level along a coefficient
+    direction; ``desc`` is the level's record descriptor with these four arrays in place."""
+
+    def __init__(self, level: FVLevel):
+        f32 = dict(dtype=torch.float32, device=level.pts.device)
+        n = level.n
+        self.level = level
+        self.lhs0 = torch.zeros(n, **f32)
+        self.diag = torch.zeros(n, **f32)
+        self.rod = torch.zeros(n, **f32)
+        self.job_A = torch.zeros(level.job_A.numel(), **f32)
+        d = level.desc
+        P = _lib.ptr
+        self.desc = _lib.RecordsT(d.pts, d.n_pts, d.h, P(self.lhs0), P(self.diag), P(self.rod), d.cnt, d.cnt_m,
+                                  d.job_off, d.job_code, P(self.job_A), d.coeff26)

@@ -180,7 +180,7 @@ def test_autotune_choice_and_unchanged_results():
     params = torch.as_tensor(case.params, device="cuda")
     ws = ops.StepWorkspace(a, lvl.n, lvl.max_jobs(lvl.n), "cuda")
     nw = ops.autotune(a, params, lvl, None, ws)
-    assert nw in (4, 6, 12)
+    assert nw in (8, 10, 12)
     lg1, gg1 = case.gpu_loss_grad()
     assert abs(lg1 - lg0) <= 1e-6 * abs(lg0)
     np.testing.assert_allclose(gg1, gg0, rtol=1e-4, atol=1e-6 * np.max(np.abs(gg0)))
