@@ -88,6 +88,9 @@ typedef struct {
   const float* job_A;       /* [jobs] lhs coefficient of the network value at the job point */
   const float* coeff26;     /* [n][26] cell coefficients (geom_pp.py:873-901); read only by the
                                learned preconditioner, may be NULL without it */
+  const float* bulk_rec;    /* [n][16] optional: each bulk point's packed record
+                               (dips_pack_bulk_records), one 64-byte read per point per step;
+                               NULL: gathered from the arrays above every step */
 } dips_records_t;
 
 typedef struct {
@@ -166,6 +169,11 @@ int dips_geometry_assemble_tangent(const dips_levelset_t* ls, const float* pts, 
                                    const uint32_t* flags, const int64_t* tri_off, const int64_t* xs_off,
                                    const int64_t* job_off, const dips_coeffs_t* co, const dips_coeffs_t* dco,
                                    float* d_lhs0, float* d_diag, float* d_rod, float* d_job_A, cudaStream_t stream);
+
+/* Packs the record of every bulk point (7 jobs, all of one network) of `rec` into out [n][16]
+   (float32: point, lhs0, the 7 stencil coefficients, diag, rod); other points' rows are left
+   unwritten.  Pass `out` as rec->bulk_rec afterwards. */
+int dips_pack_bulk_records(const dips_records_t* rec, float* out, cudaStream_t stream);
 
 /* ---- residual, loss, adjoint, optimizer: replace Trainer.loss (trainer.py:892-912),
         value_and_grad in Trainer.update (:783-789) and the optax chain ---------------- */

@@ -391,6 +391,7 @@ __device__ __forceinline__ void flush_acc(float* cta, const Acc& a, int lane) {
 enum TileMode {
   kTrain = 0,           // bulk tiles (forward, residual, loss, backward) and general tiles (backward)
   kForwardBulk = 1,     // bulk tiles: forward, residual and loss only
+  kForwardGeneral = 2,  // general tiles over every job of the job list: u into Workspace::ju
 };
 
 // One launch for both networks.  Bulk tiles hold 4 points x 7 stencil jobs (residual and loss
@@ -422,8 +423,8 @@ __global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile(PtsH ph, con
     int64_t t = 0;
     for (int q = 0; q < 2; ++q) {
       const int64_t nb = q ? c.nbp : c.nbm, jb = q ? c.jm_pad : 0, je = q ? c.total : c.jm;
-      const int64_t nbt = (nb + 3) / 4;
-      const int64_t rest = je - jb - 4 * nbt;
+      const int64_t nbt = MODE == kForwardGeneral ? 0 : (nb + 3) / 4;
+      const int64_t rest = MODE == kForwardGeneral ? je - jb : je - jb - 4 * nbt;
       const int64_t ngt = MODE == kForwardBulk || rest <= 0 ? 0 : (rest + 31) / 32;
       s_net[q][kNb] = nb;
       s_net[q][kNbt] = nbt;
@@ -577,13 +578,21 @@ __global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile(PtsH ph, con
         }
       });
     } else {
-      // ---- general tile (kTrain only): 32 jobs of the job list, dL/du known from the residual
+      // ---- general tile: 32 jobs of the job list; kTrain: dL/du known from the residual;
+      // kForwardGeneral: u of each job to ju
       X[lane] = st[4 * lane];
       X[32 + lane] = st[4 * lane + 1];
       X[64 + lane] = st[4 * lane + 2];
-      G[lane] = st[128 + lane];
+      if (BWD) G[lane] = st[128 + lane];
       __syncwarp();
-      run_tile<N, BWD>(wsm, wp, acc, lane, [](const float (&)[4]) {});
+      const int64_t j0 = sn[net][kGf] + (lt - nbt) * 32 + jc, je = sn[net][kJe];
+      run_tile<N, BWD>(wsm, wp, acc, lane, [&](const float (&u)[4]) {
+        if (MODE == kForwardGeneral && lead) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (j0 + q < je) w.ju[j0 + q] = u[q];
+        }
+      });
     }
   }
   cp_wait<0>();
@@ -598,7 +607,7 @@ __global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile(PtsH ph, con
   }
   if (BWD && cur >= 0) flush_acc<N>(sm + Cta::kAcc + cur * Cta::kAccStride, acc, lane);
   __syncthreads();
-  if (threadIdx.x < 2) {
+  if (MODE != kForwardGeneral && threadIdx.x < 2) {
     const int q = threadIdx.x;
     double t = 0.0;
     for (int k = 0; k < NW; ++k) t += wl[2 * k + q];

@@ -176,6 +176,47 @@ __global__ void k_scan_blocks(Workspace w) {
   }
 }
 
+// Record of bulk point pid (network net): point, lhs0, the coefficient of each of its 7
+// stencil jobs in stencil order, diag, rod (layout kRec*; the slot and padding are zero).
+__device__ __forceinline__ void gather_bulk_record(const dips_records_t& rec, int64_t pid, int net,
+                                                   float (&v)[kRecFloats]) {
+  const int64_t jb = net ? rec.job_off[pid + 1] - kStencil : rec.job_off[pid];
+  float A[kStencil];
+#pragma unroll
+  for (int t = 0; t < kStencil; ++t) A[t] = 0.0f;
+#pragma unroll
+  for (int q = 0; q < kStencil; ++q) {
+    const int sj = job_stencil(rec.job_code[jb + q]);
+    const float a = rec.job_A[jb + q];
+#pragma unroll
+    for (int t = 0; t < kStencil; ++t)
+      if (sj == t) A[t] = a;
+  }
+#pragma unroll
+  for (int k = 0; k < kRecFloats; ++k) v[k] = 0.0f;
+  v[kRecP] = rec.pts[3 * pid];
+  v[kRecP + 1] = rec.pts[3 * pid + 1];
+  v[kRecP + 2] = rec.pts[3 * pid + 2];
+  v[kRecLhs0] = rec.lhs0[pid];
+#pragma unroll
+  for (int t = 0; t < kStencil; ++t) v[kRecA + t] = A[t];
+  v[kRecDiag] = rec.diag[pid];
+  v[kRecRod] = rec.rod[pid];
+}
+
+__global__ void k_pack_bulk(dips_records_t rec, float* __restrict__ out) {
+  for (int64_t pid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pid < rec.n_pts;
+       pid += (int64_t)gridDim.x * blockDim.x) {
+    const int c = rec.cnt[pid], m = rec.cnt_m[pid];
+    if (c != kStencil || (m != kStencil && m != 0)) continue;
+    float v[kRecFloats];
+    gather_bulk_record(rec, pid, m ? 0 : 1, v);
+    float4* o = reinterpret_cast<float4*>(out + pid * kRecFloats);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) o[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+  }
+}
+
 __global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, dips_records_t rec, Workspace w) {
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (w.ctl->overflow) return;
@@ -196,23 +237,22 @@ __global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, dips_records_
     w.bulk[pos] = (int32_t)b;
     // the point's record, so that the tile engine reads one contiguous 64-byte block
     const int64_t pid = batch_pid(ids, b);
-    const int64_t jb = net ? rec.job_off[pid + 1] - kStencil : rec.job_off[pid];
-    float A[kStencil];
-#pragma unroll
-    for (int t = 0; t < kStencil; ++t) A[t] = 0.0f;
-#pragma unroll
-    for (int q = 0; q < kStencil; ++q) {
-      const int sj = job_stencil(rec.job_code[jb + q]);
-      const float a = rec.job_A[jb + q];
-#pragma unroll
-      for (int t = 0; t < kStencil; ++t)
-        if (sj == t) A[t] = a;
-    }
     float4* r4 = reinterpret_cast<float4*>(w.brec + pos * kRecFloats);
-    r4[0] = make_float4(rec.pts[3 * pid], rec.pts[3 * pid + 1], rec.pts[3 * pid + 2], rec.lhs0[pid]);
-    r4[1] = make_float4(A[0], A[1], A[2], A[3]);
-    r4[2] = make_float4(A[4], A[5], A[6], rec.diag[pid]);
-    r4[3] = make_float4(rec.rod[pid], __int_as_float((int32_t)b), 0.0f, 0.0f);
+    if (rec.bulk_rec) {  // packed once per level: one 64-byte read
+      const float4* s4 = reinterpret_cast<const float4*>(rec.bulk_rec + pid * kRecFloats);
+      const float4 a = __ldg(s4), c = __ldg(s4 + 1), d = __ldg(s4 + 2), e = __ldg(s4 + 3);
+      r4[0] = a;
+      r4[1] = c;
+      r4[2] = d;
+      r4[3] = make_float4(e.x, __int_as_float((int32_t)b), 0.0f, 0.0f);
+    } else {
+      float v[kRecFloats];
+      gather_bulk_record(rec, pid, net, v);
+      r4[0] = make_float4(v[0], v[1], v[2], v[3]);
+      r4[1] = make_float4(v[4], v[5], v[6], v[7]);
+      r4[2] = make_float4(v[8], v[9], v[10], v[11]);
+      r4[3] = make_float4(v[12], __int_as_float((int32_t)b), 0.0f, 0.0f);
+    }
   }
   // general points: their u- jobs go to [om, om + cm), their u+ jobs to [op, op + cp); the
   // source jobs are the first cm and the last cp of [job_off[pid], job_off[pid + 1]) (the
@@ -698,6 +738,19 @@ extern "C" int dips_residual_bwd(const dips_arch_t* arch, const float* params, c
   st = ops->bulk_fused(make_ph(rec), batch_ids, W, *rec, nullptr, true, nullptr, stream);
   if (st) return st;
   return run_backward(ops, arch, params, rec, batch_ids, batch, W, grad_out, nullptr, stream);
+}
+
+extern "C" int dips_pack_bulk_records(const dips_records_t* rec, float* out, cudaStream_t stream) {
+  DIPS_REQUIRE(rec && out && rec->pts && rec->lhs0 && rec->diag && rec->rod && rec->cnt && rec->cnt_m &&
+                   rec->job_off && rec->job_code && rec->job_A,
+               DIPS_E_ARG, "dips_pack_bulk_records: null pointer");
+  DIPS_REQUIRE(((uintptr_t)out & 15) == 0, DIPS_E_ARG, "dips_pack_bulk_records: out must be 16-byte aligned");
+  if (rec->n_pts <= 0) return DIPS_OK;
+  int64_t grid = div_up(rec->n_pts, 256);
+  if (grid > 152 * 32) grid = 152 * 32;
+  k_pack_bulk<<<(int)grid, 256, 0, stream>>>(*rec, out);
+  DIPS_CHECK_LAUNCH("dips_pack_bulk_records");
+  return DIPS_OK;
 }
 
 extern "C" int dips_loss_coeff_tangent(const dips_arch_t* arch, const float* params, const dips_records_t* rec,

@@ -575,11 +575,16 @@ static int tile_launch(const PtsH& ph, const int32_t* ids, const Workspace& w, c
 }
 
 static int job_forward(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s) {
-  // one thread per job with the weights as constant-bank operands: for the few general jobs of
-  // a batch this has more parallelism than the tile engine's 32-job tiles
-  k_job_forward<typename A::M, 0><<<152 * 24, 256, 0, s>>>(ph, ids, w, 0);
-  mark(mk, kMarkFwdM, s);
-  k_job_forward<typename A::P, A::kOffP><<<152 * 24, 256, 0, s>>>(ph, ids, w, 1);
+  if constexpr (kTileArch) {  // both networks' general jobs in one tile-engine launch
+    mark(mk, kMarkFwdM, s);
+    const dips_records_t none{};
+    const int st = tile_launch<tile::kForwardGeneral>(ph, ids, w, none, nullptr, s);
+    if (st) return st;
+  } else {  // one thread per job, the weights as constant-bank operands
+    k_job_forward<typename A::M, 0><<<152 * 24, 256, 0, s>>>(ph, ids, w, 0);
+    mark(mk, kMarkFwdM, s);
+    k_job_forward<typename A::P, A::kOffP><<<152 * 24, 256, 0, s>>>(ph, ids, w, 1);
+  }
   mark(mk, kMarkFwdP, s);
   DIPS_CHECK_LAUNCH("job forward");
   return DIPS_OK;

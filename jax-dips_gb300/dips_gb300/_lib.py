@@ -167,6 +167,7 @@ class RecordsT(ctypes.Structure):
         ("job_code", c_void_p),
         ("job_A", c_void_p),
         ("coeff26", c_void_p),
+        ("bulk_rec", c_void_p),
     ]
 
 
@@ -218,6 +219,7 @@ _SIGS = {
         [P(ArchT), c_void_p, P(RecordsT), P(RecordsT), c_void_p, c_i64, c_void_p, ctypes.c_size_t, c_void_p,
          c_void_p],
     ),
+    "dips_pack_bulk_records": (c_i32, [P(RecordsT), c_void_p, c_void_p]),
     "dips_num_params": (c_i32, [P(ArchT)]),
     "dips_arch_supported": (c_i32, [P(ArchT)]),
     "dips_step_workspace_bytes": (ctypes.c_size_t, [P(ArchT), c_i64, c_i64]),

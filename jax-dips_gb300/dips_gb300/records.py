@@ -137,8 +137,13 @@ class FVLevel:
         self.max_cnt = int(self.cnt.max()) if n else 0
         self.desc = _lib.RecordsT(
             P(self.pts), n, (_lib.c_f32 * 3)(*[float(v) for v in self.h]), P(self.lhs0), P(self.diag), P(self.rod),
-            P(self.cnt), P(self.cnt_m), P(self.job_off), P(self.job_code), P(self.job_A), P(self.coeff26),
+            P(self.cnt), P(self.cnt_m), P(self.job_off), P(self.job_code), P(self.job_A), P(self.coeff26), None,
         )
+        # each bulk point's 64-byte record, packed once so that a step reads it in one piece
+        self.bulk_rec = torch.empty(max(n, 1), 16, **f32)
+        if n:
+            _lib.check(lib.dips_pack_bulk_records(self.desc, P(self.bulk_rec), st), "dips_pack_bulk_records")
+        self.desc.bulk_rec = P(self.bulk_rec)
 
     def coefficient_tangent(self, dfns: dict) -> "TangentRecords":
         """Derivative of the records along a direction in coefficient space.
@@ -204,4 +209,4 @@ class TangentRecords:
         d = level.desc
         P = _lib.ptr
         self.desc = _lib.RecordsT(d.pts, d.n_pts, d.h, P(self.lhs0), P(self.diag), P(self.rod), d.cnt, d.cnt_m,
-                                  d.job_off, d.job_code, P(self.job_A), d.coeff26)
+                                  d.job_off, d.job_code, P(self.job_A), d.coeff26, None)

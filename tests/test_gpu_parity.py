@@ -192,6 +192,29 @@ def test_autotune_choice_and_unchanged_results():
     assert ops.autotune(sa, torch.as_tensor(small.params, device="cuda"), slvl, None, sws) == 0
 
 
+@pytest.mark.parametrize("arch", [(3, 32, 3, 32), (2, 16, 2, 16)])
+def test_packed_bulk_records_give_the_gathered_result(arch):
+    """The bulk records packed once per level (dips_pack_bulk_records) and the per-step gather
+    from the record arrays give bit-identical residuals and the same loss."""
+    from dips_gb300 import ops
+
+    case = _parity.build_case("star", n=20, arch=arch, level=1, batch=3000)
+    lvl = case.gpu_level()
+    a = case.gpu_arch()
+    params = torch.as_tensor(case.params, device="cuda")
+    ids = case.gpu_batch_ids()
+    l0, r0, _ = ops.residual_forward(a, params, lvl, ids, want_residual=True)
+    packed = lvl.desc.bulk_rec
+    assert packed
+    try:
+        lvl.desc.bulk_rec = None
+        l1, r1, _ = ops.residual_forward(a, params, lvl, ids, want_residual=True)
+    finally:
+        lvl.desc.bulk_rec = packed
+    assert torch.equal(r0, r1)
+    assert abs(float(l0) - float(l1)) <= 1e-12 * abs(float(l0))
+
+
 @pytest.mark.parametrize(
     "name,n,arch,level,batch",
     [
