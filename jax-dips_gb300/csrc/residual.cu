@@ -61,6 +61,7 @@ static size_t carve(Workspace* w, char* base, int64_t B, int64_t max_jobs, int P
   W.pre_partials = pre_n ? (float*)take(sizeof(float) * (size_t)kPreGrid * pre_n) : nullptr;
   W.partials = (float*)take(sizeof(float) * (size_t)(W.grid + W.fgrid) * P);
   W.grad = (float*)take(sizeof(float) * P);
+  W.sqp = (double*)take(sizeof(double) * ((P + 31) / 32));
   if (w) *w = W;
   return off;
 }
@@ -167,6 +168,7 @@ __global__ void k_scan_blocks(Workspace w) {
     w.ctl->engine_error = 0;
     w.ctl->floss_n[0] = w.ctl->floss_n[1] = 0;
     w.ctl->grad_rows[0] = w.ctl->grad_rows[1] = 0;
+    w.ctl->reduce_done = 0;
     w.ctl->nbm = over ? 0 : carry[0];
     w.ctl->nbp = over ? 0 : carry[1];
     w.ctl->jm = over ? 0 : jm;
@@ -324,6 +326,10 @@ __device__ __forceinline__ double block_sum_d(double v) {
 
 // One warp handles its general points one at a time, the 32 lanes splitting the point's jobs
 // (up to 7 x 28): lhs = lhs0 + sum_j A_j u_j, r = P (lhs/diag - rhs/diag), dL/du_j = dL/dlhs A_j.
+// Each lane first loads its own point's records, so that a point's turn costs one round trip
+// for its jobs.
+constexpr int kMaxJobRounds = (kStencil * kCube + 31) / 32;  // a point's jobs over 32 lanes
+
 __global__ void k_residual(const int32_t* __restrict__ ids, int64_t B, dips_records_t rec, Workspace w,
                            float* __restrict__ residual_out) {
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -335,39 +341,59 @@ __global__ void k_residual(const int32_t* __restrict__ ids, int64_t B, dips_reco
     if (residual_out) residual_out[b] = nanf("");
     l = nan("");
   }
+  int64_t om = 0, op = 0;
+  int cm = 0, n = 0;
+  float lhs0 = 0.0f, diag = 1.0f, rod = 0.0f, Pv = 1.0f;
+  if (kind == 0) {
+    const int64_t pid = batch_pid(ids, b);
+    om = w.om[b];
+    op = w.op[b];
+    cm = w.cm[b];
+    n = cm + w.cp[b];
+    lhs0 = rec.lhs0[pid];
+    diag = rec.diag[pid];
+    rod = rec.rod[pid];
+    // the learned preconditioner scales both lhs/diag and rhs/diag (discretization.py:419-420)
+    if (w.pre_P) Pv = w.pre_P[b];
+  }
   unsigned todo = __ballot_sync(0xffffffffu, kind == 0);
   while (todo) {
     const int owner = __ffs(todo) - 1;
     todo &= todo - 1;
-    const int64_t gb = __shfl_sync(0xffffffffu, b, owner);
-    const int64_t om = w.om[gb], op = w.op[gb];
-    const int cm = w.cm[gb], n = cm + w.cp[gb];
+    const int64_t g_om = __shfl_sync(0xffffffffu, om, owner), g_op = __shfl_sync(0xffffffffu, op, owner);
+    const int g_cm = __shfl_sync(0xffffffffu, cm, owner), g_n = __shfl_sync(0xffffffffu, n, owner);
+    float av[kMaxJobRounds];
     float part = 0.0f;
-    for (int q = lane; q < n; q += 32) {
-      const int64_t j = q < cm ? om + q : op + (q - cm);
-      part = fmaf(w.jA[j], w.ju[j], part);
+#pragma unroll
+    for (int k = 0; k < kMaxJobRounds; ++k) {
+      const int q = lane + 32 * k;
+      av[k] = 0.0f;
+      if (q < g_n) {
+        const int64_t j = q < g_cm ? g_om + q : g_op + (q - g_cm);
+        av[k] = w.jA[j];
+        part = fmaf(av[k], w.ju[j], part);
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    const int64_t pid = batch_pid(ids, gb);
-    const float lhs = rec.lhs0[pid] + part;
-    const float diag = rec.diag[pid];
-    const float qv = lhs / diag;
-    const float r0 = nan_to_num(qv) - rec.rod[pid];
-    // the learned preconditioner scales both lhs/diag and rhs/diag (discretization.py:419-420)
-    const float Pv = w.pre_P ? w.pre_P[gb] : 1.0f;
-    const float r = Pv * r0;
-    // d(mean 0.5 r^2)/d lhs; nan_to_num has zero derivative where lhs/diag is not finite
-    const float gs = isfinite(qv) ? (r / (float)B) * Pv / diag : 0.0f;
-    for (int q = lane; q < n; q += 32) {
-      const int64_t j = q < cm ? om + q : op + (q - cm);
-      w.jg[j] = gs * w.jA[j];
-    }
+    float gs = 0.0f;
     if (lane == owner) {
-      w.gs[gb] = gs;
-      if (w.pre_P) w.pre_r0[gb] = r0;
-      if (residual_out) residual_out[gb] = r;
+      const float lhs = lhs0 + part;
+      const float qv = lhs / diag;
+      const float r0 = nan_to_num(qv) - rod;
+      const float r = Pv * r0;
+      // d(mean 0.5 r^2)/d lhs; nan_to_num has zero derivative where lhs/diag is not finite
+      gs = isfinite(qv) ? (r / (float)B) * Pv / diag : 0.0f;
+      w.gs[b] = gs;
+      if (w.pre_P) w.pre_r0[b] = r0;
+      if (residual_out) residual_out[b] = r;
       l = 0.5 * (double)r * (double)r;
+    }
+    gs = __shfl_sync(0xffffffffu, gs, owner);
+#pragma unroll
+    for (int k = 0; k < kMaxJobRounds; ++k) {
+      const int q = lane + 32 * k;
+      if (q < g_n) w.jg[q < g_cm ? g_om + q : g_op + (q - g_cm)] = gs * av[k];
     }
   }
   const double t = block_sum_d(l);
@@ -457,11 +483,40 @@ __global__ void k_coeff_final(Workspace w, double* __restrict__ out) {
   if (threadIdx.x == 0) *out = t;
 }
 
+// The optax chain (clip_by_global_norm, scale_by_adam, exponential-decay schedule, scale by
+// -1; solvers/optimizers.py:33-54) over P parameters by one block, given the squared gradient
+// norm.  Thread 0 increments the step counter.
+__device__ void adam_update(const dips_adam_t& hp, int P, float gsq, float* __restrict__ params,
+                            const float* __restrict__ grad, float* __restrict__ mu, float* __restrict__ nu,
+                            int64_t* __restrict__ count) {
+  __shared__ int64_t s_count;
+  if (threadIdx.x == 0) s_count = *count;
+  __syncthreads();
+  const float gn = sqrtf(gsq);
+  // clip_by_global_norm: keep g when gnorm < max_norm, else g / gnorm * max_norm
+  const float gnorm = (gn < hp.max_norm) ? -1.0f : gn;
+  const int64_t cnt0 = s_count;
+  const float cnt1 = (float)(cnt0 + 1);
+  const float bc1 = 1.0f - powf(hp.b1, cnt1);
+  const float bc2 = 1.0f - powf(hp.b2, cnt1);
+  const float step = hp.lr * powf(hp.decay_rate, (float)cnt0 / hp.transition_steps);
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    float g = __ldcg(grad + i);  // L2: other blocks of k_reduce_adam wrote it in this launch
+    if (gnorm >= 0.0f) g = (g / gnorm) * hp.max_norm;
+    const float m = (1.0f - hp.b1) * g + hp.b1 * mu[i];
+    const float v = (1.0f - hp.b2) * (g * g) + hp.b2 * nu[i];
+    mu[i] = m;
+    nu[i] = v;
+    const float upd = (m / bc1) / (sqrtf(v / bc2) + hp.eps);
+    params[i] = params[i] + (upd * step) * -1.0f;
+  }
+  if (threadIdx.x == 0) *count = cnt0 + 1;
+}
+
 __global__ void k_adam(dips_adam_t hp, int P, float* __restrict__ params, const float* __restrict__ grad,
                        float* __restrict__ mu, float* __restrict__ nu, int64_t* __restrict__ count) {
   __shared__ float red[32];
-  __shared__ float s_scale;
-  __shared__ int64_t s_count;
+  __shared__ float s_sq;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   float ss = 0.0f;
   for (int i = threadIdx.x; i < P; i += blockDim.x) ss = fmaf(grad[i], grad[i], ss);
@@ -472,29 +527,73 @@ __global__ void k_adam(dips_adam_t hp, int P, float* __restrict__ params, const 
   if (threadIdx.x == 0) {
     float t = 0.0f;
     for (int q = 0; q < nw; ++q) t += red[q];
-    const float gnorm = sqrtf(t);
-    // clip_by_global_norm: keep g when gnorm < max_norm, else g / gnorm * max_norm
-    s_scale = (gnorm < hp.max_norm) ? -1.0f : gnorm;
-    s_count = *count;
+    s_sq = t;
   }
   __syncthreads();
-  const float gnorm = s_scale;
-  const int64_t cnt0 = s_count;
-  const float cnt1 = (float)(cnt0 + 1);
-  const float bc1 = 1.0f - powf(hp.b1, cnt1);
-  const float bc2 = 1.0f - powf(hp.b2, cnt1);
-  const float step = hp.lr * powf(hp.decay_rate, (float)cnt0 / hp.transition_steps);
-  for (int i = threadIdx.x; i < P; i += blockDim.x) {
-    float g = grad[i];
-    if (gnorm >= 0.0f) g = (g / gnorm) * hp.max_norm;
-    const float m = (1.0f - hp.b1) * g + hp.b1 * mu[i];
-    const float v = (1.0f - hp.b2) * (g * g) + hp.b2 * nu[i];
-    mu[i] = m;
-    nu[i] = v;
-    const float upd = (m / bc1) / (sqrtf(v / bc2) + hp.eps);
-    params[i] = params[i] + (upd * step) * -1.0f;
+  adam_update(hp, P, s_sq, params, grad, mu, nu, count);
+}
+
+// The tail of a training step in one launch.  Each block sums 32 gradient columns over the
+// partial rows, the rows split over its 32 warps (a few loads per thread instead of a
+// latency-bound column walk), and adds up the squares of its columns; the last block to finish
+// writes the loss (as k_loss_final) and applies the optax chain to all P parameters.
+__global__ void __launch_bounds__(kReduceThreads) k_reduce_adam(Workspace w, int P, int Pm, int Psol,
+                                                                float* __restrict__ grad, dips_adam_t hp,
+                                                                float* __restrict__ params, float* __restrict__ mu,
+                                                                float* __restrict__ nu, int64_t* __restrict__ count,
+                                                                int64_t B, double* __restrict__ loss_out) {
+  __shared__ float part[32][33];
+  __shared__ bool s_last;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + tx;
+  const bool err = w.ctl->engine_error != 0;
+  float v = 0.0f;
+  if (i < P) {
+    if (i >= Psol) {
+      for (int c = ty; c < kPreGrid; c += 32) v += w.pre_partials[(size_t)c * w.pre_n + (i - Psol)];
+    } else {
+      const int64_t rows = w.ctl->grad_rows[i < Pm ? 0 : 1];
+      for (int64_t c = ty; c < rows; c += 32) v += w.partials[(size_t)c * P + i];
+    }
   }
-  if (threadIdx.x == 0) *count = cnt0 + 1;
+  part[ty][tx] = v;
+  __syncthreads();
+  if (ty == 0) {
+    float t = 0.0f;
+#pragma unroll 8
+    for (int k = 0; k < 32; ++k) t += part[k][tx];
+    if (err) t = nanf("");
+    if (i < P) {
+      grad[i] = t;
+      __threadfence();  // visible to the last block before this block is counted
+    }
+    double sq = i < P ? (double)t * (double)t : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+    if (tx == 0) {
+      w.sqp[blockIdx.x] = sq;
+      __threadfence();
+      const unsigned long long n = atomicAdd(reinterpret_cast<unsigned long long*>(&w.ctl->reduce_done), 1ull);
+      s_last = n == gridDim.x - 1;
+    }
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  // loss of the batch (the FP64 partials of the residual kernels)
+  double l = 0.0;
+  for (int64_t k = threadIdx.x; k < w.nres; k += blockDim.x) l += w.lossp[k];
+  for (int net = 0; net < 2; ++net)
+    for (int64_t k = threadIdx.x; k < w.ctl->floss_n[net]; k += blockDim.x) l += w.floss[net * kLossSlots + k];
+  double g2 = 0.0;
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) g2 += __ldcg(w.sqp + k);
+  const double lt = block_sum_d(l);
+  const double gt = block_sum_d(g2);
+  if (threadIdx.x == 0 && loss_out) *loss_out = err ? nan("") : lt / (double)B;
+  __shared__ float s_g2;
+  if (threadIdx.x == 0) s_g2 = (float)gt;
+  __syncthreads();
+  adam_update(hp, P, s_g2, params, grad, mu, nu, count);
 }
 
 // ----------------------------------------------------------------------------------------
@@ -673,16 +772,24 @@ static int run_forward(const ArchOps* ops, const dips_arch_t* arch, const float*
   return DIPS_OK;
 }
 
-// general adjoint and the reduction of all partial gradient rows
-static int run_backward(const ArchOps* ops, const dips_arch_t* arch, const float* params, const dips_records_t* rec,
-                        const int32_t* ids, int64_t B, Workspace& W, float* grad_out, const Marks* mk,
-                        cudaStream_t s) {
+// general adjoint (shapes without the tile engine) and the preconditioner's backward
+static int run_adjoint(const ArchOps* ops, const dips_arch_t* arch, const float* params, const dips_records_t* rec,
+                       const int32_t* ids, int64_t B, Workspace& W, const Marks* mk, cudaStream_t s) {
   int st = ops->job_adjoint(make_ph(rec), ids, W, mk, s);
   if (st) return st;
   if (W.pre_n) {
     st = precond_backward(*arch, params + ops->n_params, *rec, ids, B, W, s);
     if (st) return st;
   }
+  return DIPS_OK;
+}
+
+// general adjoint and the reduction of all partial gradient rows
+static int run_backward(const ArchOps* ops, const dips_arch_t* arch, const float* params, const dips_records_t* rec,
+                        const int32_t* ids, int64_t B, Workspace& W, float* grad_out, const Marks* mk,
+                        cudaStream_t s) {
+  int st = run_adjoint(ops, arch, params, rec, ids, B, W, mk, s);
+  if (st) return st;
   const int Pm = ops->n_params - net_params(ops->p_layers, ops->p_width);
   const int P = ops->n_params + W.pre_n;
   k_grad_reduce<<<div_up(P, 256), 256, 0, s>>>(W, P, Pm, ops->n_params, grad_out);
@@ -803,13 +910,18 @@ static int train_step(const dips_arch_t* arch, const dips_adam_t* hp, float* par
   if (st) return st;
   st = ops->load_params(params, stream);
   if (st) return st;
-  st = run_forward(ops, arch, params, rec, batch_ids, batch, W, loss_out, nullptr, true, mk, stream);
+  // the loss is written by the step's last kernel (k_reduce_adam), before the update
+  st = run_forward(ops, arch, params, rec, batch_ids, batch, W, nullptr, nullptr, true, mk, stream);
   if (st) return st;
   float* g = grad_out ? grad_out : W.grad;
-  st = run_backward(ops, arch, params, rec, batch_ids, batch, W, g, mk, stream);
+  st = run_adjoint(ops, arch, params, rec, batch_ids, batch, W, mk, stream);
   if (st) return st;
-  k_adam<<<1, 1024, 0, stream>>>(*hp, ops->n_params + W.pre_n, params, g, mu, nu, count);
-  DIPS_CHECK_LAUNCH("dips_train_step adam");
+  const int Pm = ops->n_params - net_params(ops->p_layers, ops->p_width);
+  const int P = ops->n_params + W.pre_n;
+  k_reduce_adam<<<div_up(P, 32), kReduceThreads, 0, stream>>>(W, P, Pm, ops->n_params, g, *hp, params, mu, nu,
+                                                               count, batch, loss_out);
+  DIPS_CHECK_LAUNCH("dips_train_step gradient reduction and adam");
+  mark(mk, kMarkReduce, stream);
   mark(mk, kMarkAdam, stream);
   return DIPS_OK;
 }

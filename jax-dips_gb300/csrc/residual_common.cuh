@@ -17,6 +17,7 @@ constexpr int kPreGrid = 304;    // CTAs of the preconditioner's backward (parti
 constexpr int kPreIn = 26;       // preconditioner input: the cell coefficients
 
 // bulk point record (16 floats): point, lhs0, A of stencil points 0..6, diag, rod, batch slot
+constexpr int kReduceThreads = 1024;  // k_reduce_adam: 32 gradient columns x 32 row groups per block
 constexpr int kRecP = 0, kRecLhs0 = 3, kRecA = 4, kRecDiag = 11, kRecRod = 12, kRecSlot = 13, kRecFloats = 16;
 
 // ----------------------------------------------------------------------------------------
@@ -29,6 +30,7 @@ struct Ctl {
   int64_t engine_error;           // nonzero when a tensor-core wait gave up (the loss and gradient become NaN)
   int64_t floss_n[2];             // per-CTA loss partials written by the point kernels of each network
   int64_t grad_rows[2];           // partial gradient rows written for each network
+  uint64_t reduce_done;           // blocks of k_reduce_adam that have finished their columns
 };
 
 // Step workspace, carved from one caller-owned buffer.  Bulk points go to the fused kernel
@@ -58,6 +60,7 @@ struct Workspace {
   float* pre_partials;  // [kPreGrid][pre_n] partial gradient rows of the preconditioner
   float* partials;   // [grid + fgrid][P] partial gradient rows (count per network in Ctl::grad_rows)
   float* grad;       // [P]
+  double* sqp;       // [ceil(P / 32)] squares of the gradient, per block of k_reduce_adam
   const float* params;  // the call's parameters (device): u- net, u+ net, preconditioner
   int64_t nblk, nres, jcap, B;
   int grid, fgrid;
