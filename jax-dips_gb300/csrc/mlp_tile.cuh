@@ -1,20 +1,21 @@
-// Register-blocked engine for width-32 networks with three hidden layers (DoubleMLP 3x32,
-// nn/mlp/MLP.py:93-139): residual, adjoint and weight gradient of the NBM loss
-// (solvers/poisson/trainer.py:783-789, :892-912) for bulk points and for general jobs.
+// Register-blocked engine for DoubleMLP networks of 3 hidden layers of width 32 or 2 hidden
+// layers of width 16 (nn/mlp/MLP.py:93-139): residual, adjoint and weight gradient of the NBM
+// loss (solvers/poisson/trainer.py:783-789, :892-912) for bulk points and for general jobs.
 //
 // Included by residual_arch.cuh inside the per-shape namespace (after Net, Workspace, the
 // constant bank and act_tanh are defined).
 //
 // Work unit: one warp owns a tile of 32 jobs and runs it through the whole network with
-// __syncwarp only.  Every layer is a [32 jobs x 32] x [32 x 32] product computed as 4x8
-// register blocks: lane = jbl + 8*ob holds jobs 4*jbl..4*jbl+3 and features ob + 4t
-// (t = 0..7).  Activations and deltas sit in two warp-private shared buffers, feature-major
-// ([feature][job], row stride 36 floats, so that the blocked row loads of the weight-gradient
-// product are bank-conflict free).  The weights are copied once per CTA into shared memory,
-// permuted so that a lane's 8 features are contiguous (two float4 loads per k step); the
-// forward copies are pre-scaled by 2*log2(e), the argument scale of the exp2-based tanh.
+// __syncwarp only.  Every layer is a [32 jobs x W] x [W x W] product computed as 4 x NT
+// register blocks (NT = W/4): lane = jbl + 8*ob holds jobs 4*jbl..4*jbl+3 and features
+// ob + 4t (t < NT).  Activations and deltas sit in two warp-private shared buffers,
+// feature-major ([feature][job], row stride 36 floats, so that the blocked row loads of the
+// weight-gradient product are bank-conflict free).  The weights are copied once per CTA into
+// shared memory, permuted so that a lane's NT features are contiguous (NT/4 float4 loads per k
+// step); the forward copies are pre-scaled by 2*log2(e), the argument scale of the exp2 tanh.
 //
-// Per tile: forward (layer 1 from the job coordinates, layers 2 and 3 from the buffers),
+// Per tile (3 x 32; the 2 x 16 form drops the middle layer and needs no recompute):
+// forward (layer 1 from the job coordinates, layers 2 and 3 from the buffers),
 // u = w_o . h3 + b_o, then the loss gradient g of each job, then
 //   delta3 = g w_o (1 - h3^2)              -> buffer A (over h1)
 //   dW3 += h2^T delta3                     (register accumulators)
@@ -22,11 +23,12 @@
 //   h1 recomputed from x                   -> buffer A
 //   dW2 += h1^T delta2
 //   delta1 = (delta2 W2^T) (1 - h1^2);  dW1 += x^T delta1
-// The 32x32 weight gradients stay in registers for all tiles a warp processes (64 per lane);
-// bias, input-layer and output-layer gradients are reduce-scattered over the 8 lanes that share
-// a feature block and kept as one register each.  At the end the CTA adds its warps'
-// accumulators into shared memory and writes one partial gradient row.  12 warps share an SM
-// (168 registers each) as one CTA of 12, two of 6 or three of 4; dips_autotune picks the shape.
+// The W x W weight gradients stay in registers for all tiles a warp processes (W*W/32 per lane
+// and layer); bias, input-layer and output-layer gradients are reduce-scattered over the 8
+// lanes that share a feature block and kept as one register each.  At the end the CTA adds its
+// warps' accumulators into shared memory and writes one partial gradient row.  3 x 32: 12 warps
+// per SM (168 registers), one CTA of 12, 10 or 8 warps; 2 x 16: 24 warps per SM as 2, 3 or 4
+// CTAs; dips_autotune picks the CTA width.
 //
 // Tiles: bulk tiles hold 4 bulk points x 7 stencil points (lanes 0..27; lane = 7*point +
 // stencil), whose residual is formed inside the warp from the 7 network values, plus (in the
@@ -35,27 +37,37 @@
 
 namespace tile {
 
-constexpr int kWarpsPerSm = 12;  // 168 registers per thread; one CTA per SM of 12 (default), 10 or 8 warps
+template <class N>
+constexpr bool supported() {
+  return (N::kW == 32 && N::kL == 3) || (N::kW == 16 && N::kL == 2);
+}
+// warps per SM: the register budget of one thread (168 for 3 x 32, 85 for 2 x 16)
+template <class N>
+constexpr int warps_per_sm() {
+  return N::kW == 32 ? 12 : 24;
+}
 constexpr int kRS = 36;  // buffer row stride (floats)
 constexpr float kTanhScale = 2.8853900817779268f;  // 2 log2(e): tanh(z) = 1 - 2/(1 + 2^(kTanhScale z))
 
 template <class N>
 struct Layout {
-  static_assert(N::kW == 32 && N::kL == 3, "tile engine: 3 hidden layers of width 32");
-  static constexpr int W = 32;
+  static_assert(supported<N>(), "tile engine: 3 hidden layers of width 32 or 2 of width 16");
+  static constexpr int W = N::kW, L = N::kL;
+  static constexpr int NT = W / 4;  // features per lane in a register block
+  static constexpr int R = W / 8;   // weight-gradient rows per lane
   // CTA-shared, permuted weights (floats)
-  static constexpr int kWF = 0;                 // [2][k = in 32][8*ob + t] = c * W_l[k][ob + 4t]
-  static constexpr int kWT = kWF + 2 * W * W;   // [2][k = out 32][8*ib + t] = W_l[ib + 4t][k]
-  static constexpr int kW1 = kWT + 2 * W * W;   // [3][8*ob + t] = c * W_1[c][ob + 4t]
-  static constexpr int kB = kW1 + 3 * W;        // [3][8*ob + t] = c * b_l[ob + 4t]
-  static constexpr int kWO = kB + 3 * W;        // [8*ob + t] = w_o[ob + 4t]
-  static constexpr int kBO = kWO + W;           // b_o
+  static constexpr int kWF = 0;                     // [L-1][k = in][NT*ob + t] = c * W_l[k][ob + 4t]
+  static constexpr int kWT = kWF + (L - 1) * W * W;  // [L-1][k = out][NT*ib + t] = W_l[ib + 4t][k]
+  static constexpr int kW1 = kWT + (L - 1) * W * W;  // [3][NT*ob + t] = c * W_1[c][ob + 4t]
+  static constexpr int kB = kW1 + 3 * W;            // [L][NT*ob + t] = c * b_l[ob + 4t]
+  static constexpr int kWO = kB + L * W;            // [NT*ob + t] = w_o[ob + 4t]
+  static constexpr int kBO = kWO + W;               // b_o
   static constexpr int kShared = kBO + 4;
   static constexpr int kNetW = (kShared + 3) / 4 * 4;  // one network's tables; u- then u+
   // warp-private region
   static constexpr int kX = 0;                  // [4][32] job coordinates (x, y, z, unused)
-  static constexpr int kA = kX + 4 * 32;        // [32][kRS]
-  static constexpr int kBB = kA + W * kRS;      // [32][kRS]
+  static constexpr int kA = kX + 4 * 32;        // [W][kRS]
+  static constexpr int kBB = kA + W * kRS;      // [W][kRS]
   static constexpr int kG = kBB + W * kRS;      // [32] dL/du per job
   static constexpr int kU = kG + 32;            // [32] A_j u_j of bulk tiles
   static constexpr int kAv = kU + 32;           // [32] A_j of bulk tiles
@@ -105,30 +117,45 @@ __device__ __forceinline__ float tanh_scaled(float y) {
   return fmaf(-2.0f, r, 1.0f);
 }
 
-// z[q][t] += sum_k A[k][jc + q] * Bm[k][bc + t] over k < K (A row stride AS, Bm row stride 32)
-template <int K, int AS>
-__device__ __forceinline__ void gemm48(float (&z)[4][8], const float* A, int jc, const float* Bm, int bc) {
-#pragma unroll 4
-  for (int k = 0; k < K; ++k) {
-    const float4 a = ld4(A + k * AS + jc);
-    const float4 b0 = ld4(Bm + k * 32 + bc), b1 = ld4(Bm + k * 32 + bc + 4);
-    const float av[4] = {a.x, a.y, a.z, a.w};
-    const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+// NT consecutive floats (NT a multiple of 4) into v
+template <int NT>
+__device__ __forceinline__ void ldrow(float (&v)[NT], const float* p) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-#pragma unroll
-      for (int t = 0; t < 8; ++t) z[q][t] = fmaf(av[q], bv[t], z[q][t]);
+  for (int c = 0; c < NT / 4; ++c) {
+    const float4 b = ld4(p + 4 * c);
+    v[4 * c] = b.x;
+    v[4 * c + 1] = b.y;
+    v[4 * c + 2] = b.z;
+    v[4 * c + 3] = b.w;
   }
 }
 
-__device__ __forceinline__ void store_blk(float* buf, int ob, int jc, const float (&z)[4][8]) {
+// z[q][t] += sum_k A[k][jc + q] * Bm[k][bc + t] over k < K (A row stride AS, Bm row stride 4 NT)
+template <int K, int AS, int NT>
+__device__ __forceinline__ void gemm(float (&z)[4][NT], const float* A, int jc, const float* Bm, int bc) {
+#pragma unroll 4
+  for (int k = 0; k < K; ++k) {
+    const float4 a = ld4(A + k * AS + jc);
+    const float av[4] = {a.x, a.y, a.z, a.w};
+    float bv[NT];
+    ldrow(bv, Bm + k * 4 * NT + bc);
 #pragma unroll
-  for (int t = 0; t < 8; ++t) st4(buf + (ob + 4 * t) * kRS + jc, z[0][t], z[1][t], z[2][t], z[3][t]);
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int t = 0; t < NT; ++t) z[q][t] = fmaf(av[q], bv[t], z[q][t]);
+  }
 }
 
-__device__ __forceinline__ void load_blk(const float* buf, int ob, int jc, float (&z)[4][8]) {
+template <int NT>
+__device__ __forceinline__ void store_blk(float* buf, int ob, int jc, const float (&z)[4][NT]) {
 #pragma unroll
-  for (int t = 0; t < 8; ++t) {
+  for (int t = 0; t < NT; ++t) st4(buf + (ob + 4 * t) * kRS + jc, z[0][t], z[1][t], z[2][t], z[3][t]);
+}
+
+template <int NT>
+__device__ __forceinline__ void load_blk(const float* buf, int ob, int jc, float (&z)[4][NT]) {
+#pragma unroll
+  for (int t = 0; t < NT; ++t) {
     const float4 v = ld4(buf + (ob + 4 * t) * kRS + jc);
     z[0][t] = v.x;
     z[1][t] = v.y;
@@ -137,42 +164,46 @@ __device__ __forceinline__ void load_blk(const float* buf, int ob, int jc, float
   }
 }
 
-__device__ __forceinline__ void fill_rows(float (&z)[4][8], const float* b) {
-  const float4 b0 = ld4(b), b1 = ld4(b + 4);
-  const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+template <int NT>
+__device__ __forceinline__ void fill_rows(float (&z)[4][NT], const float* b) {
+  float bv[NT];
+  ldrow(bv, b);
 #pragma unroll
   for (int q = 0; q < 4; ++q)
 #pragma unroll
-    for (int t = 0; t < 8; ++t) z[q][t] = bv[t];
+    for (int t = 0; t < NT; ++t) z[q][t] = bv[t];
 }
 
-__device__ __forceinline__ void zero_blk(float (&z)[4][8]) {
+template <int NT>
+__device__ __forceinline__ void zero_blk(float (&z)[4][NT]) {
 #pragma unroll
   for (int q = 0; q < 4; ++q)
 #pragma unroll
-    for (int t = 0; t < 8; ++t) z[q][t] = 0.0f;
+    for (int t = 0; t < NT; ++t) z[q][t] = 0.0f;
 }
 
-__device__ __forceinline__ void tanh_blk(float (&z)[4][8]) {
+template <int NT>
+__device__ __forceinline__ void tanh_blk(float (&z)[4][NT]) {
 #pragma unroll
   for (int q = 0; q < 4; ++q)
 #pragma unroll
-    for (int t = 0; t < 8; ++t) z[q][t] = tanh_scaled(z[q][t]);
+    for (int t = 0; t < NT; ++t) z[q][t] = tanh_scaled(z[q][t]);
 }
 
 // z *= 1 - a^2 with a this lane's block of `buf`
-__device__ __forceinline__ void times_dtanh(float (&z)[4][8], const float* buf, int ob, int jc) {
-  float a[4][8];
+template <int NT>
+__device__ __forceinline__ void times_dtanh(float (&z)[4][NT], const float* buf, int ob, int jc) {
+  float a[4][NT];
   load_blk(buf, ob, jc, a);
 #pragma unroll
   for (int q = 0; q < 4; ++q)
 #pragma unroll
-    for (int t = 0; t < 8; ++t) z[q][t] *= fmaf(-a[q][t], a[q][t], 1.0f);
+    for (int t = 0; t < NT; ++t) z[q][t] *= fmaf(-a[q][t], a[q][t], 1.0f);
 }
 
 // Reduce-scatter of v[0..7] over the 8 lanes that share lane bits 3..4: returns the sum of
 // v[jbl] over those lanes (jbl = lane bits 0..2).
-__device__ __forceinline__ float rs8(const float (&v)[8], int jbl) {
+__device__ __forceinline__ float rs(const float (&v)[8], int jbl) {
   const bool b2 = jbl & 4, b1 = jbl & 2, b0 = jbl & 1;
   float w[4], y[2];
 #pragma unroll
@@ -189,21 +220,49 @@ __device__ __forceinline__ float rs8(const float (&v)[8], int jbl) {
   return keep + __shfl_xor_sync(0xffffffffu, send, 1);
 }
 
-// sum over this lane's 4 jobs, per feature
-__device__ __forceinline__ float colsum_rs(const float (&d)[4][8], int jbl) {
-  float v[8];
+// The same for v[0..3]: the sum over the 8 lanes of v[jbl & 3]; lanes jbl and jbl ^ 4 hold the
+// same value.
+__device__ __forceinline__ float rs(const float (&v)[4], int jbl) {
+  const bool b1 = jbl & 2, b0 = jbl & 1;
+  float w[4], y[2];
 #pragma unroll
-  for (int t = 0; t < 8; ++t) v[t] = (d[0][t] + d[1][t]) + (d[2][t] + d[3][t]);
-  return rs8(v, jbl);
+  for (int q = 0; q < 4; ++q) w[q] = v[q] + __shfl_xor_sync(0xffffffffu, v[q], 4);
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const float send = b1 ? w[q] : w[q + 2], keep = b1 ? w[q + 2] : w[q];
+    y[q] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+  }
+  const float send = b0 ? y[0] : y[1], keep = b0 ? y[1] : y[0];
+  return keep + __shfl_xor_sync(0xffffffffu, send, 1);
+}
+
+// feature of the reduce-scattered values of a lane, and whether the lane adds it in
+template <int NT>
+__device__ __forceinline__ int rs_feature(int lane) {
+  return (lane >> 3) + 4 * (NT == 8 ? (lane & 7) : (lane & 3));
+}
+template <int NT>
+__device__ __forceinline__ bool rs_owner(int lane) {
+  return NT == 8 || (lane & 4) == 0;
+}
+
+// sum over this lane's 4 jobs, per feature
+template <int NT>
+__device__ __forceinline__ float colsum_rs(const float (&d)[4][NT], int jbl) {
+  float v[NT];
+#pragma unroll
+  for (int t = 0; t < NT; ++t) v[t] = (d[0][t] + d[1][t]) + (d[2][t] + d[3][t]);
+  return rs(v, jbl);
 }
 
 // acc[r][t] += sum over the tile's 32 jobs of H[row jbl + 8r][j] * D[row ob + 4t][j]
-__device__ __forceinline__ void dw48(float (&acc)[4][8], const float* H, const float* D, int jbl, int ob) {
+template <int R, int NT>
+__device__ __forceinline__ void dw(float (&acc)[R][NT], const float* H, const float* D, int jbl, int ob) {
 #pragma unroll 2
   for (int s = 0; s < 8; ++s) {
-    float hv[4][4], dv[8][4];
+    float hv[R][4], dv[NT][4];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
+    for (int r = 0; r < R; ++r) {
       const float4 v = ld4(H + (jbl + 8 * r) * kRS + 4 * s);
       hv[r][0] = v.x;
       hv[r][1] = v.y;
@@ -211,7 +270,7 @@ __device__ __forceinline__ void dw48(float (&acc)[4][8], const float* H, const f
       hv[r][3] = v.w;
     }
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
+    for (int t = 0; t < NT; ++t) {
       const float4 v = ld4(D + (ob + 4 * t) * kRS + 4 * s);
       dv[t][0] = v.x;
       dv[t][1] = v.y;
@@ -221,57 +280,76 @@ __device__ __forceinline__ void dw48(float (&acc)[4][8], const float* H, const f
 #pragma unroll
     for (int q = 0; q < 4; ++q)
 #pragma unroll
-      for (int r = 0; r < 4; ++r)
+      for (int r = 0; r < R; ++r)
 #pragma unroll
-        for (int t = 0; t < 8; ++t) acc[r][t] = fmaf(hv[r][q], dv[t][q], acc[r][t]);
+        for (int t = 0; t < NT; ++t) acc[r][t] = fmaf(hv[r][q], dv[t][q], acc[r][t]);
   }
 }
 
 // Gradient accumulators of one warp (see the file comment for the lane ownership).
+template <class N>
 struct Acc {
-  float w3[4][8], w2[4][8];          // dW3, dW2: rows jbl + 8r, columns ob + 4t
-  float wo, b3, b2, b1, w10, w11, w12;  // feature ob + 4*jbl of dWo, db3, db2, db1, dW1[0..2]
-  float bo;                          // dbo (lanes with ob == 0)
+  static constexpr int L = N::kL, R = N::kW / 8, NT = N::kW / 4;
+  float wh[L - 1][R][NT];  // dW of the hidden-to-hidden layers: rows jbl + 8r, columns ob + 4t
+  float b[L];              // db of each hidden layer, feature rs_feature(lane)
+  float w1[3];             // dW of the input layer, feature rs_feature(lane)
+  float wo;                // dw_o, feature rs_feature(lane)
+  float bo;                // db_o (every lane holds the total)
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int m = 0; m < L - 1; ++m)
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int t = 0; t < NT; ++t) wh[m][r][t] = 0.0f;
+#pragma unroll
+    for (int l = 0; l < L; ++l) b[l] = 0.0f;
+    w1[0] = w1[1] = w1[2] = wo = bo = 0.0f;
+  }
 };
 
 // One tile: forward of the 32 jobs whose coordinates are in X, then (with BWD) the backward
 // with dL/du from G.  EPI(u[4]) runs between the two: it receives this lane's 4 network
 // values (jobs jc..jc+3) and must leave G filled for the warp (it may synchronise the warp).
 template <class N, bool BWD, class Epi>
-__device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc& acc, int lane, Epi epi) {
+__device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc<N>& acc, int lane, Epi epi) {
   using Lay = Layout<N>;
-  const int jbl = lane & 7, ob = lane >> 3, jc = 4 * jbl, bc = 8 * ob;
+  constexpr int W = Lay::W, L = Lay::L, NT = Lay::NT;
+  const int jbl = lane & 7, ob = lane >> 3, jc = 4 * jbl, bc = NT * ob;
   float* X = wp + Lay::kX;
   float* bufA = wp + Lay::kA;
   float* bufB = wp + Lay::kBB;
   float* G = wp + Lay::kG;
-  float h[4][8];
+  float h[4][NT];
   // layer 1: x -> bufA
   fill_rows(h, sm + Lay::kB + bc);
-  gemm48<3, 32>(h, X, jc, sm + Lay::kW1, bc);
+  gemm<3, 32>(h, X, jc, sm + Lay::kW1, bc);
   tanh_blk(h);
   store_blk(bufA, ob, jc, h);
   __syncwarp();
-  // layer 2: bufA -> bufB
-  fill_rows(h, sm + Lay::kB + 32 + bc);
-  gemm48<32, kRS>(h, bufA, jc, sm + Lay::kWF, bc);
-  tanh_blk(h);
-  store_blk(bufB, ob, jc, h);
-  __syncwarp();
-  // layer 3: bufB -> registers
-  fill_rows(h, sm + Lay::kB + 64 + bc);
-  gemm48<32, kRS>(h, bufB, jc, sm + Lay::kWF + 32 * 32, bc);
+  if constexpr (L == 3) {
+    // layer 2: bufA -> bufB
+    fill_rows(h, sm + Lay::kB + W + bc);
+    gemm<W, kRS>(h, bufA, jc, sm + Lay::kWF, bc);
+    tanh_blk(h);
+    store_blk(bufB, ob, jc, h);
+    __syncwarp();
+  }
+  // last hidden layer: h_{L-1} (bufB for 3 layers, bufA for 2) -> registers
+  float* hprev = L == 3 ? bufB : bufA;
+  fill_rows(h, sm + Lay::kB + (L - 1) * W + bc);
+  gemm<W, kRS>(h, hprev, jc, sm + Lay::kWF + (L - 2) * W * W, bc);
   tanh_blk(h);
   // output layer, reduced over the 4 feature blocks
-  const float4 wo0 = ld4(sm + Lay::kWO + bc), wo1 = ld4(sm + Lay::kWO + bc + 4);
-  const float wo[8] = {wo0.x, wo0.y, wo0.z, wo0.w, wo1.x, wo1.y, wo1.z, wo1.w};
+  float wo[NT];
+  ldrow(wo, sm + Lay::kWO + bc);
   const float bo = sm[Lay::kBO];
   float u[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     float s = 0.0f;
 #pragma unroll
-    for (int t = 0; t < 8; ++t) s = fmaf(h[q][t], wo[t], s);
+    for (int t = 0; t < NT; ++t) s = fmaf(h[q][t], wo[t], s);
     s += __shfl_xor_sync(0xffffffffu, s, 8);
     s += __shfl_xor_sync(0xffffffffu, s, 16);
     u[q] = s + bo;
@@ -285,58 +363,62 @@ __device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc& acc, i
   const float4 g4 = ld4(G + jc);
   const float gv[4] = {g4.x, g4.y, g4.z, g4.w};
   {
-    float v[8];
+    float v[NT];
 #pragma unroll
-    for (int t = 0; t < 8; ++t) v[t] = fmaf(gv[0], h[0][t], gv[1] * h[1][t]) + fmaf(gv[2], h[2][t], gv[3] * h[3][t]);
-    acc.wo += rs8(v, jbl);
+    for (int t = 0; t < NT; ++t) v[t] = fmaf(gv[0], h[0][t], gv[1] * h[1][t]) + fmaf(gv[2], h[2][t], gv[3] * h[3][t]);
+    acc.wo += rs(v, jbl);
     float gs = (gv[0] + gv[1]) + (gv[2] + gv[3]);
     gs += __shfl_xor_sync(0xffffffffu, gs, 1);
     gs += __shfl_xor_sync(0xffffffffu, gs, 2);
     gs += __shfl_xor_sync(0xffffffffu, gs, 4);
     acc.bo += gs;
   }
-  // delta3 = g w_o (1 - h3^2) over h1
+  // delta_L = g w_o (1 - h_L^2) over the buffer that held h_{L-2} (3 layers: h1) or is free
+  float* dbuf = L == 3 ? bufA : bufB;
 #pragma unroll
   for (int q = 0; q < 4; ++q)
 #pragma unroll
-    for (int t = 0; t < 8; ++t) h[q][t] = gv[q] * wo[t] * fmaf(-h[q][t], h[q][t], 1.0f);
-  acc.b3 += colsum_rs(h, jbl);
-  store_blk(bufA, ob, jc, h);
+    for (int t = 0; t < NT; ++t) h[q][t] = gv[q] * wo[t] * fmaf(-h[q][t], h[q][t], 1.0f);
+  acc.b[L - 1] += colsum_rs(h, jbl);
+  store_blk(dbuf, ob, jc, h);
   __syncwarp();
-  dw48(acc.w3, bufB, bufA, jbl, ob);
-  // delta2 = (delta3 W3^T) (1 - h2^2) over h2
+  dw(acc.wh[L - 2], hprev, dbuf, jbl, ob);
+  // delta_{L-1} = (delta_L W_L^T) (1 - h_{L-1}^2)
   zero_blk(h);
-  gemm48<32, kRS>(h, bufA, jc, sm + Lay::kWT + 32 * 32, bc);
-  times_dtanh(h, bufB, ob, jc);
-  acc.b2 += colsum_rs(h, jbl);
-  __syncwarp();
-  store_blk(bufB, ob, jc, h);
-  {  // h1 again, over delta3
-    float h1[4][8];
-    fill_rows(h1, sm + Lay::kB + bc);
-    gemm48<3, 32>(h1, X, jc, sm + Lay::kW1, bc);
-    tanh_blk(h1);
-    store_blk(bufA, ob, jc, h1);
+  gemm<W, kRS>(h, dbuf, jc, sm + Lay::kWT + (L - 2) * W * W, bc);
+  times_dtanh(h, hprev, ob, jc);
+  acc.b[L - 2] += colsum_rs(h, jbl);
+  if constexpr (L == 3) {
+    __syncwarp();
+    store_blk(bufB, ob, jc, h);  // delta2 over h2
+    {  // h1 again, over delta3
+      float h1[4][NT];
+      fill_rows(h1, sm + Lay::kB + bc);
+      gemm<3, 32>(h1, X, jc, sm + Lay::kW1, bc);
+      tanh_blk(h1);
+      store_blk(bufA, ob, jc, h1);
+    }
+    __syncwarp();
+    dw(acc.wh[0], bufA, bufB, jbl, ob);
+    // delta1 = (delta2 W2^T) (1 - h1^2)
+    zero_blk(h);
+    gemm<W, kRS>(h, bufB, jc, sm + Lay::kWT, bc);
+    times_dtanh(h, bufA, ob, jc);
+    acc.b[0] += colsum_rs(h, jbl);
   }
-  __syncwarp();
-  dw48(acc.w2, bufA, bufB, jbl, ob);
-  // delta1 = (delta2 W2^T) (1 - h1^2)
-  zero_blk(h);
-  gemm48<32, kRS>(h, bufB, jc, sm + Lay::kWT, bc);
-  times_dtanh(h, bufA, ob, jc);
-  acc.b1 += colsum_rs(h, jbl);
+  // h = delta1: dW1 += x^T delta1
   {
     const float4 x0 = ld4(X + jc), x1 = ld4(X + 32 + jc), x2 = ld4(X + 64 + jc);
-    float v[8];
+    float v[NT];
 #pragma unroll
-    for (int t = 0; t < 8; ++t) v[t] = fmaf(x0.x, h[0][t], fmaf(x0.y, h[1][t], fmaf(x0.z, h[2][t], x0.w * h[3][t])));
-    acc.w10 += rs8(v, jbl);
+    for (int t = 0; t < NT; ++t) v[t] = fmaf(x0.x, h[0][t], fmaf(x0.y, h[1][t], fmaf(x0.z, h[2][t], x0.w * h[3][t])));
+    acc.w1[0] += rs(v, jbl);
 #pragma unroll
-    for (int t = 0; t < 8; ++t) v[t] = fmaf(x1.x, h[0][t], fmaf(x1.y, h[1][t], fmaf(x1.z, h[2][t], x1.w * h[3][t])));
-    acc.w11 += rs8(v, jbl);
+    for (int t = 0; t < NT; ++t) v[t] = fmaf(x1.x, h[0][t], fmaf(x1.y, h[1][t], fmaf(x1.z, h[2][t], x1.w * h[3][t])));
+    acc.w1[1] += rs(v, jbl);
 #pragma unroll
-    for (int t = 0; t < 8; ++t) v[t] = fmaf(x2.x, h[0][t], fmaf(x2.y, h[1][t], fmaf(x2.z, h[2][t], x2.w * h[3][t])));
-    acc.w12 += rs8(v, jbl);
+    for (int t = 0; t < NT; ++t) v[t] = fmaf(x2.x, h[0][t], fmaf(x2.y, h[1][t], fmaf(x2.z, h[2][t], x2.w * h[3][t])));
+    acc.w1[2] += rs(v, jbl);
   }
   __syncwarp();  // the next tile overwrites X, G and both buffers
 }
@@ -347,44 +429,49 @@ __device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc& acc, i
 template <class N>
 __device__ __forceinline__ void load_weights(float* sm, const float* __restrict__ params, int OFF) {
   using Lay = Layout<N>;
+  constexpr int W = Lay::W, L = Lay::L, NT = Lay::NT;
   const float c = kTanhScale;
   const float* pw = params + OFF;
-  for (int e = threadIdx.x; e < 2 * 32 * 32; e += blockDim.x) {
-    const int l = e >> 10, r = e & 1023, k = r >> 5, col = r & 31, hi = col >> 3, t = col & 7;
-    const float* wl = pw + (l ? N::layer_off(2) : N::layer_off(1));
-    sm[Lay::kWF + e] = c * __ldg(wl + k * 32 + hi + 4 * t);
-    sm[Lay::kWT + e] = __ldg(wl + (hi + 4 * t) * 32 + k);
+  for (int e = threadIdx.x; e < (L - 1) * W * W; e += blockDim.x) {
+    const int l = e / (W * W), r = e % (W * W), k = r / W, col = r % W, hi = col / NT, t = col % NT;
+    const float* wl = pw + N::layer_off(l + 1);
+    sm[Lay::kWF + e] = c * __ldg(wl + k * W + hi + 4 * t);
+    sm[Lay::kWT + e] = __ldg(wl + (hi + 4 * t) * W + k);
   }
-  for (int e = threadIdx.x; e < 3 * 32; e += blockDim.x) {
-    const int row = e >> 5, col = e & 31, f = (col >> 3) + 4 * (col & 7);
-    const int boff = row == 0 ? N::layer_off(0) + 3 * 32 : (row == 1 ? N::layer_off(1) : N::layer_off(2)) + 32 * 32;
-    sm[Lay::kW1 + e] = c * __ldg(pw + row * 32 + f);
+  for (int e = threadIdx.x; e < 3 * W; e += blockDim.x) {
+    const int col = e % W, f = col / NT + 4 * (col % NT);
+    sm[Lay::kW1 + e] = c * __ldg(pw + (e / W) * W + f);
+  }
+  for (int e = threadIdx.x; e < L * W; e += blockDim.x) {
+    const int l = e / W, col = e % W, f = col / NT + 4 * (col % NT);
+    const int boff = l == 0 ? N::layer_off(0) + 3 * W : N::layer_off(l) + W * W;
     sm[Lay::kB + e] = c * __ldg(pw + boff + f);
   }
-  for (int e = threadIdx.x; e < 32; e += blockDim.x) sm[Lay::kWO + e] = __ldg(pw + N::kOut + (e >> 3) + 4 * (e & 7));
-  if (threadIdx.x == 0) sm[Lay::kBO] = __ldg(pw + N::kOut + 32);
+  for (int e = threadIdx.x; e < W; e += blockDim.x) sm[Lay::kWO + e] = __ldg(pw + N::kOut + e / NT + 4 * (e % NT));
+  if (threadIdx.x == 0) sm[Lay::kBO] = __ldg(pw + N::kOut + W);
 }
 
 // Add a warp's accumulators into the CTA accumulator (flat layout of network N).
 template <class N>
-__device__ __forceinline__ void flush_acc(float* cta, const Acc& a, int lane) {
-  const int jbl = lane & 7, ob = lane >> 3, f = ob + 4 * jbl;
+__device__ __forceinline__ void flush_acc(float* cta, const Acc<N>& a, int lane) {
+  using Lay = Layout<N>;
+  constexpr int W = Lay::W, L = Lay::L, NT = Lay::NT, R = Lay::R;
+  const int jbl = lane & 7, ob = lane >> 3;
 #pragma unroll
-  for (int r = 0; r < 4; ++r)
+  for (int m = 0; m < L - 1; ++m)
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      const int cell = (jbl + 8 * r) * 32 + ob + 4 * t;
-      atomicAdd(cta + N::layer_off(2) + cell, a.w3[r][t]);
-      atomicAdd(cta + N::layer_off(1) + cell, a.w2[r][t]);
-    }
-  atomicAdd(cta + N::kOut + f, a.wo);
-  atomicAdd(cta + N::layer_off(2) + 32 * 32 + f, a.b3);
-  atomicAdd(cta + N::layer_off(1) + 32 * 32 + f, a.b2);
-  atomicAdd(cta + 3 * 32 + f, a.b1);
-  atomicAdd(cta + 0 * 32 + f, a.w10);
-  atomicAdd(cta + 1 * 32 + f, a.w11);
-  atomicAdd(cta + 2 * 32 + f, a.w12);
-  if (lane == 0) atomicAdd(cta + N::kOut + 32, a.bo);
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+      for (int t = 0; t < NT; ++t) atomicAdd(cta + N::layer_off(m + 1) + (jbl + 8 * r) * W + ob + 4 * t, a.wh[m][r][t]);
+  if (rs_owner<NT>(lane)) {
+    const int f = rs_feature<NT>(lane);
+    atomicAdd(cta + N::kOut + f, a.wo);
+#pragma unroll
+    for (int l = 0; l < L; ++l) atomicAdd(cta + (l == 0 ? 3 * W : N::layer_off(l) + W * W) + f, a.b[l]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) atomicAdd(cta + c * W + f, a.w1[c]);
+  }
+  if (lane == 0) atomicAdd(cta + N::kOut + W, a.bo);
 }
 
 // Launch modes of the engine.  One launch covers both networks (u- tiles first, then u+).
@@ -399,7 +486,7 @@ enum TileMode {
 // partials floss[net][blockIdx.x], residual_out of the bulk slots and, in kTrain, the partial
 // gradient row blockIdx.x (both networks' columns).
 template <class N, int MODE, int NW>
-__global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile(PtsH ph, const int32_t* __restrict__ ids, Workspace w,
+__global__ void __launch_bounds__(32 * NW, warps_per_sm<N>() / NW) k_tile(PtsH ph, const int32_t* __restrict__ ids, Workspace w,
                                                                    dips_records_t rec, int off_p,
                                                                    float* __restrict__ residual_out) {
   using Lay = Layout<N>;
@@ -441,15 +528,8 @@ __global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile(PtsH ph, con
   float* G = wp + Lay::kG;
   float* U = wp + Lay::kU;
   float* Av = wp + Lay::kAv;
-  Acc acc;
-  auto clear = [&]() {
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-      for (int t = 0; t < 8; ++t) acc.w3[r][t] = acc.w2[r][t] = 0.0f;
-    acc.wo = acc.b3 = acc.b2 = acc.b1 = acc.w10 = acc.w11 = acc.w12 = acc.bo = 0.0f;
-  };
-  clear();
+  Acc<N> acc;
+  acc.clear();
 
   const int64_t tiles_m = s_tiles[0], tiles = s_tiles[1];
   const volatile int64_t(*sn)[5] = s_net;  // read per tile, not held in registers
@@ -506,7 +586,7 @@ __global__ void __launch_bounds__(32 * NW, kWarpsPerSm / NW) k_tile(PtsH ph, con
     if (BWD && net != cur) {  // tiles come in increasing order: at most one switch, u- to u+
       if (cur >= 0) {
         flush_acc<N>(sm + Cta::kAcc + cur * Cta::kAccStride, acc, lane);
-        clear();
+        acc.clear();
       }
       cur = net;
     }

@@ -823,7 +823,7 @@ extern "C" int dips_residual_fwd(const dips_arch_t* arch, const float* params, c
   Workspace W;
   st = prep_ws(arch, params, batch, workspace, ws_bytes, &W);
   if (st) return st;
-  st = ops->load_params(params, stream);
+  st = ops->load_params(params, 0, stream);
   if (st) return st;
   return run_forward(ops, arch, params, rec, batch_ids, batch, W, loss_out, residual_out, false, nullptr, stream);
 }
@@ -839,7 +839,7 @@ extern "C" int dips_residual_bwd(const dips_arch_t* arch, const float* params, c
   Workspace W;
   st = prep_ws(arch, params, batch, workspace, ws_bytes, &W);
   if (st) return st;
-  st = ops->load_params(params, stream);
+  st = ops->load_params(params, 0, stream);
   if (st) return st;
   // the bulk points' gradient comes from the fused kernel, run again with its backward half
   st = ops->bulk_fused(make_ph(rec), batch_ids, W, *rec, nullptr, true, nullptr, stream);
@@ -875,7 +875,7 @@ extern "C" int dips_loss_coeff_tangent(const dips_arch_t* arch, const float* par
   Workspace W;
   st = prep_ws(arch, params, batch, workspace, ws_bytes, &W);
   if (st) return st;
-  st = ops->load_params(params, stream);
+  st = ops->load_params(params, 0, stream);
   if (st) return st;
   st = expand(rec, batch_ids, batch, W, 0, nullptr, stream);  // every point general: u of all jobs
   if (st) return st;
@@ -908,7 +908,7 @@ static int train_step(const dips_arch_t* arch, const dips_adam_t* hp, float* par
   Workspace W;
   st = prep_ws(arch, params, batch, workspace, ws_bytes, &W);
   if (st) return st;
-  st = ops->load_params(params, stream);
+  st = ops->load_params(params, 0, stream);
   if (st) return st;
   // the loss is written by the step's last kernel (k_reduce_adam), before the update
   st = run_forward(ops, arch, params, rec, batch_ids, batch, W, nullptr, nullptr, true, mk, stream);
@@ -956,7 +956,7 @@ extern "C" int dips_autotune(const dips_arch_t* arch, const float* params, const
   Workspace W;
   st = prep_ws(arch, params, batch, workspace, ws_bytes, &W);
   if (st) return st;
-  st = ops->load_params(params, stream);
+  st = ops->load_params(params, 0, stream);
   if (st) return st;
   int chosen = 0;
   if (ops->autotune) {
@@ -1006,7 +1006,7 @@ extern "C" int dips_mlp_eval(const dips_arch_t* arch, const float* params, const
   DIPS_REQUIRE(params && pts && phi_at && u_out, DIPS_E_ARG, "dips_mlp_eval: null pointer");
   const ArchOps* ops = find_arch(arch);
   if (!ops) return DIPS_E_UNSUPPORTED;
-  int st = ops->load_params(params, stream);
+  int st = ops->load_params(params, 1, stream);
   if (st) return st;
   return ops->mlp_eval(pts, phi_at, n, u_out, grad_out, stream);
 }

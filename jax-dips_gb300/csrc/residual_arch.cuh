@@ -501,8 +501,14 @@ __global__ void __launch_bounds__(128) k_mlp_eval(const float* __restrict__ pts,
 
 using A = Arch<DIPS_LM, DIPS_WM, DIPS_LP, DIPS_WP>;
 
-static int load_params(const float* params, cudaStream_t s) {
+// both networks on the register-blocked tile engine (one shape for both), one launch per phase
+constexpr bool kTileArch = tile::supported<typename A::M>() && tile::supported<typename A::P>() &&
+                           A::M::kW == A::P::kW && A::M::kL == A::P::kL;
+
+static int load_params(const float* params, int for_eval, cudaStream_t s) {
   static_assert(2 * A::kParams <= kMaxConstParams, "network too large for the constant bank");
+  // the tile engine reads the parameters from global memory; only mlp_eval needs the bank
+  if (kTileArch && !for_eval) return DIPS_OK;
   // two copies: forward-pass operands at 0, backward-pass operands at kParams (with one
   // copy the compiler keeps every weight used by both passes in registers)
   cudaError_t e = cudaMemcpyToSymbolAsync(c_w, params, sizeof(float) * A::kParams, 0, cudaMemcpyDeviceToDevice, s);
@@ -512,15 +518,11 @@ static int load_params(const float* params, cudaStream_t s) {
   return e == cudaSuccess ? DIPS_OK : cuda_status(e, "cudaMemcpyToSymbolAsync(params)");
 }
 
-template <class N>
-constexpr bool uses_tile() {
-  return N::kW == 32 && N::kL == 3;
-}
-// both networks on the register-blocked tile engine, one launch per phase
-constexpr bool kTileArch = uses_tile<typename A::M>() && uses_tile<typename A::P>();
 
-// CTA width of the tile engine per device (one CTA per SM): 12 warps (default), 10 or 8,
-// chosen by dips_autotune
+// CTA widths of the tile engine (warps per CTA): width 32 fills an SM with one CTA of 12, 10 or 8
+// warps; width 16 runs 24 warps per SM as 2 x 12, 3 x 8 or 4 x 6.  dips_autotune picks one per
+// device; the first is the default.
+constexpr int kTileCand[3] = {12, A::M::kW == 32 ? 10 : 8, A::M::kW == 32 ? 8 : 6};
 constexpr int kMaxDevices = 64;
 static std::atomic<int> g_tile_nw[kMaxDevices];
 static std::mutex g_tune_mu;
@@ -534,7 +536,7 @@ static int current_device() {
 static int tile_nw() {
   const int dev = current_device();
   const int v = dev < 0 ? 0 : g_tile_nw[dev].load(std::memory_order_relaxed);
-  return v ? v : tile::kWarpsPerSm;
+  return v ? v : kTileCand[0];
 }
 
 template <class N, int MODE, int NW>
@@ -550,7 +552,9 @@ static int tile_launch_nw(const PtsH& ph, const int32_t* ids, const Workspace& w
     if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(tile engine smem)");
     attr_done = true;
   }
-  tile::k_tile<N, MODE, NW><<<kTileGrid, 32 * NW, bytes, s>>>(ph, ids, w, rec, A::kOffP, residual_out);
+  constexpr int ctas_per_sm = tile::warps_per_sm<N>() / NW;
+  static_assert(ctas_per_sm * (bytes + 1024) <= 228 * 1024, "tile engine: CTAs per SM do not fit in shared memory");
+  tile::k_tile<N, MODE, NW><<<kTileGrid * ctas_per_sm, 32 * NW, bytes, s>>>(ph, ids, w, rec, A::kOffP, residual_out);
   return DIPS_OK;
 }
 
@@ -560,14 +564,10 @@ static int tile_launch(const PtsH& ph, const int32_t* ids, const Workspace& w, c
                        float* residual_out, cudaStream_t s) {
   if constexpr (TILE) {
     using N = typename A::M;
-    switch (tile_nw()) {
-      case 10:
-        return tile_launch_nw<N, MODE, 10>(ph, ids, w, rec, residual_out, s);
-      case 8:
-        return tile_launch_nw<N, MODE, 8>(ph, ids, w, rec, residual_out, s);
-      default:
-        return tile_launch_nw<N, MODE, 12>(ph, ids, w, rec, residual_out, s);
-    }
+    const int nw = tile_nw();
+    if (nw == kTileCand[1]) return tile_launch_nw<N, MODE, kTileCand[1]>(ph, ids, w, rec, residual_out, s);
+    if (nw == kTileCand[2]) return tile_launch_nw<N, MODE, kTileCand[2]>(ph, ids, w, rec, residual_out, s);
+    return tile_launch_nw<N, MODE, kTileCand[0]>(ph, ids, w, rec, residual_out, s);
   } else {
     ::dips::set_error("tile engine: network shape without the engine");
     return DIPS_E_UNSUPPORTED;
@@ -679,11 +679,12 @@ static int autotune(const PtsH& ph, const int32_t* ids, const Workspace& w, cons
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
       return cuda_status(cudaGetLastError(), "autotune: cudaEventCreate");
-    const int cand[3] = {12, 10, 8};
+    const int* cand = kTileCand;
     float best = 3.4e38f;
-    int best_nw = tile::kWarpsPerSm;
+    int best_nw = kTileCand[0];
     int st = DIPS_OK;
-    for (int c : cand) {
+    for (int ci = 0; ci < 3; ++ci) {
+      const int c = cand[ci];
       g_tile_nw[dev].store(c);
       for (int r = 0; r < 4 && !st; ++r) {
         if (r == 1) cudaEventRecord(e0, s);

@@ -112,7 +112,9 @@ struct ArchOps {
   int m_layers, m_width, p_layers, p_width;
   int n_params;
   int bulk_ok;  // 0: no bulk-point kernel; every point is expanded into jobs
-  int (*load_params)(const float* params, cudaStream_t s);
+  // makes params the operands of the kernels that follow on s; for_eval: also for mlp_eval (the
+  // constant-bank copy, which the tile engine's training launches do not read)
+  int (*load_params)(const float* params, int for_eval, cudaStream_t s);
   int (*job_forward)(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s);
   int (*job_adjoint)(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s);
   // bulk points: forward, residual, loss partials, residual_out (may be NULL) and, with bwd,

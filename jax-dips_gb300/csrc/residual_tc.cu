@@ -606,7 +606,7 @@ __global__ void __launch_bounds__(128) k_tc_eval(const float* __restrict__ param
 // the calling thread.
 thread_local const float* t_params = nullptr;
 
-static int load_params(const float* params, cudaStream_t) {
+static int load_params(const float* params, int, cudaStream_t) {
   t_params = params;
   return DIPS_OK;
 }

@@ -1,10 +1,12 @@
 """Many independent interface problems of uneven size trained together.
 
-Each instance has its own level set, residual records, network parameters and Adam state (the
-reference trains one problem per ``Trainer``; examples/benchmark_LPBE runs its molecules one by
-one).  ``InstanceBatch`` captures the training steps of all instances in one CUDA graph, so
-that a batched step is one graph launch: the batch-id kernel and the fused training step of
-every instance, largest instance first, on one stream.
+Each instance has its own level set, residual records, network parameters, Adam state and step
+workspace (the reference trains one problem per ``Trainer``; examples/benchmark_LPBE runs its
+molecules one by one).  ``InstanceBatch`` captures the training steps of all instances in one
+CUDA graph, so that a batched step is one graph launch: the batch-id kernel and the fused
+training step of every instance.  The instances share nothing on the GPU, so they are dealt,
+largest first, over several capture streams; the graph keeps them as independent chains that
+the GPU runs side by side, which fills the SMs that one small instance leaves idle.
 """
 
 from __future__ import annotations
@@ -46,7 +48,7 @@ class InstanceBatch:
     """
 
     def __init__(self, instances, arch: nn.Arch, batch: int = 1 << 15, lr: float = 1e-3, seed: int = 0,
-                 device="cuda"):
+                 device="cuda", streams: int = 8):
         if not torch.cuda.is_available():
             raise RuntimeError("dips_gb300 runs on a CUDA GPU; none is available")
         lib = _lib.load()
@@ -57,16 +59,28 @@ class InstanceBatch:
         self.items = [Instance(side, prob, arch, batch, lr, seed + i, device) for i, (side, prob) in enumerate(instances)]
         self.order = sorted(range(len(self.items)), key=lambda i: -self.items[i].level.n)
         self.losses = torch.zeros(len(self.items), dtype=torch.float64, device=device)
+        self.streams = [torch.cuda.Stream(device=device) for _ in range(max(1, int(streams)))]
         self.graph = None
 
-    def _step_all(self):
+    def _step_one(self, i):
         lib = _lib.load()
-        for i in self.order:
-            it = self.items[i]
-            _lib.check(lib.dips_batch_ids_device(it.level.n, it.batch, it.n_batches, it.seed, 1, _lib.ptr(it.opt.count),
-                                                 _lib.ptr(it.ids), _lib.stream_handle()), "dips_batch_ids_device")
-            ops.train_step(self.arch, it.params, it.opt, it.level, it.ids, it.ws, it.loss)
-            self.losses[i : i + 1].copy_(it.loss.reshape(1))
+        it = self.items[i]
+        _lib.check(lib.dips_batch_ids_device(it.level.n, it.batch, it.n_batches, it.seed, 1, _lib.ptr(it.opt.count),
+                                             _lib.ptr(it.ids), _lib.stream_handle()), "dips_batch_ids_device")
+        ops.train_step(self.arch, it.params, it.opt, it.level, it.ids, it.ws, it.loss)
+        self.losses[i : i + 1].copy_(it.loss.reshape(1))
+
+    def _step_all(self):
+        """Every instance's step, dealt over the side streams (fork from and join to the current
+        stream, so that the whole batched step is ordered like one launch)."""
+        main = torch.cuda.current_stream()
+        for s in self.streams:
+            s.wait_stream(main)
+        for k, i in enumerate(self.order):
+            with torch.cuda.stream(self.streams[k % len(self.streams)]):
+                self._step_one(i)
+        for s in self.streams:
+            main.wait_stream(s)
 
     def capture(self):
         """Warm up once (restoring the state), then capture every instance's step in one graph."""
@@ -100,4 +114,10 @@ class InstanceBatch:
 
     @property
     def kernels_per_step(self) -> int:
-        return 14 * len(self.items)
+        """This library's kernel launches per batched step: per instance the batch ids, the
+        expansion (3), the general forward, the general residual, the bulk training launch and
+        the gradient tail (reduction, loss, Adam); shapes off the tile engine launch the forward,
+        the bulk kernel and the adjoint once per network.  (A loss copy per instance is torch's.)"""
+        a = self.arch
+        tile = (a.m_layers, a.m_width) == (a.p_layers, a.p_width) and (a.m_layers, a.m_width) in ((2, 16), (3, 32))
+        return (8 if tile else 12) * len(self.items)

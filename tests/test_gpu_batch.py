@@ -1,6 +1,7 @@
-"""Batched instances (uneven grids, one graph launch per step): every instance's step in the
-captured graph gives what the same step gives when run on its own (up to the order of the
-shared-memory atomic additions inside the 2x16 adjoint, which is not fixed)."""
+"""Batched instances (uneven grids, one graph launch per step, instances side by side on the
+graph's streams): every instance's step in the captured graph gives what the same step gives
+when the instances run one after another on one stream without a graph (up to the order of the
+shared-memory atomic additions of the weight gradients, which is not fixed)."""
 
 import numpy as np
 import pytest
@@ -24,7 +25,7 @@ def test_instance_batch_graph_matches_independent_steps():
     arch = nn.Arch(2, 16, 2, 16)
     insts = _instances()
     b = batch.InstanceBatch(insts, arch, batch=2048, lr=1e-3, seed=3).capture()
-    ref = batch.InstanceBatch(insts, arch, batch=2048, lr=1e-3, seed=3)  # same seeds, no graph
+    ref = batch.InstanceBatch(insts, arch, batch=2048, lr=1e-3, seed=3, streams=1)  # same seeds, no graph
     for _ in range(4):
         lb = b.step().clone()
         lr = ref.step().clone()
