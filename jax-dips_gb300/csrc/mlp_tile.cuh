@@ -258,7 +258,7 @@ __device__ __forceinline__ float colsum_rs(const float (&d)[4][NT], int jbl) {
 // acc[r][t] += sum over the tile's 32 jobs of H[row jbl + 8r][j] * D[row ob + 4t][j]
 template <int R, int NT>
 __device__ __forceinline__ void dw(float (&acc)[R][NT], const float* H, const float* D, int jbl, int ob) {
-#pragma unroll 2
+#pragma unroll 1  // measured: 1.2 % faster than 2, 1.2 % than 4 (3x32 training launch)
   for (int s = 0; s < 8; ++s) {
     float hv[R][4], dv[NT][4];
 #pragma unroll
