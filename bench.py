@@ -485,16 +485,10 @@ def run_instances(args, rank, world):
     te0 = time.perf_counter()
     for _ in range(e2e_steps):
         main = torch.cuda.current_stream()
-        for s in ib.streams:
-            s.wait_stream(main)
-        for k, i in enumerate(ib.order):  # the instances side by side, as in the captured step
-            it = ib.items[i]
-            with torch.cuda.stream(ib.streams[k % len(ib.streams)]):
-                it.ids.copy_(host[i], non_blocking=True)
-                _ops.train_step(arch, it.params, it.opt, it.level, it.ids, it.ws, it.loss)
-        for s in ib.streams:
-            main.wait_stream(s)
-        out.copy_(torch.stack([it.loss for it in ib.items]), non_blocking=True)
+        for hbuf, it in zip(host, ib.items):
+            it.ids.copy_(hbuf, non_blocking=True)
+        ib.step_with_ids()  # the multi-instance step on the copied ids
+        out.copy_(ib.losses, non_blocking=True)
         main.synchronize()
     te = time.perf_counter() - te0
     if rank == 0:
@@ -505,13 +499,16 @@ def run_instances(args, rank, world):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"{len(ib.items)} linearised Poisson-Boltzmann instances, sides {sides[0]}..{sides[-1]} "
                                    "(uniform in steps of 16), phi = min over 50-2000 spheres, DoubleMLP 2x16/2x16 tanh; "
-                                   "one CUDA graph launch per batched step (every instance's batch ids + training step, "
-                                   "instances side by side on the graph's streams)",
+                                   "one CUDA graph launch per batched step: dips_train_step_instances (one launch "
+                                   "per phase for all instances, the tile-engine launches persistent over every "
+                                   "instance's tiles)",
                        "global_batch": pts * world, "points": int(sum(it.level.n for it in ib.items)),
                        "batch_per_instance": args.batch, "jobs_per_step": jobs, "setup_s": setup_s,
                        "l2": "flushed (256 MB write) between timed steps", "cuda_graph": True},
-            "roofline": {"bound": "fp32", "kernel": f"whole batched step ({ib.kernels_per_step // len(ib.items)} launches "
-                                                    f"per instance on {len(ib.streams)} capture streams)",
+            "roofline": {"bound": "fp32", "kernel": (f"whole batched step ({ib.kernels_per_step} launches for all "
+                                                     "instances: dips_train_step_instances)" if ib.persistent else
+                                                     f"whole batched step ({ib.kernels_per_step // len(ib.items)} "
+                                                     f"launches per instance on {len(ib.streams)} capture streams)"),
                          "achieved": step_tflops, "peak": 78.4, "unit": "TFLOP/s", "frac": step_tflops / 78.4,
                          "traffic": None, "algorithmic": "3 x F(2x16) x jobs per step",
                          "peak_source": "FFMA probe value measured in the headline runs"},

@@ -229,6 +229,41 @@ int dips_train_step_profiled(const dips_arch_t* arch, const dips_adam_t* hp, flo
 int dips_train_step_noalloc(const dips_arch_t* arch, const dips_adam_t* hp, float* params, float* mu, float* nu,
                             int64_t* count, const dips_records_t* rec, const int32_t* batch_ids, int64_t batch,
                             int64_t max_jobs, double* loss_out, float* grad_out, cudaStream_t stream);
+/* ---- many instances trained together (configuration 4; no counterpart in the reference,
+        whose LPBE example trains its molecules one after another): each instance has its own
+        records, batch, parameters, optimizer state and workspace; all share the network shape
+        and the Adam hyper-parameters ----------------------------------------------------- */
+typedef struct {
+  const dips_records_t* rec;  /* the instance's level (read when the table is prepared) */
+  int32_t* batch_ids;         /* [batch] device; drawn by each step when ids_mode >= 0 */
+  int64_t batch;
+  int64_t n_batches;          /* batches per epoch, for ids drawn from *count (ids_mode >= 0) */
+  uint64_t seed;
+  int32_t ids_mode;           /* -1: batch_ids given by the caller; 0: consecutive ranges;
+                                 1: a seeded permutation per epoch (as dips_batch_ids_device) */
+  float* params;
+  float* mu;
+  float* nu;
+  int64_t* count;
+  void* workspace;            /* dips_step_workspace_bytes(arch, batch, max jobs) bytes */
+  size_t ws_bytes;
+  double* loss_out;           /* device double, may be NULL */
+  float* grad_out;            /* [num_params] device, may be NULL */
+} dips_instance_t;
+/* Device bytes of the instance table of n instances. */
+size_t dips_instances_table_bytes(int32_t n);
+/* Writes the instance table (device memory, dips_instances_table_bytes(n)) and waits for the
+   copy (not capturable: call it once, before capturing steps).  n <= 256. */
+int dips_instances_prepare(const dips_arch_t* arch, const dips_instance_t* inst, int32_t n, void* table,
+                           size_t table_bytes, cudaStream_t stream);
+/* One training step of every instance of a prepared table: per phase one launch for all
+   instances (batch ids, expansion, the general forward, the general residual, the training
+   launch, the gradient tail); the two tile-engine launches are persistent over all instances'
+   tiles.  max_batch: the largest batch of the table.  Tile-engine shapes (3x32, 2x16) without
+   the learned preconditioner; others return DIPS_E_UNSUPPORTED. */
+int dips_train_step_instances(const dips_arch_t* arch, const dips_adam_t* hp, const void* table, int32_t n,
+                              int64_t max_batch, cudaStream_t stream);
+
 /* Autotuner (no counterpart in the reference): runs the residual forward on this batch, then
    times each launch configuration of the shape's tunable point kernel (for 3x32: the
    register-blocked engine, one CTA per SM of 12, 10 or 8 warps) and keeps the fastest for

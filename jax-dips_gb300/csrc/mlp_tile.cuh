@@ -481,14 +481,162 @@ enum TileMode {
   kForwardGeneral = 2,  // general tiles over every job of the job list: u into Workspace::ju
 };
 
+// Tiles of one network of one batch: bulk points, bulk tiles, job range [jb, je) and the first
+// job of the general tiles (after the jobs the bulk tiles' spare lanes carry).
+struct NetTiles {
+  int64_t nb, nbt, jb, je, gf, tiles;
+};
+
+template <int MODE>
+__device__ __forceinline__ NetTiles net_tiles(const Ctl& c, int q) {
+  NetTiles t;
+  t.nb = q ? c.nbp : c.nbm;
+  t.jb = q ? c.jm_pad : 0;
+  t.je = q ? c.total : c.jm;
+  t.nbt = MODE == kForwardGeneral ? 0 : (t.nb + 3) / 4;
+  const int64_t rest = MODE == kForwardGeneral ? t.je - t.jb : t.je - t.jb - 4 * t.nbt;
+  const int64_t ngt = MODE == kForwardBulk || rest <= 0 ? 0 : (rest + 31) / 32;
+  t.gf = t.jb + (MODE == kTrain ? 4 * t.nbt : 0);
+  t.tiles = t.nbt + ngt;
+  return t;
+}
+
+// Stage layout.  Bulk tile: 4 point records [0, 64), spare-lane coordinates [64, 80) and dL/du
+// [80, 84).  General tile: coordinates [0, 128), dL/du [128, 160).  Issues this lane's part of
+// tile lt (of network net) into st and commits a cp.async group (an empty one when !valid).
+template <int MODE>
+__device__ __forceinline__ void issue_tile(const Workspace& w, const NetTiles& nt, int net, int64_t lt, bool valid,
+                                           float* st, int lane) {
+  constexpr bool BWD = MODE == kTrain;
+  if (valid) {
+    if (lt < nt.nbt) {
+      const float* recs = w.brec + (size_t)(net ? w.B : 0) * kRecFloats;
+      if (lane < 16) {
+        const int64_t pidx = lt * 4 + (lane >> 2);
+        const bool ok = pidx < nt.nb;
+        cp_async16(st + 4 * lane, recs + (ok ? pidx : 0) * kRecFloats + 4 * (lane & 3), ok);
+      } else if (BWD && lane < 20) {
+        const int64_t j = nt.jb + 4 * lt + (lane - 16);
+        const bool ok = j < nt.je;
+        cp_async16(st + 64 + 4 * (lane - 16), w.jx + (ok ? j : 0), ok);
+      } else if (BWD && lane < 24) {
+        const int64_t j = nt.jb + 4 * lt + (lane - 20);
+        const bool ok = j < nt.je;
+        cp_async4(st + 80 + (lane - 20), w.jg + (ok ? j : 0), ok);
+      }
+    } else {
+      const int64_t j = nt.gf + (lt - nt.nbt) * 32 + lane;
+      const bool ok = j < nt.je;
+      cp_async16(st + 4 * lane, w.jx + (ok ? j : 0), ok);
+      if (BWD) cp_async4(st + 128 + lane, w.jg + (ok ? j : 0), ok);
+    }
+  }
+  cp_commit();
+}
+
+// Tile lt of network net, its inputs staged in st: forward, bulk residual and loss, and (kTrain)
+// the backward into acc.  lsum: this lane's loss partial of the network.
+template <class N, int MODE>
+__device__ __forceinline__ void do_tile(const Workspace& w, const float* hh, const NetTiles& nt, int net, int64_t lt,
+                                        const float* wsm, float* wp, const float* st, Acc<N>& acc, int lane,
+                                        double& lsum, float* __restrict__ residual_out) {
+  using Lay = Layout<N>;
+  constexpr bool BWD = MODE == kTrain;
+  float* X = wp + Lay::kX;
+  float* G = wp + Lay::kG;
+  float* U = wp + Lay::kU;
+  float* Av = wp + Lay::kAv;
+  const int jc = 4 * (lane & 7);
+  const bool lead = (lane >> 3) == 0;  // lanes holding u of jobs jc..jc+3 after the reduction
+  if (lt < nt.nbt) {
+    // ---- bulk tile: lane = 7 * point + stencil point; with BWD, lanes 28..31 carry four
+    // general jobs (their dL/du is known) instead of idling
+    const int pl = lane / kStencil, s = lane - kStencil * pl;
+    float x[3] = {0.0f, 0.0f, 0.0f};
+    float A = 0.0f;
+    if (lane < 4 * kStencil) {
+      if (lt * 4 + pl < nt.nb) {
+        const float* r = st + pl * kRecFloats;
+        const float p[3] = {r[kRecP], r[kRecP + 1], r[kRecP + 2]};
+        stencil_point(p, hh, s, x);
+        A = r[kRecA + s];
+      }
+    } else if (BWD) {
+      const float* xv = st + 64 + 4 * (lane - 4 * kStencil);
+      x[0] = xv[0];
+      x[1] = xv[1];
+      x[2] = xv[2];
+      G[lane] = st[80 + lane - 4 * kStencil];
+    }
+    // the residual's point records, for lanes 0..3 (point `lane` of the tile)
+    int32_t rslot = -1;
+    float r_lhs0 = 0.0f, r_diag = 1.0f, r_rod = 0.0f;
+    if (lane < 4 && lt * 4 + lane < nt.nb) {
+      const float* r = st + lane * kRecFloats;
+      rslot = __float_as_int(r[kRecSlot]);
+      r_lhs0 = r[kRecLhs0];
+      r_diag = r[kRecDiag];
+      r_rod = r[kRecRod];
+    }
+    X[lane] = x[0];
+    X[32 + lane] = x[1];
+    X[64 + lane] = x[2];
+    Av[lane] = A;
+    __syncwarp();
+    const float Bf = (float)w.B;
+    run_tile<N, BWD>(wsm, wp, acc, lane, [&](const float (&u)[4]) {
+      if (lead) st4(U + jc, u[0] * Av[jc], u[1] * Av[jc + 1], u[2] * Av[jc + 2], u[3] * Av[jc + 3]);
+      __syncwarp();
+      // lanes 0..3: residual of point `lane`; then dL/du of its 7 jobs
+      if (lane < 4) {
+        float gc = 0.0f;
+        if (rslot >= 0) {
+          float lhs = r_lhs0;
+#pragma unroll
+          for (int q = 0; q < kStencil; ++q) lhs += U[kStencil * lane + q];
+          const float qv = lhs / r_diag;
+          const float r0 = nan_to_num(qv) - r_rod;
+          const float Pv = w.pre_P ? w.pre_P[rslot] : 1.0f;  // learned preconditioner
+          const float r = Pv * r0;
+          if (w.pre_P) w.pre_r0[rslot] = r0;
+          gc = isfinite(qv) ? (r / Bf) * Pv / r_diag : 0.0f;
+          lsum += 0.5 * (double)r * (double)r;
+          if (residual_out) residual_out[rslot] = r;
+        }
+        if (BWD) {
+#pragma unroll
+          for (int q = 0; q < kStencil; ++q) G[kStencil * lane + q] = gc * Av[kStencil * lane + q];
+        }
+      }
+    });
+  } else {
+    // ---- general tile: 32 jobs of the job list; kTrain: dL/du known from the residual;
+    // kForwardGeneral: u of each job to ju
+    X[lane] = st[4 * lane];
+    X[32 + lane] = st[4 * lane + 1];
+    X[64 + lane] = st[4 * lane + 2];
+    if (BWD) G[lane] = st[128 + lane];
+    __syncwarp();
+    const int64_t j0 = nt.gf + (lt - nt.nbt) * 32 + jc, je = nt.je;
+    run_tile<N, BWD>(wsm, wp, acc, lane, [&](const float (&u)[4]) {
+      if (MODE == kForwardGeneral && lead) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (j0 + q < je) w.ju[j0 + q] = u[q];
+      }
+    });
+  }
+}
+
 // One launch for both networks.  Bulk tiles hold 4 points x 7 stencil jobs (residual and loss
 // formed in the warp); general tiles hold 32 jobs of the job list.  Writes the per-CTA loss
 // partials floss[net][blockIdx.x], residual_out of the bulk slots and, in kTrain, the partial
 // gradient row blockIdx.x (both networks' columns).
 template <class N, int MODE, int NW>
-__global__ void __launch_bounds__(32 * NW, warps_per_sm<N>() / NW) k_tile(PtsH ph, const int32_t* __restrict__ ids, Workspace w,
-                                                                   dips_records_t rec, int off_p,
-                                                                   float* __restrict__ residual_out) {
+__global__ void __launch_bounds__(32 * NW, warps_per_sm<N>() / NW) k_tile(PtsH ph, const int32_t* __restrict__ ids,
+                                                                         const __grid_constant__ Workspace w,
+                                                                         dips_records_t rec, int off_p,
+                                                                         float* __restrict__ residual_out) {
   using Lay = Layout<N>;
   using Cta = CtaLayout<N, NW>;
   constexpr bool BWD = MODE == kTrain;
@@ -499,78 +647,33 @@ __global__ void __launch_bounds__(32 * NW, warps_per_sm<N>() / NW) k_tile(PtsH p
   load_weights<N>(sm + Lay::kNetW, w.params, off_p);
   if (BWD)
     for (int i = threadIdx.x; i < 2 * Cta::kAccStride; i += blockDim.x) sm[Cta::kAcc + i] = 0.0f;
-  // per network (u- then u+): bulk points, bulk tiles, job range [jb, je) and the first job of
-  // the general tiles (after the jobs the bulk tiles' spare lanes carry); tiles [0, s_tiles[0])
-  // belong to u-, [s_tiles[0], s_tiles[1]) to u+
-  __shared__ int64_t s_net[2][5];
-  __shared__ int64_t s_tiles[2];
-  enum { kNb = 0, kNbt = 1, kJb = 2, kJe = 3, kGf = 4 };
-  if (threadIdx.x == 0) {
-    const Ctl& c = *w.ctl;
-    int64_t t = 0;
-    for (int q = 0; q < 2; ++q) {
-      const int64_t nb = q ? c.nbp : c.nbm, jb = q ? c.jm_pad : 0, je = q ? c.total : c.jm;
-      const int64_t nbt = MODE == kForwardGeneral ? 0 : (nb + 3) / 4;
-      const int64_t rest = MODE == kForwardGeneral ? je - jb : je - jb - 4 * nbt;
-      const int64_t ngt = MODE == kForwardBulk || rest <= 0 ? 0 : (rest + 31) / 32;
-      s_net[q][kNb] = nb;
-      s_net[q][kNbt] = nbt;
-      s_net[q][kJb] = jb;
-      s_net[q][kJe] = je;
-      s_net[q][kGf] = jb + (MODE == kTrain ? 4 * nbt : 0);
-      t += nbt + ngt;
-      s_tiles[q] = t;
-    }
-  }
+  // per network (u- then u+); read per tile from shared memory, not held in registers
+  __shared__ NetTiles s_nt[2];
+  if (threadIdx.x < 2) s_nt[threadIdx.x] = net_tiles<MODE>(*w.ctl, threadIdx.x);
   __syncthreads();
   float* wp = sm + Lay::kWarp0 + warp * Lay::kWarpFloats;
-  float* X = wp + Lay::kX;
-  float* G = wp + Lay::kG;
-  float* U = wp + Lay::kU;
-  float* Av = wp + Lay::kAv;
   Acc<N> acc;
   acc.clear();
-
-  const int64_t tiles_m = s_tiles[0], tiles = s_tiles[1];
-  const volatile int64_t(*sn)[5] = s_net;  // read per tile, not held in registers
-  const float Bf = (float)w.B;
-  const int jc = 4 * (lane & 7);
-  const bool lead = (lane >> 3) == 0;  // lanes holding u of jobs jc..jc+3 after the reduction
+  const int64_t tiles_m = s_nt[0].tiles, tiles = tiles_m + s_nt[1].tiles;
+  const volatile NetTiles* snt = s_nt;
+  auto nt_of = [&](int net) {
+    NetTiles t;
+    t.nb = snt[net].nb;
+    t.nbt = snt[net].nbt;
+    t.jb = snt[net].jb;
+    t.je = snt[net].je;
+    t.gf = snt[net].gf;
+    t.tiles = 0;
+    return t;
+  };
+  const float hh[3] = {ph.h[0], ph.h[1], ph.h[2]};  // registers, not a local copy of ph
   double lsum0 = 0.0, lsum1 = 0.0;
 
-  // Stage layout.  Bulk tile: 4 point records [0, 64), spare-lane coordinates [64, 80) and
-  // dL/du [80, 84).  General tile: coordinates [0, 128), dL/du [128, 160).
   float* stage0 = wp + Lay::kStage;
   auto issue = [&](int64_t t, float* st) {
-    if (t < tiles) {
-      const int net = t >= tiles_m ? 1 : 0;
-      const int64_t lt = net ? t - tiles_m : t;
-      const int64_t nb = sn[net][kNb], jb = sn[net][kJb], je = sn[net][kJe], nbt = sn[net][kNbt];
-      if (lt < nbt) {
-        const float* recs = w.brec + (size_t)(net ? w.B : 0) * kRecFloats;
-        if (lane < 16) {
-          const int64_t pidx = lt * 4 + (lane >> 2);
-          const bool ok = pidx < nb;
-          cp_async16(st + 4 * lane, recs + (ok ? pidx : 0) * kRecFloats + 4 * (lane & 3), ok);
-        } else if (BWD && lane < 20) {
-          const int64_t j = jb + 4 * lt + (lane - 16);
-          const bool ok = j < je;
-          cp_async16(st + 64 + 4 * (lane - 16), w.jx + (ok ? j : 0), ok);
-        } else if (BWD && lane < 24) {
-          const int64_t j = jb + 4 * lt + (lane - 20);
-          const bool ok = j < je;
-          cp_async4(st + 80 + (lane - 20), w.jg + (ok ? j : 0), ok);
-        }
-      } else {
-        const int64_t j = sn[net][kGf] + (lt - nbt) * 32 + lane;
-        const bool ok = j < je;
-        cp_async16(st + 4 * lane, w.jx + (ok ? j : 0), ok);
-        if (BWD) cp_async4(st + 128 + lane, w.jg + (ok ? j : 0), ok);
-      }
-    }
-    cp_commit();
+    const int net = t >= tiles_m ? 1 : 0;
+    issue_tile<MODE>(w, nt_of(net), net, net ? t - tiles_m : t, t < tiles, st, lane);
   };
-
   const int64_t stride = (int64_t)gridDim.x * NW;
   int64_t tile = (int64_t)blockIdx.x * NW + warp;
   issue(tile, stage0);
@@ -581,8 +684,6 @@ __global__ void __launch_bounds__(32 * NW, warps_per_sm<N>() / NW) k_tile(PtsH p
     cp_wait<1>();  // this tile's copies have landed
     __syncwarp();
     const int net = tile < tiles_m ? 0 : 1;
-    const int64_t lt = net ? tile - tiles_m : tile;
-    const int64_t nb = sn[net][kNb], nbt = sn[net][kNbt];
     if (BWD && net != cur) {  // tiles come in increasing order: at most one switch, u- to u+
       if (cur >= 0) {
         flush_acc<N>(sm + Cta::kAcc + cur * Cta::kAccStride, acc, lane);
@@ -590,90 +691,8 @@ __global__ void __launch_bounds__(32 * NW, warps_per_sm<N>() / NW) k_tile(PtsH p
       }
       cur = net;
     }
-    const float* wsm = sm + net * Lay::kNetW;
-    const float* st = stage0 + sidx * Lay::kStageFloats;
-    if (lt < nbt) {
-      // ---- bulk tile: lane = 7 * point + stencil point; with BWD, lanes 28..31 carry four
-      // general jobs (their dL/du is known) instead of idling
-      const int pl = lane / kStencil, s = lane - kStencil * pl;
-      float x[3] = {0.0f, 0.0f, 0.0f};
-      float A = 0.0f;
-      if (lane < 4 * kStencil) {
-        if (lt * 4 + pl < nb) {
-          const float* r = st + pl * kRecFloats;
-          const float p[3] = {r[kRecP], r[kRecP + 1], r[kRecP + 2]};
-          const float hh[3] = {ph.h[0], ph.h[1], ph.h[2]};  // registers, not a local copy of ph
-          stencil_point(p, hh, s, x);
-          A = r[kRecA + s];
-        }
-      } else if (BWD) {
-        const float* xv = st + 64 + 4 * (lane - 4 * kStencil);
-        x[0] = xv[0];
-        x[1] = xv[1];
-        x[2] = xv[2];
-        G[lane] = st[80 + lane - 4 * kStencil];
-      }
-      // the residual's point records, for lanes 0..3 (point `lane` of the tile)
-      int32_t rslot = -1;
-      float r_lhs0 = 0.0f, r_diag = 1.0f, r_rod = 0.0f;
-      if (lane < 4 && lt * 4 + lane < nb) {
-        const float* r = st + lane * kRecFloats;
-        rslot = __float_as_int(r[kRecSlot]);
-        r_lhs0 = r[kRecLhs0];
-        r_diag = r[kRecDiag];
-        r_rod = r[kRecRod];
-      }
-      X[lane] = x[0];
-      X[32 + lane] = x[1];
-      X[64 + lane] = x[2];
-      Av[lane] = A;
-      __syncwarp();
-      run_tile<N, BWD>(wsm, wp, acc, lane, [&](const float (&u)[4]) {
-        if (lead) st4(U + jc, u[0] * Av[jc], u[1] * Av[jc + 1], u[2] * Av[jc + 2], u[3] * Av[jc + 3]);
-        __syncwarp();
-        // lanes 0..3: residual of point `lane`; then dL/du of its 7 jobs
-        if (lane < 4) {
-          float gc = 0.0f;
-          if (rslot >= 0) {
-            float lhs = r_lhs0;
-#pragma unroll
-            for (int q = 0; q < kStencil; ++q) lhs += U[kStencil * lane + q];
-            const float qv = lhs / r_diag;
-            const float r0 = nan_to_num(qv) - r_rod;
-            const float Pv = w.pre_P ? w.pre_P[rslot] : 1.0f;  // learned preconditioner
-            const float r = Pv * r0;
-            if (w.pre_P) w.pre_r0[rslot] = r0;
-            gc = isfinite(qv) ? (r / Bf) * Pv / r_diag : 0.0f;
-            const double l = 0.5 * (double)r * (double)r;
-            if (net)
-              lsum1 += l;
-            else
-              lsum0 += l;
-            if (residual_out) residual_out[rslot] = r;
-          }
-          if (BWD) {
-#pragma unroll
-            for (int q = 0; q < kStencil; ++q) G[kStencil * lane + q] = gc * Av[kStencil * lane + q];
-          }
-        }
-      });
-    } else {
-      // ---- general tile: 32 jobs of the job list; kTrain: dL/du known from the residual;
-      // kForwardGeneral: u of each job to ju
-      X[lane] = st[4 * lane];
-      X[32 + lane] = st[4 * lane + 1];
-      X[64 + lane] = st[4 * lane + 2];
-      if (BWD) G[lane] = st[128 + lane];
-      __syncwarp();
-      const int64_t j0 = sn[net][kGf] + (lt - nbt) * 32 + jc, je = sn[net][kJe];
-      run_tile<N, BWD>(wsm, wp, acc, lane, [&](const float (&u)[4]) {
-        if (MODE == kForwardGeneral && lead) {
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-            if (j0 + q < je) w.ju[j0 + q] = u[q];
-        }
-      });
-    }
+    do_tile<N, MODE>(w, hh, nt_of(net), net, net ? tile - tiles_m : tile, sm + net * Lay::kNetW, wp,
+                     stage0 + sidx * Lay::kStageFloats, acc, lane, net ? lsum1 : lsum0, residual_out);
   }
   cp_wait<0>();
   // loss partials of the CTA, per network
@@ -704,6 +723,160 @@ __global__ void __launch_bounds__(32 * NW, warps_per_sm<N>() / NW) k_tile(PtsH p
       row[off_p + i] = sm[Cta::kAcc + Cta::kAccStride + i];
     }
   }
+}
+
+constexpr int kMaxInstances = 256;  // instances per multi-instance launch
+
+// The persistent launch of a multi-instance step: one launch for every tile of every instance
+// of the table.  Work comes in chunks of NW consecutive tiles of one instance (one tile per
+// warp); each CTA takes one contiguous range of chunks, so that it meets an instance in one run
+// and crosses few instance boundaries (each costs a weight reload and a row write).  On
+// entering an instance the CTA loads its two networks' weights; on leaving it, it adds its loss
+// partials and (kTrain) its gradient row into the next free slot of that instance
+// (Ctl::floss_n, Ctl::grad_rows, counted with atomics; the per-step expansion reset them).
+template <class N, int MODE, int NW>
+__global__ void __launch_bounds__(32 * NW, warps_per_sm<N>() / NW) k_tile_multi(const Inst* __restrict__ T, int n_inst,
+                                                                               int off_p) {
+  using Lay = Layout<N>;
+  using Cta = CtaLayout<N, NW>;
+  constexpr bool BWD = MODE == kTrain;
+  extern __shared__ float4 smem4[];
+  float* sm = reinterpret_cast<float*>(smem4);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ int64_t s_chunk0[kMaxInstances + 1];  // first chunk of each instance
+  __shared__ NetTiles s_nt[2];
+  if (threadIdx.x == 0) {
+    int64_t c = 0;
+    for (int i = 0; i < n_inst; ++i) {
+      s_chunk0[i] = c;
+      const Ctl& ct = *T[i].w.ctl;
+      const int64_t tiles = net_tiles<MODE>(ct, 0).tiles + net_tiles<MODE>(ct, 1).tiles;
+      c += (tiles + NW - 1) / NW;
+    }
+    s_chunk0[n_inst] = c;
+  }
+  __syncthreads();
+  const int64_t chunks = s_chunk0[n_inst];
+  float* wp = sm + Lay::kWarp0 + warp * Lay::kWarpFloats;
+  double* wl = reinterpret_cast<double*>(sm + Cta::kLoss);
+  Acc<N> acc;
+  acc.clear();
+  double lsum0 = 0.0, lsum1 = 0.0;
+  int cur = -1;   // network of the warp's accumulators
+  int inst = -1;  // the CTA's instance
+  const volatile NetTiles* snt = s_nt;
+  auto nt_of = [&](int net) {
+    NetTiles t;
+    t.nb = snt[net].nb;
+    t.nbt = snt[net].nbt;
+    t.jb = snt[net].jb;
+    t.je = snt[net].je;
+    t.gf = snt[net].gf;
+    t.tiles = snt[net].tiles;
+    return t;
+  };
+  // leave instance `inst`: warps add their accumulators and loss partials into the CTA's, which
+  // go to the instance's next free slots
+  __shared__ int64_t s_row;
+  auto leave = [&]() {
+    const Workspace& w = T[inst].w;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      double v = q ? lsum1 : lsum0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) wl[2 * warp + q] = v;
+    }
+    lsum0 = lsum1 = 0.0;
+    if (BWD && cur >= 0) flush_acc<N>(sm + Cta::kAcc + cur * Cta::kAccStride, acc, lane);
+    acc.clear();
+    cur = -1;
+    __syncthreads();
+    if (MODE != kForwardGeneral && threadIdx.x < 2) {
+      const int q = threadIdx.x;
+      double t = 0.0;
+      for (int k = 0; k < NW; ++k) t += wl[2 * k + q];
+      const unsigned long long slot =
+          atomicAdd(reinterpret_cast<unsigned long long*>(&w.ctl->floss_n[q]), 1ull);
+      w.floss[q * kLossSlots + slot] = t;
+      if (BWD) {
+        const unsigned long long r =
+            atomicAdd(reinterpret_cast<unsigned long long*>(&w.ctl->grad_rows[q]), 1ull);
+        if (q == 0) s_row = (int64_t)r;
+      }
+    }
+    if (BWD) {
+      __syncthreads();
+      float* row = w.partials + (size_t)s_row * w.n_params;
+      for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) {
+        row[i] = sm[Cta::kAcc + i];
+        row[off_p + i] = sm[Cta::kAcc + Cta::kAccStride + i];
+        sm[Cta::kAcc + i] = 0.0f;
+        sm[Cta::kAcc + Cta::kAccStride + i] = 0.0f;
+      }
+    }
+    __syncthreads();
+  };
+  if (BWD)
+    for (int i = threadIdx.x; i < 2 * Cta::kAccStride; i += blockDim.x) sm[Cta::kAcc + i] = 0.0f;
+  float* stage0 = wp + Lay::kStage;
+  int next_inst = 0;
+  int sidx = 0;
+  bool have = false;  // stage sidx already holds this chunk's tile (prefetched in the last round)
+  // a contiguous range of chunks per CTA: it crosses at most a few instance boundaries
+  const int64_t per = (chunks + gridDim.x - 1) / gridDim.x;
+  const int64_t c_end = min(chunks, (int64_t)(blockIdx.x + 1) * per);
+  for (int64_t c = (int64_t)blockIdx.x * per; c < c_end; ++c, sidx ^= 1) {
+    while (next_inst < n_inst && c >= s_chunk0[next_inst + 1]) ++next_inst;  // instance of chunk c
+    if (next_inst != inst) {
+      if (inst >= 0) leave();
+      inst = next_inst;
+      const Inst& I = T[inst];
+      load_weights<N>(sm, I.w.params, 0);
+      load_weights<N>(sm + Lay::kNetW, I.w.params, off_p);
+      if (threadIdx.x < 2) s_nt[threadIdx.x] = net_tiles<MODE>(*I.w.ctl, threadIdx.x);
+      __syncthreads();
+      have = false;
+    }
+    const Inst& I = T[inst];
+    const int64_t tiles_m = snt[0].tiles, tiles = tiles_m + snt[1].tiles;
+    auto where = [&](int64_t cc, int& net, int64_t& lt) {  // network and net-local tile of chunk cc
+      const int64_t t = (cc - s_chunk0[inst]) * NW + warp;
+      net = t < tiles_m ? 0 : 1;
+      lt = net ? t - tiles_m : t;
+      return t;
+    };
+    int net;
+    int64_t lt;
+    const int64_t tile = where(c, net, lt);
+    const NetTiles nt = nt_of(net);
+    if (!have) issue_tile<MODE>(I.w, nt, net, lt, tile < tiles, stage0 + sidx * Lay::kStageFloats, lane);
+    // the next chunk of this CTA, when it is in the same instance: its copies run under this tile
+    const int64_t c2 = c + 1;
+    have = c2 < c_end && c2 < s_chunk0[inst + 1];
+    {
+      int net2 = 0;
+      int64_t lt2 = 0;
+      const int64_t t2 = have ? where(c2, net2, lt2) : tiles;
+      issue_tile<MODE>(I.w, nt_of(net2), net2, lt2, t2 < tiles, stage0 + (sidx ^ 1) * Lay::kStageFloats, lane);
+    }
+    cp_wait<1>();  // this chunk's copies have landed
+    __syncwarp();
+    if (tile < tiles) {
+      if (BWD && net != cur) {
+        if (cur >= 0) {
+          flush_acc<N>(sm + Cta::kAcc + cur * Cta::kAccStride, acc, lane);
+          acc.clear();
+        }
+        cur = net;
+      }
+      const float hh[3] = {I.rec.h[0], I.rec.h[1], I.rec.h[2]};
+      do_tile<N, MODE>(I.w, hh, nt, net, lt, sm + net * Lay::kNetW, wp, stage0 + sidx * Lay::kStageFloats, acc, lane,
+                       net ? lsum1 : lsum0, nullptr);
+    }
+  }
+  cp_wait<0>();
+  if (inst >= 0) leave();
 }
 
 }  // namespace tile

@@ -15,6 +15,8 @@
 
 #include <math.h>
 
+#include <vector>
+
 #include "residual_common.cuh"
 
 namespace dips {
@@ -109,10 +111,11 @@ __device__ __forceinline__ void block_scan4(const int64_t v[4], int64_t ex[4], i
 }
 
 // A point is "bulk" when it has exactly 7 jobs (its stencil points, no cube vertices) all of
-// one network; the fused kernel handles it.
-__global__ void k_count(const int32_t* __restrict__ ids, int64_t B, int64_t n_pts, const int32_t* __restrict__ cnt,
-                        const int32_t* __restrict__ cnt_m, int bulk_ok, Workspace w) {
-  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+// one network; the fused kernel handles it.  bx: this block's index within the instance.
+__device__ __forceinline__ void count_body(const int32_t* __restrict__ ids, int64_t B, int64_t n_pts,
+                                           const int32_t* __restrict__ cnt, const int32_t* __restrict__ cnt_m,
+                                           int bulk_ok, const Workspace& w, int bx) {
+  const int64_t b = bx * (int64_t)blockDim.x + threadIdx.x;
   int64_t v[4] = {0, 0, 0, 0};  // bulk u-, bulk u+, general u- jobs, general u+ jobs
   if (b < B) {
     const int64_t pid = batch_pid(ids, b);
@@ -141,10 +144,22 @@ __global__ void k_count(const int32_t* __restrict__ ids, int64_t B, int64_t n_pt
     w.op[b] = ex[3];
   }
   if (threadIdx.x == 0)
-    for (int k = 0; k < 4; ++k) w.blk[4 * blockIdx.x + k] = tot[k];
+    for (int k = 0; k < 4; ++k) w.blk[4 * bx + k] = tot[k];
 }
 
-__global__ void k_scan_blocks(Workspace w) {
+__global__ void k_count(const int32_t* __restrict__ ids, int64_t B, int64_t n_pts, const int32_t* __restrict__ cnt,
+                        const int32_t* __restrict__ cnt_m, int bulk_ok, const __grid_constant__ Workspace w) {
+  count_body(ids, B, n_pts, cnt, cnt_m, bulk_ok, w, blockIdx.x);
+}
+
+// instance blockIdx.y of the table
+__global__ void k_count_multi(const Inst* __restrict__ T, int bulk_ok) {
+  const Inst& I = T[blockIdx.y];
+  if ((int64_t)blockIdx.x >= I.w.nblk) return;
+  count_body(I.ids, I.B, I.rec.n_pts, I.rec.cnt, I.rec.cnt_m, bulk_ok, I.w, blockIdx.x);
+}
+
+__device__ __forceinline__ void scan_body(const Workspace& w) {
   int64_t carry[4] = {0, 0, 0, 0};
   for (int64_t base = 0; base < w.nblk; base += blockDim.x) {
     const int64_t i = base + threadIdx.x;
@@ -177,6 +192,11 @@ __global__ void k_scan_blocks(Workspace w) {
     w.ctl->total = over ? 0 : jm_pad + jp;
   }
 }
+
+__global__ void k_scan_blocks(const __grid_constant__ Workspace w) { scan_body(w); }
+
+// one block per instance
+__global__ void k_scan_blocks_multi(const Inst* __restrict__ T) { scan_body(T[blockIdx.x].w); }
 
 // Record of bulk point pid (network net): point, lhs0, the coefficient of each of its 7
 // stencil jobs in stencil order, diag, rod (layout kRec*; the slot and padding are zero).
@@ -219,8 +239,9 @@ __global__ void k_pack_bulk(dips_records_t rec, float* __restrict__ out) {
   }
 }
 
-__global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, dips_records_t rec, Workspace w) {
-  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void emit_body(const int32_t* __restrict__ ids, int64_t B, const dips_records_t& rec,
+                                          const Workspace& w, int bx) {
+  const int64_t b = bx * (int64_t)blockDim.x + threadIdx.x;
   if (w.ctl->overflow) return;
   const int64_t jm = w.ctl->jm, jm_pad = w.ctl->jm_pad;
   if (b == 0) {  // padding jobs between the u- and u+ segments
@@ -235,7 +256,7 @@ __global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, dips_records_
   const int kind = b < B ? w.bk[b] : 3;
   if (kind == 1 || kind == 2) {
     const int net = kind - 1;
-    const int64_t pos = net * B + w.ob[b] + w.blk[4 * blockIdx.x + net];
+    const int64_t pos = net * B + w.ob[b] + w.blk[4 * bx + net];
     w.bulk[pos] = (int32_t)b;
     // the point's record, so that the tile engine reads one contiguous 64-byte block
     const int64_t pid = batch_pid(ids, b);
@@ -266,8 +287,8 @@ __global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, dips_records_
   float p0 = 0.0f, p1 = 0.0f, p2 = 0.0f;
   if (gen) {
     const int64_t pid = batch_pid(ids, b);
-    om = w.om[b] + w.blk[4 * blockIdx.x + 2];
-    op = w.op[b] + w.blk[4 * blockIdx.x + 3] + jm_pad;
+    om = w.om[b] + w.blk[4 * bx + 2];
+    op = w.op[b] + w.blk[4 * bx + 3] + jm_pad;
     w.om[b] = om;
     w.op[b] = op;
     cm = w.cm[b];
@@ -304,6 +325,17 @@ __global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, dips_records_
   }
 }
 
+__global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, const __grid_constant__ dips_records_t rec,
+                       const __grid_constant__ Workspace w) {
+  emit_body(ids, B, rec, w, blockIdx.x);
+}
+
+__global__ void k_emit_multi(const Inst* __restrict__ T) {
+  const Inst& I = T[blockIdx.y];
+  if ((int64_t)blockIdx.x >= I.w.nblk) return;
+  emit_body(I.ids, I.B, I.rec, I.w, blockIdx.x);
+}
+
 // ----------------------------------------------------------------------------------------
 // residual and loss of the general points
 // ----------------------------------------------------------------------------------------
@@ -330,9 +362,9 @@ __device__ __forceinline__ double block_sum_d(double v) {
 // for its jobs.
 constexpr int kMaxJobRounds = (kStencil * kCube + 31) / 32;  // a point's jobs over 32 lanes
 
-__global__ void k_residual(const int32_t* __restrict__ ids, int64_t B, dips_records_t rec, Workspace w,
-                           float* __restrict__ residual_out) {
-  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void residual_body(const int32_t* __restrict__ ids, int64_t B, const dips_records_t& rec,
+                                              const Workspace& w, float* __restrict__ residual_out, int bx) {
+  const int64_t b = bx * (int64_t)blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool overflow = w.ctl->overflow != 0;
   const int kind = b < B ? (overflow ? 3 : w.bk[b]) : -1;
@@ -397,7 +429,18 @@ __global__ void k_residual(const int32_t* __restrict__ ids, int64_t B, dips_reco
     }
   }
   const double t = block_sum_d(l);
-  if (threadIdx.x == 0) w.lossp[blockIdx.x] = t;
+  if (threadIdx.x == 0) w.lossp[bx] = t;
+}
+
+__global__ void k_residual(const int32_t* __restrict__ ids, int64_t B, const __grid_constant__ dips_records_t rec,
+                           const __grid_constant__ Workspace w, float* __restrict__ residual_out) {
+  residual_body(ids, B, rec, w, residual_out, blockIdx.x);
+}
+
+__global__ void k_residual_multi(const Inst* __restrict__ T) {
+  const Inst& I = T[blockIdx.y];
+  if ((int64_t)blockIdx.x >= I.w.nres) return;
+  residual_body(I.ids, I.B, I.rec, I.w, nullptr, blockIdx.x);
 }
 
 __global__ void k_loss_final(Workspace w, int64_t B, double* __restrict__ loss_out) {
@@ -537,15 +580,15 @@ __global__ void k_adam(dips_adam_t hp, int P, float* __restrict__ params, const 
 // partial rows, the rows split over its 32 warps (a few loads per thread instead of a
 // latency-bound column walk), and adds up the squares of its columns; the last block to finish
 // writes the loss (as k_loss_final) and applies the optax chain to all P parameters.
-__global__ void __launch_bounds__(kReduceThreads) k_reduce_adam(Workspace w, int P, int Pm, int Psol,
-                                                                float* __restrict__ grad, dips_adam_t hp,
-                                                                float* __restrict__ params, float* __restrict__ mu,
-                                                                float* __restrict__ nu, int64_t* __restrict__ count,
-                                                                int64_t B, double* __restrict__ loss_out) {
+__device__ __forceinline__ void reduce_adam_body(const Workspace& w, int P, int Pm, int Psol, float* __restrict__ grad,
+                                                 const dips_adam_t& hp, float* __restrict__ params,
+                                                 float* __restrict__ mu, float* __restrict__ nu,
+                                                 int64_t* __restrict__ count, int64_t B, double* __restrict__ loss_out,
+                                                 int bx, int nb) {
   __shared__ float part[32][33];
   __shared__ bool s_last;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int i = blockIdx.x * 32 + tx;
+  const int i = bx * 32 + tx;
   const bool err = w.ctl->engine_error != 0;
   float v = 0.0f;
   if (i < P) {
@@ -571,10 +614,10 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce_adam(Workspace w, int
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
     if (tx == 0) {
-      w.sqp[blockIdx.x] = sq;
+      w.sqp[bx] = sq;
       __threadfence();
       const unsigned long long n = atomicAdd(reinterpret_cast<unsigned long long*>(&w.ctl->reduce_done), 1ull);
-      s_last = n == gridDim.x - 1;
+      s_last = n == (unsigned long long)(nb - 1);
     }
   }
   __syncthreads();
@@ -586,7 +629,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce_adam(Workspace w, int
   for (int net = 0; net < 2; ++net)
     for (int64_t k = threadIdx.x; k < w.ctl->floss_n[net]; k += blockDim.x) l += w.floss[net * kLossSlots + k];
   double g2 = 0.0;
-  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) g2 += __ldcg(w.sqp + k);
+  for (int k = threadIdx.x; k < nb; k += blockDim.x) g2 += __ldcg(w.sqp + k);
   const double lt = block_sum_d(l);
   const double gt = block_sum_d(g2);
   if (threadIdx.x == 0 && loss_out) *loss_out = err ? nan("") : lt / (double)B;
@@ -594,6 +637,21 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce_adam(Workspace w, int
   if (threadIdx.x == 0) s_g2 = (float)gt;
   __syncthreads();
   adam_update(hp, P, s_g2, params, grad, mu, nu, count);
+}
+
+__global__ void __launch_bounds__(kReduceThreads) k_reduce_adam(const __grid_constant__ Workspace w, int P, int Pm,
+                                                                int Psol, float* __restrict__ grad, dips_adam_t hp,
+                                                                float* __restrict__ params, float* __restrict__ mu,
+                                                                float* __restrict__ nu, int64_t* __restrict__ count,
+                                                                int64_t B, double* __restrict__ loss_out) {
+  reduce_adam_body(w, P, Pm, Psol, grad, hp, params, mu, nu, count, B, loss_out, blockIdx.x, gridDim.x);
+}
+
+__global__ void __launch_bounds__(kReduceThreads) k_reduce_adam_multi(const Inst* __restrict__ T, int P, int Pm,
+                                                                      int Psol, dips_adam_t hp) {
+  const Inst& I = T[blockIdx.y];
+  reduce_adam_body(I.w, P, Pm, Psol, I.grad, hp, I.params, I.mu, I.nu, I.count, I.B, I.loss_out, blockIdx.x,
+                   gridDim.x);
 }
 
 // ----------------------------------------------------------------------------------------
@@ -637,9 +695,9 @@ __global__ void k_batch_ids(int64_t n, uint64_t key, int half, int64_t start, in
 // batch ids from a device step counter (graph-replay friendly): step = *counter,
 // batch = step % nb, epoch = step / nb.  mode 0: consecutive ranges (the reference's fixed
 // sequential batches, data_management.py:104-159); mode 1: a per-epoch seeded permutation.
-__global__ void k_batch_ids_dev(int64_t n, int64_t B, int64_t nb, uint64_t seed, int mode, int half,
-                                const int64_t* __restrict__ counter, int32_t* __restrict__ ids) {
-  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void batch_ids_body(int64_t n, int64_t B, int64_t nb, uint64_t seed, int mode, int half,
+                                               const int64_t* __restrict__ counter, int32_t* __restrict__ ids,
+                                               int64_t b) {
   if (b >= B) return;
   const int64_t step = *counter;
   const int64_t bi = step % nb, epoch = step / nb;
@@ -654,6 +712,18 @@ __global__ void k_batch_ids_dev(int64_t n, int64_t B, int64_t nb, uint64_t seed,
     if (v < (uint64_t)n) break;
   }
   ids[b] = (int32_t)v;
+}
+
+__global__ void k_batch_ids_dev(int64_t n, int64_t B, int64_t nb, uint64_t seed, int mode, int half,
+                                const int64_t* __restrict__ counter, int32_t* __restrict__ ids) {
+  batch_ids_body(n, B, nb, seed, mode, half, counter, ids, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
+__global__ void k_batch_ids_multi(const Inst* __restrict__ T) {
+  const Inst& I = T[blockIdx.y];
+  if (I.ids_mode < 0) return;
+  batch_ids_body(I.rec.n_pts, I.B, I.n_batches, I.seed, I.ids_mode, I.ids_half, I.count, I.ids,
+                 blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
 }
 
 // ----------------------------------------------------------------------------------------
@@ -967,6 +1037,82 @@ extern "C" int dips_autotune(const dips_arch_t* arch, const float* params, const
     if (st) return st;
   }
   if (choice_out) *choice_out = chosen;
+  return DIPS_OK;
+}
+
+extern "C" size_t dips_instances_table_bytes(int32_t n) { return n > 0 ? sizeof(Inst) * (size_t)n : 0; }
+
+static int feistel_half(int64_t n) {
+  int bits = 1;
+  while ((1ll << bits) < n) ++bits;
+  return (bits + 1) / 2;
+}
+
+extern "C" int dips_instances_prepare(const dips_arch_t* arch, const dips_instance_t* inst, int32_t n, void* table,
+                                      size_t table_bytes, cudaStream_t stream) {
+  DIPS_REQUIRE(arch && inst && table && n > 0 && n <= 256, DIPS_E_ARG, "dips_instances_prepare: bad argument");
+  DIPS_REQUIRE(table_bytes >= sizeof(Inst) * (size_t)n, DIPS_E_WORKSPACE, "dips_instances_prepare: table too small");
+  const ArchOps* ops = find_arch(arch);
+  if (!ops) return DIPS_E_UNSUPPORTED;
+  std::vector<Inst> host((size_t)n);
+  for (int i = 0; i < n; ++i) {
+    const dips_instance_t& d = inst[i];
+    int st = check_rec(d.rec, d.batch);
+    if (st) return st;
+    DIPS_REQUIRE(d.params && d.mu && d.nu && d.count && d.batch_ids, DIPS_E_ARG,
+                 "dips_instances_prepare: instance %d: null pointer", i);
+    DIPS_REQUIRE(d.ids_mode >= -1 && d.ids_mode <= 1, DIPS_E_ARG, "dips_instances_prepare: instance %d: ids_mode", i);
+    if (d.ids_mode >= 0)
+      DIPS_REQUIRE(d.n_batches > 0 && d.n_batches * d.batch <= d.rec->n_pts && d.rec->n_pts <= 0x7fffffff, DIPS_E_ARG,
+                   "dips_instances_prepare: instance %d: %lld batches of %lld exceed n=%lld", i,
+                   (long long)d.n_batches, (long long)d.batch, (long long)d.rec->n_pts);
+    Inst& I = host[(size_t)i];
+    st = prep_ws(arch, d.params, d.batch, d.workspace, d.ws_bytes, &I.w);
+    if (st) return st;
+    I.rec = *d.rec;
+    I.ids = d.batch_ids;
+    I.B = d.batch;
+    I.n_batches = d.n_batches;
+    I.seed = d.seed;
+    I.ids_mode = d.ids_mode;
+    I.ids_half = feistel_half(d.rec->n_pts);
+    I.params = d.params;
+    I.mu = d.mu;
+    I.nu = d.nu;
+    I.count = d.count;
+    I.grad = d.grad_out ? d.grad_out : I.w.grad;
+    I.loss_out = d.loss_out;
+  }
+  cudaError_t e = cudaMemcpyAsync(table, host.data(), sizeof(Inst) * (size_t)n, cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  return e == cudaSuccess ? DIPS_OK : cuda_status(e, "dips_instances_prepare: table copy");
+}
+
+extern "C" int dips_train_step_instances(const dips_arch_t* arch, const dips_adam_t* hp, const void* table, int32_t n,
+                                         int64_t max_batch, cudaStream_t stream) {
+  DIPS_REQUIRE(arch && hp && table && n > 0 && n <= 256 && max_batch > 0 && max_batch <= 0x7fffffff, DIPS_E_ARG,
+               "dips_train_step_instances: bad argument");
+  const ArchOps* ops = find_arch(arch);
+  if (!ops) return DIPS_E_UNSUPPORTED;
+  DIPS_REQUIRE(ops->multi_forward && ops->multi_train && arch->pre_layers == 0, DIPS_E_UNSUPPORTED,
+               "dips_train_step_instances: needs a tile-engine shape (3x32, 2x16) without the preconditioner");
+  const Inst* T = static_cast<const Inst*>(table);
+  const int nblk = div_up(max_batch, kScanBlock), nres = div_up(max_batch, 256);
+  k_batch_ids_multi<<<dim3(div_up(max_batch, 256), n), 256, 0, stream>>>(T);
+  k_count_multi<<<dim3(nblk, n), kScanBlock, 0, stream>>>(T, ops->bulk_ok);
+  k_scan_blocks_multi<<<n, kScanBlock, 0, stream>>>(T);
+  k_emit_multi<<<dim3(nblk, n), kScanBlock, 0, stream>>>(T);
+  DIPS_CHECK_LAUNCH("dips_train_step_instances expansion");
+  int st = ops->multi_forward(T, n, stream);
+  if (st) return st;
+  k_residual_multi<<<dim3(nres, n), 256, 0, stream>>>(T);
+  DIPS_CHECK_LAUNCH("dips_train_step_instances residual");
+  st = ops->multi_train(T, n, stream);
+  if (st) return st;
+  const int Pm = ops->n_params - net_params(ops->p_layers, ops->p_width);
+  const int P = ops->n_params;
+  k_reduce_adam_multi<<<dim3(div_up(P, 32), n), kReduceThreads, 0, stream>>>(T, P, Pm, ops->n_params, *hp);
+  DIPS_CHECK_LAUNCH("dips_train_step_instances gradient tail");
   return DIPS_OK;
 }
 

@@ -553,6 +553,8 @@ static int tile_launch_nw(const PtsH& ph, const int32_t* ids, const Workspace& w
     attr_done = true;
   }
   constexpr int ctas_per_sm = tile::warps_per_sm<N>() / NW;
+  static_assert(kTileGrid * ctas_per_sm <= kLossSlots && kTileGrid * ctas_per_sm <= kAdjGrid + kFusedGrid,
+                "tile engine: more CTAs than loss slots or partial gradient rows");
   static_assert(ctas_per_sm * (bytes + 1024) <= 228 * 1024, "tile engine: CTAs per SM do not fit in shared memory");
   tile::k_tile<N, MODE, NW><<<kTileGrid * ctas_per_sm, 32 * NW, bytes, s>>>(ph, ids, w, rec, A::kOffP, residual_out);
   return DIPS_OK;
@@ -572,6 +574,56 @@ static int tile_launch(const PtsH& ph, const int32_t* ids, const Workspace& w, c
     ::dips::set_error("tile engine: network shape without the engine");
     return DIPS_E_UNSUPPORTED;
   }
+}
+
+template <class N, int MODE, int NW>
+static int tile_multi_launch_nw(const Inst* T, int n, cudaStream_t s) {
+  constexpr size_t bytes = tile::CtaLayout<N, NW>::kBytes;
+  constexpr int ctas_per_sm = tile::warps_per_sm<N>() / NW;
+  constexpr size_t static_bytes = sizeof(int64_t) * (tile::kMaxInstances + 2) + 2 * sizeof(tile::NetTiles);
+  static_assert(ctas_per_sm * (bytes + static_bytes + 1024) <= 228 * 1024,
+                "multi-instance tile engine: CTAs per SM do not fit in shared memory");
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(tile::k_tile_multi<N, MODE, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)bytes);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(multi-instance tile engine smem)");
+    attr_done = true;
+  }
+  tile::k_tile_multi<N, MODE, NW><<<kTileGrid * ctas_per_sm, 32 * NW, bytes, s>>>(T, n, A::kOffP);
+  return DIPS_OK;
+}
+
+template <int MODE, bool TILE = kTileArch>
+static int tile_multi(const Inst* T, int n, cudaStream_t s) {
+  if constexpr (TILE) {
+    using N = typename A::M;
+    if (n > tile::kMaxInstances) {
+      ::dips::set_error("multi-instance step: %d instances, at most %d per launch", n, tile::kMaxInstances);
+      return DIPS_E_ARG;
+    }
+    const int nw = tile_nw();
+    if (nw == kTileCand[1]) return tile_multi_launch_nw<N, MODE, kTileCand[1]>(T, n, s);
+    if (nw == kTileCand[2]) return tile_multi_launch_nw<N, MODE, kTileCand[2]>(T, n, s);
+    return tile_multi_launch_nw<N, MODE, kTileCand[0]>(T, n, s);
+  } else {
+    ::dips::set_error("multi-instance step: network shape without the tile engine");
+    return DIPS_E_UNSUPPORTED;
+  }
+}
+
+static int multi_forward(const Inst* T, int n, cudaStream_t s) {
+  const int st = tile_multi<tile::kForwardGeneral>(T, n, s);
+  if (st) return st;
+  DIPS_CHECK_LAUNCH("multi-instance general forward");
+  return DIPS_OK;
+}
+
+static int multi_train(const Inst* T, int n, cudaStream_t s) {
+  const int st = tile_multi<tile::kTrain>(T, n, s);
+  if (st) return st;
+  DIPS_CHECK_LAUNCH("multi-instance training launch");
+  return DIPS_OK;
 }
 
 static int job_forward(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s) {
@@ -719,7 +771,9 @@ const ArchOps* DIPS_GETTER() {
                               1,
                               DIPS_NS::load_params,
                               DIPS_NS::job_forward, DIPS_NS::job_adjoint, DIPS_NS::bulk_fused,
-                              DIPS_NS::mlp_eval, DIPS_NS::autotune};
+                              DIPS_NS::mlp_eval, DIPS_NS::autotune,
+                              DIPS_NS::kTileArch ? DIPS_NS::multi_forward : nullptr,
+                              DIPS_NS::kTileArch ? DIPS_NS::multi_train : nullptr};
   return &ops;
 }
 

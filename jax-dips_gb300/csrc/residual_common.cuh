@@ -12,7 +12,7 @@ constexpr int kAdjGrid = 152 * 2;    // two adjoint CTAs per SM (GB300 has 152 S
 constexpr int kFusedThreads = 224;   // fused bulk CTA: one warp per stencil point
 constexpr int kFusedGrid = 152 * 2;
 constexpr int kTileGrid = 152;  // register-blocked engine: 12 warps per SM (one CTA of 12 by default)
-constexpr int kLossSlots = 512;  // per-network capacity of the per-CTA loss partials
+constexpr int kLossSlots = 1024;  // per-network capacity of the per-CTA loss partials
 constexpr int kPreGrid = 304;    // CTAs of the preconditioner's backward (partial rows)
 constexpr int kPreIn = 26;       // preconditioner input: the cell coefficients
 
@@ -73,6 +73,26 @@ struct PtsH {
   float h[3];
 };
 
+// One problem of a multi-instance step (many instances trained together, one launch per phase
+// for all of them): what its kernels need, in a device table that the per-step kernels index
+// with blockIdx.y and the persistent tile launch walks.
+struct Inst {
+  Workspace w;        // carved from the instance's workspace; w.params = its parameters
+  dips_records_t rec;  // its level
+  int32_t* ids;       // [B] batch ids (drawn on the device when ids_mode >= 0)
+  int64_t B;
+  int64_t n_batches;  // batches per epoch, for ids drawn from *count
+  uint64_t seed;
+  int32_t ids_mode;   // -1: ids given; 0: consecutive ranges; 1: seeded permutation per epoch
+  int32_t ids_half;   // half-width of the permutation's Feistel network
+  float* params;
+  float* mu;
+  float* nu;
+  int64_t* count;
+  float* grad;        // [P] (the workspace's when the caller gave none)
+  double* loss_out;   // device double, may be NULL
+};
+
 __device__ __forceinline__ int64_t batch_pid(const int32_t* ids, int64_t b) { return ids ? (int64_t)ids[b] : b; }
 
 __device__ __forceinline__ void job_point(const PtsH& ph, const int32_t* ids, int32_t slot, uint16_t code, float x[3]) {
@@ -126,6 +146,10 @@ struct ArchOps {
   // fastest for the current device (NULL: nothing to tune); *chosen = the choice (0: none)
   int (*autotune)(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec, cudaStream_t s,
                   int* chosen);
+  // multi-instance step (tile-engine shapes; NULL otherwise): the general forward and the
+  // training launch of every instance of the device table T[0..n) in one persistent launch
+  int (*multi_forward)(const Inst* T, int n, cudaStream_t s);
+  int (*multi_train)(const Inst* T, int n, cudaStream_t s);
 };
 
 // learned preconditioner (implemented in precond.cu)

@@ -664,7 +664,8 @@ static int mlp_eval(const float* pts, const float* phi, int64_t n, float* u, flo
 
 const ArchOps* arch_ops_4_64_4_64() {
   static const ArchOps ops = {4, 64, 4, 64, tcnet::kParams, 0, tcnet::load_params, tcnet::job_forward,
-                              tcnet::job_adjoint, tcnet::bulk_fused, tcnet::mlp_eval, nullptr};
+                              tcnet::job_adjoint, tcnet::bulk_fused, tcnet::mlp_eval, nullptr, nullptr,
+                              nullptr};
   return &ops;
 }
 

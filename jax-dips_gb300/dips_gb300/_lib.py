@@ -180,6 +180,25 @@ class AdamT(ctypes.Structure):
     _fields_ = [(n, c_f32) for n in ("lr", "decay_rate", "transition_steps", "max_norm", "b1", "b2", "eps")]
 
 
+class InstanceT(ctypes.Structure):
+    _fields_ = [
+        ("rec", ctypes.c_void_p),
+        ("batch_ids", c_void_p),
+        ("batch", c_i64),
+        ("n_batches", c_i64),
+        ("seed", ctypes.c_uint64),
+        ("ids_mode", c_i32),
+        ("params", c_void_p),
+        ("mu", c_void_p),
+        ("nu", c_void_p),
+        ("count", c_void_p),
+        ("workspace", c_void_p),
+        ("ws_bytes", ctypes.c_size_t),
+        ("loss_out", c_void_p),
+        ("grad_out", c_void_p),
+    ]
+
+
 class KrylovStatsT(ctypes.Structure):
     _fields_ = [("iterations", c_i32), ("target_iteration", c_i32), ("breakdown", c_i32),
                 ("rel_residual", ctypes.c_double), ("rel_linf", c_f32)]
@@ -220,6 +239,9 @@ _SIGS = {
          c_void_p],
     ),
     "dips_pack_bulk_records": (c_i32, [P(RecordsT), c_void_p, c_void_p]),
+    "dips_instances_table_bytes": (ctypes.c_size_t, [c_i32]),
+    "dips_instances_prepare": (c_i32, [P(ArchT), P(InstanceT), c_i32, c_void_p, ctypes.c_size_t, c_void_p]),
+    "dips_train_step_instances": (c_i32, [P(ArchT), P(AdamT), c_void_p, c_i32, c_i64, c_void_p]),
     "dips_num_params": (c_i32, [P(ArchT)]),
     "dips_arch_supported": (c_i32, [P(ArchT)]),
     "dips_step_workspace_bytes": (ctypes.c_size_t, [P(ArchT), c_i64, c_i64]),

@@ -2,14 +2,19 @@
 
 Each instance has its own level set, residual records, network parameters, Adam state and step
 workspace (the reference trains one problem per ``Trainer``; examples/benchmark_LPBE runs its
-molecules one by one).  ``InstanceBatch`` captures the training steps of all instances in one
-CUDA graph, so that a batched step is one graph launch: the batch-id kernel and the fused
-training step of every instance.  The instances share nothing on the GPU, so they are dealt,
-largest first, over several capture streams; the graph keeps them as independent chains that
-the GPU runs side by side, which fills the SMs that one small instance leaves idle.
+molecules one by one).  ``InstanceBatch`` trains them together and captures the batched step in
+one CUDA graph, so that a batched step is one graph launch.
+
+For the tile-engine shapes (3x32, 2x16) the step is ``dips_train_step_instances``: one launch
+per phase for all instances over a device table of the instances (batch ids, expansion, general
+forward, general residual, training launch, gradient tail), the two tile-engine launches
+persistent over every instance's tiles.  Other shapes run one ``dips_train_step`` per instance,
+dealt largest first over several capture streams, which the GPU runs side by side.
 """
 
 from __future__ import annotations
+
+import ctypes
 
 import numpy as np
 import torch
@@ -48,7 +53,7 @@ class InstanceBatch:
     """
 
     def __init__(self, instances, arch: nn.Arch, batch: int = 1 << 15, lr: float = 1e-3, seed: int = 0,
-                 device="cuda", streams: int = 8):
+                 device="cuda", streams: int = 8, persistent=None):
         if not torch.cuda.is_available():
             raise RuntimeError("dips_gb300 runs on a CUDA GPU; none is available")
         lib = _lib.load()
@@ -61,6 +66,53 @@ class InstanceBatch:
         self.losses = torch.zeros(len(self.items), dtype=torch.float64, device=device)
         self.streams = [torch.cuda.Stream(device=device) for _ in range(max(1, int(streams)))]
         self.graph = None
+        tile = (arch.m_layers, arch.m_width) == (arch.p_layers, arch.p_width) and \
+            (arch.m_layers, arch.m_width) in ((2, 16), (3, 32)) and arch.pre_layers == 0
+        self.persistent = tile if persistent is None else bool(persistent)
+        if self.persistent and not tile:
+            raise NotImplementedError("the persistent multi-instance step needs a 3x32 or 2x16 shape")
+        self.max_batch = max(it.batch for it in self.items)
+        self._tables = {}
+        if self.persistent:
+            self._table(ids_mode=1)
+
+    def _table(self, ids_mode: int):
+        """The device table of the instances (batch ids drawn on the device, ids_mode 1, or
+        given by the caller, -1), prepared once."""
+        if ids_mode in self._tables:
+            return self._tables[ids_mode]
+        lib = _lib.load()
+        n = len(self.items)
+        arr = (_lib.InstanceT * n)()
+        for i, it in enumerate(self.items):
+            arr[i] = _lib.InstanceT(
+                ctypes.addressof(it.level.desc), _lib.ptr(it.ids), it.batch, it.n_batches, it.seed, ids_mode,
+                _lib.ptr(it.params), _lib.ptr(it.opt.mu), _lib.ptr(it.opt.nu), _lib.ptr(it.opt.count),
+                _lib.ptr(it.ws.buf), it.ws.nbytes, _lib.ptr(self.losses[i:i + 1]), None)
+        nbytes = int(lib.dips_instances_table_bytes(n))
+        table = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        _lib.check(lib.dips_instances_prepare(self.arch.ctype(), arr, n, _lib.ptr(table), nbytes,
+                                              _lib.stream_handle()), "dips_instances_prepare")
+        self._tables[ids_mode] = table
+        return table
+
+    def _step_persistent(self, ids_mode: int = 1):
+        lib = _lib.load()
+        _lib.check(lib.dips_train_step_instances(self.arch.ctype(), self.items[0].opt.hp,
+                                                 _lib.ptr(self._table(ids_mode)), len(self.items), self.max_batch,
+                                                 _lib.stream_handle()), "dips_train_step_instances")
+
+    def step_with_ids(self):
+        """One step of every instance on the batch ids already in each instance's ``ids`` (e.g.
+        copied from the host), without a graph."""
+        if self.persistent:
+            self._step_persistent(ids_mode=-1)
+            return self.losses
+        for i in self.order:
+            it = self.items[i]
+            ops.train_step(self.arch, it.params, it.opt, it.level, it.ids, it.ws, it.loss)
+            self.losses[i : i + 1].copy_(it.loss.reshape(1))
+        return self.losses
 
     def _step_one(self, i):
         lib = _lib.load()
@@ -71,8 +123,12 @@ class InstanceBatch:
         self.losses[i : i + 1].copy_(it.loss.reshape(1))
 
     def _step_all(self):
-        """Every instance's step, dealt over the side streams (fork from and join to the current
-        stream, so that the whole batched step is ordered like one launch)."""
+        """Every instance's step: the persistent multi-instance step, or one step per instance
+        dealt over the side streams (fork from and join to the current stream, so that the whole
+        batched step is ordered like one launch)."""
+        if self.persistent:
+            self._step_persistent()
+            return
         main = torch.cuda.current_stream()
         for s in self.streams:
             s.wait_stream(main)
@@ -118,6 +174,8 @@ class InstanceBatch:
         expansion (3), the general forward, the general residual, the bulk training launch and
         the gradient tail (reduction, loss, Adam); shapes off the tile engine launch the forward,
         the bulk kernel and the adjoint once per network.  (A loss copy per instance is torch's.)"""
+        if self.persistent:  # one launch per phase for all instances
+            return 8
         a = self.arch
         tile = (a.m_layers, a.m_width) == (a.p_layers, a.p_width) and (a.m_layers, a.m_width) in ((2, 16), (3, 32))
         return (8 if tile else 12) * len(self.items)
