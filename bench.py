@@ -353,6 +353,28 @@ def run_ours(args, rank, world):
                                          "MEASURED_PEAKS.json has no FP32 figure")
     step_tflops = 3 * fwd_flops / (t_total / args.steps) / 1e12
 
+    # ---- evaluate_solution_and_gradients's kernel (dips_mlp_eval: u and grad u) on a 256^3
+    # evaluation grid, both networks chosen by the sign of phi
+    evaluation = None
+    if rank == 0:
+        ne = 256 ** 3
+        gen = torch.Generator(device=dev).manual_seed(3)
+        epts = torch.rand(ne, 3, device=dev, generator=gen) * 2.0 - 1.0
+        ephi = lvl.ls(epts)
+        nn.mlp_eval(arch, params, epts, ephi, want_grad=True)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(3):
+            nn.mlp_eval(arch, params, epts, ephi, want_grad=True)
+        ev1.record()
+        torch.cuda.synchronize()
+        t_ev = ev0.elapsed_time(ev1) / 3 / 1e3
+        # forward F plus the input-gradient pass (a W^T product per layer: about F again)
+        evaluation = {"points": ne, "ms": 1e3 * t_ev, "pts_per_s": ne / t_ev,
+                      "tflops": 2 * f_p * ne / t_ev / 1e12, "algorithmic": "2 x F per point (u and grad u)",
+                      "kernel": "k_mlp_eval (one thread per point, weights as constant-bank operands)"}
+        del epts, ephi
+
     # ---- e2e through the public API with host buffers
     host_ids = torch.empty(B, dtype=torch.int32).pin_memory()
     host_loss = torch.empty((), dtype=torch.float64).pin_memory()
@@ -416,6 +438,8 @@ def run_ours(args, rank, world):
                          "algorithmic": f"3 x F per job, F = sum(2*in*out+out) + tanh count = "
                                         f"{dom_f}; {dom_jobs} jobs per launch (bulk points: {bulk_m} u-, {bulk_p} u+)",
                          "peak_source": peak_src, "fp32_peak_tflops": fp32_peak,
+                         "fp32_peak_nominal_tflops": torch.cuda.get_device_properties(dev).multi_processor_count
+                                                     * 128 * 2 * float(clk.get("sm_max_mhz") or 0) * 1e6 / 1e12,
                          "phase_ms": phase_med,
                          "step_tflops": step_tflops, "step_frac": step_tflops / fp32_peak,
                          "step_algorithmic": "3 x F x (all jobs of the batch) per step"},
@@ -424,6 +448,7 @@ def run_ours(args, rank, world):
             "gpu_launches": (10 if tensor else 8) * args.steps,
             "clocks": clk,
             "time_to_target": tta,
+            "evaluation_256": evaluation,
         }
         print(json.dumps(line), flush=True)
 

@@ -35,8 +35,10 @@ def test_instance_batch_graph_matches_independent_steps(arch, persistent):
     torch.cuda.synchronize()
     assert torch.isfinite(lb).all()
     np.testing.assert_allclose(lb.cpu().numpy(), lr.cpu().numpy(), rtol=1e-5)
+    # the weight-gradient sums are added in another order; Adam (lr 1e-3) turns that into
+    # parameter differences of a few 1e-7 on the smallest parameters
     for x, y in zip(b.items, ref.items):
-        np.testing.assert_allclose(x.params.cpu().numpy(), y.params.cpu().numpy(), rtol=1e-4, atol=1e-7)
+        np.testing.assert_allclose(x.params.cpu().numpy(), y.params.cpu().numpy(), rtol=1e-4, atol=2e-6)
     assert b.points_per_step == sum(min(2048, it.level.n) for it in b.items)
 
 
@@ -57,4 +59,4 @@ def test_persistent_step_on_given_ids():
         lr = ref.step_with_ids().clone()
         np.testing.assert_allclose(lb.cpu().numpy(), lr.cpu().numpy(), rtol=1e-5)
     for x, y in zip(b.items, ref.items):
-        np.testing.assert_allclose(x.params.cpu().numpy(), y.params.cpu().numpy(), rtol=1e-4, atol=1e-7)
+        np.testing.assert_allclose(x.params.cpu().numpy(), y.params.cpu().numpy(), rtol=1e-4, atol=2e-6)
