@@ -354,12 +354,12 @@ def run_ours(args, rank, world):
     step_tflops = 3 * fwd_flops / (t_total / args.steps) / 1e12
 
     # ---- evaluate_solution_and_gradients's kernel (dips_mlp_eval: u and grad u) on a 256^3
-    # evaluation grid, both networks chosen by the sign of phi
+    # evaluation grid, each point's network chosen by the sign of phi
     evaluation = None
     if rank == 0:
-        ne = 256 ** 3
-        gen = torch.Generator(device=dev).manual_seed(3)
-        epts = torch.rand(ne, 3, device=dev, generator=gen) * 2.0 - 1.0
+        ne = 256 ** 3  # the evaluation grid's points in 'ij' C order, as eval_gstate.R
+        xs = torch.linspace(-1.0, 1.0, 256, device=dev)
+        epts = torch.stack(torch.meshgrid(xs, xs, xs, indexing="ij"), dim=-1).reshape(-1, 3).contiguous()
         ephi = lvl.ls(epts)
         nn.mlp_eval(arch, params, epts, ephi, want_grad=True)
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -372,7 +372,8 @@ def run_ours(args, rank, world):
         # forward F plus the input-gradient pass (a W^T product per layer: about F again)
         evaluation = {"points": ne, "ms": 1e3 * t_ev, "pts_per_s": ne / t_ev,
                       "tflops": 2 * f_p * ne / t_ev / 1e12, "algorithmic": "2 x F per point (u and grad u)",
-                      "kernel": "k_mlp_eval (one thread per point, weights as constant-bank operands)"}
+                      "kernel": ("tcnet::k_tc_eval" if tensor else "tile::k_tile_eval (32-point tiles, both networks "
+                                 "where a tile straddles the interface)")}
         del epts, ephi
 
     # ---- e2e through the public API with host buffers

@@ -308,13 +308,23 @@ struct Acc {
   }
 };
 
-// One tile: forward of the 32 jobs whose coordinates are in X, then (with BWD) the backward
-// with dL/du from G.  EPI(u[4]) runs between the two: it receives this lane's 4 network
-// values (jobs jc..jc+3) and must leave G filled for the warp (it may synchronise the warp).
-template <class N, bool BWD, class Epi>
-__device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc<N>& acc, int lane, Epi epi) {
+// Backward modes of one tile
+enum TileBwd {
+  kBwdNone = 0,   // forward only
+  kBwdTrain = 1,  // dL/du from G; weight gradients into the accumulators
+  kBwdInput = 2,  // du/dx: the backward with dL/du = 1 down to the input, no weight gradients
+};
+
+// One tile: forward of the 32 jobs whose coordinates are in X, then the backward of mode BM.
+// EPI(u[4]) runs between the two: it receives this lane's 4 network values (jobs jc..jc+3) and,
+// for kBwdTrain, must leave G filled for the warp (it may synchronise the warp).  With
+// kBwdInput, gin[q][c] receives du/dx_c of job jc + q (every lane of the job's block).
+template <class N, int BM, class Epi>
+__device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc<N>& acc, int lane, Epi epi,
+                                         float (&gin)[4][3]) {
   using Lay = Layout<N>;
   constexpr int W = Lay::W, L = Lay::L, NT = Lay::NT;
+  constexpr bool TRAIN = BM == kBwdTrain;
   const int jbl = lane & 7, ob = lane >> 3, jc = 4 * jbl, bc = NT * ob;
   float* X = wp + Lay::kX;
   float* bufA = wp + Lay::kA;
@@ -355,14 +365,18 @@ __device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc<N>& acc
     u[q] = s + bo;
   }
   epi(u);
-  if (!BWD) {
+  if (BM == kBwdNone) {
     __syncwarp();
     return;
   }
   __syncwarp();
-  const float4 g4 = ld4(G + jc);
-  const float gv[4] = {g4.x, g4.y, g4.z, g4.w};
-  {
+  float gv[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+  if constexpr (TRAIN) {
+    const float4 g4 = ld4(G + jc);
+    gv[0] = g4.x;
+    gv[1] = g4.y;
+    gv[2] = g4.z;
+    gv[3] = g4.w;
     float v[NT];
 #pragma unroll
     for (int t = 0; t < NT; ++t) v[t] = fmaf(gv[0], h[0][t], gv[1] * h[1][t]) + fmaf(gv[2], h[2][t], gv[3] * h[3][t]);
@@ -379,15 +393,15 @@ __device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc<N>& acc
   for (int q = 0; q < 4; ++q)
 #pragma unroll
     for (int t = 0; t < NT; ++t) h[q][t] = gv[q] * wo[t] * fmaf(-h[q][t], h[q][t], 1.0f);
-  acc.b[L - 1] += colsum_rs(h, jbl);
+  if constexpr (TRAIN) acc.b[L - 1] += colsum_rs(h, jbl);
   store_blk(dbuf, ob, jc, h);
   __syncwarp();
-  dw(acc.wh[L - 2], hprev, dbuf, jbl, ob);
+  if constexpr (TRAIN) dw(acc.wh[L - 2], hprev, dbuf, jbl, ob);
   // delta_{L-1} = (delta_L W_L^T) (1 - h_{L-1}^2)
   zero_blk(h);
   gemm<W, kRS>(h, dbuf, jc, sm + Lay::kWT + (L - 2) * W * W, bc);
   times_dtanh(h, hprev, ob, jc);
-  acc.b[L - 2] += colsum_rs(h, jbl);
+  if constexpr (TRAIN) acc.b[L - 2] += colsum_rs(h, jbl);
   if constexpr (L == 3) {
     __syncwarp();
     store_blk(bufB, ob, jc, h);  // delta2 over h2
@@ -399,15 +413,15 @@ __device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc<N>& acc
       store_blk(bufA, ob, jc, h1);
     }
     __syncwarp();
-    dw(acc.wh[0], bufA, bufB, jbl, ob);
+    if constexpr (TRAIN) dw(acc.wh[0], bufA, bufB, jbl, ob);
     // delta1 = (delta2 W2^T) (1 - h1^2)
     zero_blk(h);
     gemm<W, kRS>(h, bufB, jc, sm + Lay::kWT, bc);
     times_dtanh(h, bufA, ob, jc);
-    acc.b[0] += colsum_rs(h, jbl);
+    if constexpr (TRAIN) acc.b[0] += colsum_rs(h, jbl);
   }
-  // h = delta1: dW1 += x^T delta1
-  {
+  if constexpr (TRAIN) {
+    // h = delta1: dW1 += x^T delta1
     const float4 x0 = ld4(X + jc), x1 = ld4(X + 32 + jc), x2 = ld4(X + 64 + jc);
     float v[NT];
 #pragma unroll
@@ -419,8 +433,30 @@ __device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc<N>& acc
 #pragma unroll
     for (int t = 0; t < NT; ++t) v[t] = fmaf(x2.x, h[0][t], fmaf(x2.y, h[1][t], fmaf(x2.z, h[2][t], x2.w * h[3][t])));
     acc.w1[2] += rs(v, jbl);
+  } else if constexpr (BM == kBwdInput) {
+    // du/dx_c = sum_f W_1[c][f] delta1_f; the table holds c W_1, scaled for the exp2 tanh
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      float w1[NT];
+      ldrow(w1, sm + Lay::kW1 + c * W + bc);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        float s = 0.0f;
+#pragma unroll
+        for (int t = 0; t < NT; ++t) s = fmaf(h[q][t], w1[t], s);
+        s += __shfl_xor_sync(0xffffffffu, s, 8);
+        s += __shfl_xor_sync(0xffffffffu, s, 16);
+        gin[q][c] = s * (1.0f / kTanhScale);
+      }
+    }
   }
   __syncwarp();  // the next tile overwrites X, G and both buffers
+}
+
+template <class N, bool BWD, class Epi>
+__device__ __forceinline__ void run_tile(const float* sm, float* wp, Acc<N>& acc, int lane, Epi epi) {
+  float unused[4][3];
+  run_tile<N, BWD ? kBwdTrain : kBwdNone>(sm, wp, acc, lane, epi, unused);
 }
 
 // Copy network N's weights (flat layout at params + OFF, global memory) into the CTA's permuted
@@ -877,6 +913,67 @@ __global__ void __launch_bounds__(32 * NW, warps_per_sm<N>() / NW) k_tile_multi(
   }
   cp_wait<0>();
   if (inst >= 0) leave();
+}
+
+// u and du/dx at n points (evaluate_solution_and_gradients, trainer.py:929-977): tiles of 32
+// consecutive points, the network of each point chosen by the sign of phi.  A tile whose points
+// all lie on one side runs that network once; a tile that straddles the interface runs both
+// and keeps each point's own.
+template <class N, int NW>
+__global__ void __launch_bounds__(32 * NW, warps_per_sm<N>() / NW) k_tile_eval(const float* __restrict__ pts,
+                                                                              const float* __restrict__ phi, int64_t n,
+                                                                              const float* __restrict__ params,
+                                                                              int off_p, float* __restrict__ u_out,
+                                                                              float* __restrict__ g_out) {
+  using Lay = Layout<N>;
+  extern __shared__ float4 smem4[];
+  float* sm = reinterpret_cast<float*>(smem4);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  load_weights<N>(sm, params, 0);
+  load_weights<N>(sm + Lay::kNetW, params, off_p);
+  __syncthreads();
+  float* wp = sm + Lay::kWarp0 + warp * Lay::kWarpFloats;
+  float* X = wp + Lay::kX;
+  const int jc = 4 * (lane & 7);
+  const bool lead = (lane >> 3) == 0;
+  Acc<N> unused;
+  const int64_t tiles = (n + 31) / 32;
+  for (int64_t tile = (int64_t)blockIdx.x * NW + warp; tile < tiles; tile += (int64_t)gridDim.x * NW) {
+    const int64_t i = tile * 32 + lane;
+    const bool ok = i < n;
+    X[lane] = ok ? pts[3 * i] : 0.0f;
+    X[32 + lane] = ok ? pts[3 * i + 1] : 0.0f;
+    X[64 + lane] = ok ? pts[3 * i + 2] : 0.0f;
+    const bool side = ok && phi[i] >= 0.0f;
+    const unsigned on_p = __ballot_sync(0xffffffffu, side), on_m = __ballot_sync(0xffffffffu, ok && !side);
+    __syncwarp();
+#pragma unroll 1
+    for (int net = 0; net < 2; ++net) {
+      const unsigned mine = net ? on_p : on_m;
+      if (!mine) continue;
+      float gin[4][3];
+      float uv[4];
+      run_tile<N, kBwdInput>(sm + net * Lay::kNetW, wp, unused, lane,
+                             [&](const float (&u)[4]) {
+#pragma unroll
+                               for (int q = 0; q < 4; ++q) uv[q] = u[q];
+                             },
+                             gin);
+      if (lead) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (!((mine >> (jc + q)) & 1u)) continue;
+          const int64_t j = tile * 32 + jc + q;
+          u_out[j] = uv[q];
+          if (g_out) {
+            g_out[3 * j] = gin[q][0];
+            g_out[3 * j + 1] = gin[q][1];
+            g_out[3 * j + 2] = gin[q][2];
+          }
+        }
+      }
+    }
+  }
 }
 
 }  // namespace tile

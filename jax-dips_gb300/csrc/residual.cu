@@ -1154,5 +1154,5 @@ extern "C" int dips_mlp_eval(const dips_arch_t* arch, const float* params, const
   if (!ops) return DIPS_E_UNSUPPORTED;
   int st = ops->load_params(params, 1, stream);
   if (st) return st;
-  return ops->mlp_eval(pts, phi_at, n, u_out, grad_out, stream);
+  return ops->mlp_eval(params, pts, phi_at, n, u_out, grad_out, stream);
 }

@@ -507,8 +507,9 @@ constexpr bool kTileArch = tile::supported<typename A::M>() && tile::supported<t
 
 static int load_params(const float* params, int for_eval, cudaStream_t s) {
   static_assert(2 * A::kParams <= kMaxConstParams, "network too large for the constant bank");
-  // the tile engine reads the parameters from global memory; only mlp_eval needs the bank
-  if (kTileArch && !for_eval) return DIPS_OK;
+  // the tile engine (training and evaluation) reads the parameters from global memory
+  (void)for_eval;
+  if (kTileArch) return DIPS_OK;
   // two copies: forward-pass operands at 0, backward-pass operands at kParams (with one
   // copy the compiler keeps every weight used by both passes in registers)
   cudaError_t e = cudaMemcpyToSymbolAsync(c_w, params, sizeof(float) * A::kParams, 0, cudaMemcpyDeviceToDevice, s);
@@ -706,7 +707,37 @@ static int bulk_fused(const PtsH& ph, const int32_t* ids, const Workspace& w, co
   return DIPS_OK;
 }
 
-static int mlp_eval(const float* pts, const float* phi, int64_t n, float* u, float* g, cudaStream_t s) {
+template <class N, int NW>
+static int tile_eval_nw(const float* params, const float* pts, const float* phi, int64_t n, float* u, float* g,
+                        cudaStream_t s) {
+  constexpr size_t bytes = tile::CtaLayout<N, NW>::kBytes;
+  constexpr int ctas_per_sm = tile::warps_per_sm<N>() / NW;
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(tile::k_tile_eval<N, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)bytes);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(tile evaluation smem)");
+    attr_done = true;
+  }
+  tile::k_tile_eval<N, NW><<<kTileGrid * ctas_per_sm, 32 * NW, bytes, s>>>(pts, phi, n, params, A::kOffP, u, g);
+  DIPS_CHECK_LAUNCH("tile evaluation");
+  return DIPS_OK;
+}
+
+template <bool TILE = kTileArch>
+static int tile_eval(const float* params, const float* pts, const float* phi, int64_t n, float* u, float* g,
+                     cudaStream_t s) {
+  if constexpr (TILE) {
+    return tile_eval_nw<typename A::M, kTileCand[0]>(params, pts, phi, n, u, g, s);
+  } else {
+    ::dips::set_error("tile evaluation: network shape without the tile engine");
+    return DIPS_E_UNSUPPORTED;
+  }
+}
+
+static int mlp_eval(const float* params, const float* pts, const float* phi, int64_t n, float* u, float* g,
+                    cudaStream_t s) {
+  if constexpr (kTileArch) return tile_eval(params, pts, phi, n, u, g, s);
   int64_t grid = (n + 127) / 128;
   if (grid > 152 * 16) grid = 152 * 16;
   k_mlp_eval<typename A::M, 0, A::kParams><<<(int)grid, 128, 0, s>>>(pts, phi, n, u, g, 0);

@@ -141,7 +141,8 @@ struct ArchOps {
   // the gradient partial rows
   int (*bulk_fused)(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec,
                     float* residual_out, bool bwd, const Marks* mk, cudaStream_t s);
-  int (*mlp_eval)(const float* pts, const float* phi, int64_t n, float* u, float* g, cudaStream_t s);
+  int (*mlp_eval)(const float* params, const float* pts, const float* phi, int64_t n, float* u, float* g,
+                  cudaStream_t s);
   // times the shape's tunable launch configurations on a prepared workspace and keeps the
   // fastest for the current device (NULL: nothing to tune); *chosen = the choice (0: none)
   int (*autotune)(const PtsH& ph, const int32_t* ids, const Workspace& w, const dips_records_t& rec, cudaStream_t s,

@@ -651,7 +651,7 @@ static int bulk_fused(const PtsH&, const int32_t*, const Workspace&, const dips_
   return DIPS_OK;
 }
 
-static int mlp_eval(const float* pts, const float* phi, int64_t n, float* u, float* g, cudaStream_t s) {
+static int mlp_eval(const float*, const float* pts, const float* phi, int64_t n, float* u, float* g, cudaStream_t s) {
   int64_t grid = (n + 127) / 128;
   if (grid > 152 * 16) grid = 152 * 16;
   k_tc_eval<<<(int)grid, 128, 0, s>>>(t_params, 0, pts, phi, n, u, g, 0);

@@ -100,12 +100,16 @@ def test_residual_vector_and_minibatch():
     _grad_close(gg, gr)
 
 
-def test_mlp_eval_and_input_gradient():
+@pytest.mark.parametrize("arch", [(3, 32, 3, 32), (2, 16, 2, 16), (1, 1, 2, 10)])
+def test_mlp_eval_and_input_gradient(arch):
+    """u and du/dx (the tile engine's evaluation for 3x32 and 2x16, a thread per point for the
+    other shapes) against the oracle's network in FP64 with autograd; 5,001 points, so that the
+    last 32-point tile is partial and most tiles straddle the interface."""
     from dips_gb300 import nn
 
-    case = _parity.build_case("sphere", n=16, arch=(3, 32, 3, 32))
+    case = _parity.build_case("sphere", n=16, arch=arch)
     rng = np.random.default_rng(0)
-    pts = rng.uniform(-1, 1, (5000, 3)).astype(F32)
+    pts = rng.uniform(-1, 1, (5001, 3)).astype(F32)
     phi = case.oracle_problem.phi(pts)
     u, g = nn.mlp_eval(case.gpu_arch(), torch.as_tensor(case.params, device="cuda"),
                        torch.as_tensor(pts, device="cuda"), torch.as_tensor(phi, device="cuda"), want_grad=True)
