@@ -314,12 +314,12 @@ def run_ours(args, rank, world):
     tensor = ARCH[1] == 64
     # the dominant launch: for 3x32 the tile engine's training launch, one launch for both
     # networks (forward + adjoint + dW of every job: the 7 stencil jobs of each bulk point and the
-    # jobs of the other points); for 4x64 the u+ tensor-core adjoint (which also recomputes the
-    # forward).  3 F per job either way; the forward that feeds the residual and the recompute
-    # are not counted.
-    if tensor:
-        dom_net = "p" if phase_med["adjoint_p"] >= phase_med["adjoint_m"] else "m"
-        t_dom = phase_med[f"adjoint_{dom_net}"] / 1e3
+    # jobs of the other points); for 4x64 the larger network's tensor-core launch (forward of
+    # its bulk jobs with their residual, recomputed forward of its general jobs, adjoint and dW
+    # of all).  3 F per job either way; the recompute is not counted.
+    if tensor:  # the tcgen05 bulk/adjoint launch of one network (bulk tiles with their residual)
+        dom_net = "p" if phase_med["fused_p"] >= phase_med["fused_m"] else "m"
+        t_dom = phase_med[f"fused_{dom_net}"] / 1e3
         dom_jobs, dom_f = (jobs_p, f_p) if dom_net == "p" else (jobs_m, f_m)
         dom_flops = 3 * dom_jobs * dom_f
     else:
@@ -431,7 +431,7 @@ def run_ours(args, rank, world):
                        "setup_s": setup_s, "wall_s_timed": wall},
             "roofline": {"bound": "tensor" if tensor else "fp32",
                          "kernel": (f"tcnet::k_tc_adjoint<u{'+' if dom_net == 'p' else '-'} net> (tcgen05 TF32: "
-                                    "recomputed forward, adjoint and dW of every job of that network)" if tensor else
+                                    "bulk residual, forward, adjoint and dW of every job of that network)" if tensor else
                                     "tile::k_tile<3x32, kTrain> (one launch for both networks: forward, bulk "
                                     "residual, adjoint and dW of every job)"),
                          "achieved": dom_tflops, "peak": dom_peak, "unit": "TFLOP/s",

@@ -327,8 +327,16 @@ constexpr int kOffGX = kOffZ + kFM72;
 constexpr int kOffSmall = kOffGX + kFM8;
 constexpr size_t kAdjSmem = kOffSmall + sizeof(float) * kSmallFloats + 64;
 
+// Bulk points (7 stencil jobs of this network) come in tiles of 18 points = 126 jobs (lanes 126
+// and 127 idle): after the forward the CTA forms their residuals and dL/du in shared memory, so
+// that their network values need no separate forward launch.  General jobs follow in tiles of
+// 128 with dL/du from the general residual.  BWD = false: bulk tiles only, forward, residual
+// and loss (the forward-only path); BWD = true: the backward of every tile as well.
+constexpr int kBulkPts = 18;
+
+template <bool BWD>
 __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restrict__ params, int off, Workspace w,
-                                                            int net_p) {
+                                                            int net_p, PtsH ph, float* __restrict__ residual_out) {
   extern __shared__ __align__(1024) unsigned char sm[];
   unsigned char* wf = sm + kOffWF;
   unsigned char* wb = sm + kOffWB;
@@ -364,7 +372,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
   const uint32_t lb = tb + ((uint32_t)(32 * (warp & 3)) << 16);
   const Ctl ctl = *w.ctl;
   const int64_t jbeg = net_p ? ctl.jm_pad : 0, jend = net_p ? ctl.total : ctl.jm;
-  const int64_t ntiles = (jend - jbeg + kTile - 1) / kTile;
+  const int64_t nb = net_p ? ctl.nbp : ctl.nbm;
+  const int64_t nbt = (nb + kBulkPts - 1) / kBulkPts;
+  const int64_t ntiles = nbt + (BWD ? (jend - jbeg + kTile - 1) / kTile : 0);
+  const float* recs = w.brec + (size_t)(net_p ? w.B : 0) * kRecFloats;
+  const float hh[3] = {ph.h[0], ph.h[1], ph.h[2]};
+  const float Bf = (float)w.B;
+  __shared__ float s_part[kTile], s_au[kTile], s_g[kTile];
+  __shared__ double s_loss[kThreads / 32];
+  double lsum = 0.0;
   uint32_t phase = 0;
   bool first = true;
   auto wait = [&]() {
@@ -376,15 +392,46 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     fence_after();
   };
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t j = jbeg + tile * kTile + job;
+    const bool bulk = tile < nbt;
     float x[3] = {0.0f, 0.0f, 0.0f};
-    float g = 0.0f;
-    if (j < jend) {
-      const float4 xv = w.jx[j];
-      x[0] = xv.x;
-      x[1] = xv.y;
-      x[2] = xv.z;
-      g = w.jg[j];
+    float g = 0.0f, A = 0.0f;
+    const int pl = job / kStencil, sj = job - kStencil * pl;  // bulk tile: point and stencil point
+    const int64_t pidx = tile * kBulkPts + pl;
+    const bool bvalid = bulk && job < kBulkPts * kStencil && pidx < nb;
+    // threads 0..17 of a bulk tile: their point's record, loaded now so that the loads run under
+    // the forward's MMAs rather than between the barriers of the residual step
+    const int64_t qpt = tile * kBulkPts + t;
+    const bool rvalid = bulk && t < kBulkPts && qpt < nb;
+    float r_lhs0 = 0.0f, r_diag = 1.0f, r_rod = 0.0f, r_P = 1.0f, r_A[kStencil];
+    int32_t rslot = 0;
+#pragma unroll
+    for (int k = 0; k < kStencil; ++k) r_A[k] = 0.0f;
+    if (rvalid) {
+      const float* r = recs + qpt * kRecFloats;
+      r_lhs0 = r[kRecLhs0];
+      r_diag = r[kRecDiag];
+      r_rod = r[kRecRod];
+      rslot = __float_as_int(r[kRecSlot]);
+#pragma unroll
+      for (int k = 0; k < kStencil; ++k) r_A[k] = r[kRecA + k];
+      if (w.pre_P) r_P = w.pre_P[rslot];
+    }
+    if (bulk) {
+      if (bvalid) {
+        const float* r = recs + pidx * kRecFloats;
+        const float p[3] = {r[kRecP], r[kRecP + 1], r[kRecP + 2]};
+        stencil_point(p, hh, sj, x);
+        A = r[kRecA + sj];
+      }
+    } else {
+      const int64_t j = jbeg + (tile - nbt) * kTile + job;
+      if (j < jend) {
+        const float4 xv = w.jx[j];
+        x[0] = xv.x;
+        x[1] = xv.y;
+        x[2] = xv.z;
+        g = w.jg[j];
+      }
     }
     // ---- forward, keeping h2^T and h3^T
     float h[kHalf];
@@ -424,6 +471,38 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     from_tmem(lb, cD + f0, h);
 #pragma unroll
     for (int o = 0; o < kHalf; ++o) h[o] = tanh_f(h[o] + small[6 * W + f0 + o]);  // h4
+    if (bulk) {
+      // u of every job, A_j u_j, the residual of each of the tile's points, then dL/du
+      float u = 0.0f;
+#pragma unroll
+      for (int o = 0; o < kHalf; ++o) u = fmaf(small[7 * W + f0 + o], h[o], u);
+      if (f0) s_part[job] = u;
+      __syncthreads();
+      if (!f0) s_au[job] = A * (u + s_part[job] + small[8 * W]);
+      __syncthreads();
+      if (t < kBulkPts) {
+        if (rvalid) {
+          float lhs = r_lhs0;
+#pragma unroll
+          for (int k = 0; k < kStencil; ++k) lhs += s_au[kStencil * t + k];
+          const float qv = lhs / r_diag;
+          const float r0 = nan_to_num(qv) - r_rod;
+          const float rr = r_P * r0;  // learned preconditioner (1 without it)
+          if (w.pre_P) w.pre_r0[rslot] = r0;
+          const float gc = isfinite(qv) ? (rr / Bf) * r_P / r_diag : 0.0f;
+          lsum += 0.5 * (double)rr * (double)rr;
+          if (residual_out) residual_out[rslot] = rr;
+#pragma unroll
+          for (int k = 0; k < kStencil; ++k) s_g[kStencil * t + k] = gc * r_A[k];
+        } else {
+#pragma unroll
+          for (int k = 0; k < kStencil; ++k) s_g[kStencil * t + k] = 0.0f;
+        }
+      }
+      __syncthreads();
+      g = bvalid ? s_g[job] : 0.0f;
+    }
+    if (!BWD) continue;
     // ---- output layer: dWo, dbo = sum_j g_j [h4, 1]  (A = [g] replicated, B = h4^T with its ones row)
     to_fm(Z, job, h, f0);
     if (!f0) {
@@ -508,6 +587,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     }
     wait();
     first = false;
+  }
+  // ---- loss partial of the bulk points of this CTA
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+  if (lane == 0) s_loss[warp] = lsum;
+  __syncthreads();
+  if (t == 0) {
+    double v = 0.0;
+    for (int k = 0; k < kThreads / 32; ++k) v += s_loss[k];
+    w.floss[net_p * kLossSlots + blockIdx.x] = v;
+    if (blockIdx.x == 0) w.ctl->floss_n[net_p] = gridDim.x;
+  }
+  if (!BWD) {
+    fence_before();
+    __syncthreads();
+    fence_after();
+    tmem_free(tb, kAdjCols);
+    return;
   }
   // ---- partial gradient row of this CTA (columns of this network)
   float* row = w.partials + (size_t)blockIdx.x * w.n_params + off;
@@ -631,24 +728,30 @@ static int job_forward(const PtsH&, const int32_t*, const Workspace& w, const Ma
   return DIPS_OK;
 }
 
-static int job_adjoint(const PtsH&, const int32_t*, const Workspace& w, const Marks* mk, cudaStream_t s) {
-  static bool attr = false;
-  int st = set_smem((const void*)k_tc_adjoint, kAdjSmem, &attr);
-  if (st) return st;
-  k_tc_adjoint<<<kGrid, kThreads, kAdjSmem, s>>>(t_params, 0, w, 0);
+// the backward of every job is part of the bulk launch
+static int job_adjoint(const PtsH&, const int32_t*, const Workspace&, const Marks* mk, cudaStream_t s) {
   mark(mk, kMarkAdjM, s);
-  k_tc_adjoint<<<kGrid, kThreads, kAdjSmem, s>>>(t_params, kNetParams, w, 1);
   mark(mk, kMarkAdjP, s);
-  DIPS_CHECK_LAUNCH("tcgen05 adjoint");
   return DIPS_OK;
 }
 
-// no bulk points for this shape (their loss-partial count stays 0)
-static int bulk_fused(const PtsH&, const int32_t*, const Workspace&, const dips_records_t&, float*, bool,
-                      const Marks* mk, cudaStream_t s) {
+template <bool BWD>
+static int adjoint_pair(const PtsH& ph, const Workspace& w, float* residual_out, const Marks* mk, cudaStream_t s) {
+  static bool attr = false;
+  int st = set_smem((const void*)k_tc_adjoint<BWD>, kAdjSmem, &attr);
+  if (st) return st;
+  k_tc_adjoint<BWD><<<kGrid, kThreads, kAdjSmem, s>>>(t_params, 0, w, 0, ph, residual_out);
   mark(mk, kMarkFusedM, s);
+  k_tc_adjoint<BWD><<<kGrid, kThreads, kAdjSmem, s>>>(t_params, kNetParams, w, 1, ph, residual_out);
   mark(mk, kMarkFusedP, s);
+  DIPS_CHECK_LAUNCH("tcgen05 bulk / adjoint");
   return DIPS_OK;
+}
+
+// bulk points' forward, residual and loss (and, with bwd, the backward of every job)
+static int bulk_fused(const PtsH& ph, const int32_t*, const Workspace& w, const dips_records_t&, float* residual_out,
+                      bool bwd, const Marks* mk, cudaStream_t s) {
+  return bwd ? adjoint_pair<true>(ph, w, residual_out, mk, s) : adjoint_pair<false>(ph, w, residual_out, mk, s);
 }
 
 static int mlp_eval(const float*, const float* pts, const float* phi, int64_t n, float* u, float* g, cudaStream_t s) {
@@ -663,7 +766,7 @@ static int mlp_eval(const float*, const float* pts, const float* phi, int64_t n,
 }  // namespace tcnet
 
 const ArchOps* arch_ops_4_64_4_64() {
-  static const ArchOps ops = {4, 64, 4, 64, tcnet::kParams, 0, tcnet::load_params, tcnet::job_forward,
+  static const ArchOps ops = {4, 64, 4, 64, tcnet::kParams, 1, tcnet::load_params, tcnet::job_forward,
                               tcnet::job_adjoint, tcnet::bulk_fused, tcnet::mlp_eval, nullptr, nullptr,
                               nullptr};
   return &ops;
