@@ -440,7 +440,7 @@ def run_ours(args, rank, world):
                                         f"{dom_f}; {dom_jobs} jobs per launch (bulk points: {bulk_m} u-, {bulk_p} u+)",
                          "peak_source": peak_src, "fp32_peak_tflops": fp32_peak,
                          "fp32_peak_nominal_tflops": torch.cuda.get_device_properties(dev).multi_processor_count
-                                                     * 128 * 2 * float(clk.get("sm_max_mhz") or 0) * 1e6 / 1e12,
+                                                     * 128 * 2 * float((clk or {}).get("sm_max_mhz") or 0) * 1e6 / 1e12,
                          "phase_ms": phase_med,
                          "step_tflops": step_tflops, "step_frac": step_tflops / fp32_peak,
                          "step_algorithmic": "3 x F x (all jobs of the batch) per step"},
