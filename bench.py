@@ -68,6 +68,9 @@ def parse():
                          "500 Gaussians, mu 1/100, k = 0.5; lpbe: --instances linearised Poisson-Boltzmann problems "
                          "of uneven size (sides 48..160), 2x16 networks, one graph launch per batched step")
     ap.add_argument("--instances", type=int, default=64)
+    ap.add_argument("--instance-streams", action="store_true",
+                    help="lpbe: one training step per instance on 8 graph streams instead of the persistent "
+                         "multi-instance step")
     ap.add_argument("--c1", action="store_true",
                     help="configuration 1 end to end through trainer.setup/init_fn/solve_fn: sphere 32^3, "
                          "DoubleMLP 1x1/2x10, full batch, 200 epochs, lr 1e-3 decaying 0.9; CPU oracle timed "
@@ -467,7 +470,8 @@ def run_instances(args, rank, world):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     insts = [(side, problems.lpbe_problem(c, r, q)) for side, c, r, q in problems.lpbe_instances(args.instances, seed=rank)]
-    ib = batch.InstanceBatch(insts, arch, batch=args.batch, lr=1e-3, seed=rank)
+    ib = batch.InstanceBatch(insts, arch, batch=args.batch, lr=1e-3, seed=rank,
+                             persistent=False if args.instance_streams else None)
     for _ in range(max(args.warmup, 3)):
         ib.step()
     ib.capture()
