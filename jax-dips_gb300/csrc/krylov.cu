@@ -44,19 +44,54 @@ __device__ __forceinline__ int64_t job_node(int64_t p, uint16_t c, const Grid3& 
   return ((int64_t)i * g.ny + j) * g.nz + k;
 }
 
-// (K x)_p, i.e. the row's linear part divided by its diagonal coefficient
-__device__ __forceinline__ float row_apply(const dips_records_t& rec, const Grid3& g, int64_t p, const float* x) {
-  const int64_t o0 = rec.job_off[p], o1 = rec.job_off[p + 1];
-  const int cm = rec.cnt_m[p], cp = rec.cnt[p] - cm;
-  float acc = 0.0f;
-  for (int q = 0; q < cm; ++q) acc = fmaf(rec.job_A[o0 + q], __ldg(x + job_node(p, rec.job_code[o0 + q], g)), acc);
-  for (int q = 0; q < cp; ++q) {
-    const int64_t o = o1 - cp + q;
-    acc = fmaf(rec.job_A[o], __ldg(x + job_node(p, rec.job_code[o], g)), acc);
+// (K x)_p of the rows p of one warp (valid lanes).  Bulk rows (7 stencil jobs of one network,
+// interior) read their packed record (rec.bulk_rec: the 7 coefficients in stencil order and
+// diag) and the 7 neighbouring nodes directly; the other rows, with up to 7 x 28 jobs, are
+// taken one at a time by the whole warp, the lanes splitting the jobs.  All 32 lanes call it.
+__device__ __forceinline__ float warp_apply(const dips_records_t& rec, const Grid3& g, int64_t p, bool valid,
+                                            const float* __restrict__ x) {
+  const int lane = threadIdx.x & 31;
+  float out = 0.0f;
+  bool gen = false;
+  if (valid) {
+    const int c = rec.cnt[p], m = rec.cnt_m[p];
+    if (rec.bulk_rec && c == kStencil && (m == kStencil || m == 0)) {
+      const float4* r4 = reinterpret_cast<const float4*>(rec.bulk_rec + p * 16);
+      const float4 a = __ldg(r4 + 1), b = __ldg(r4 + 2);  // A0..A3; A4..A6, diag
+      const int64_t sj = g.nz, si = (int64_t)g.ny * g.nz;
+      float acc = a.x * __ldg(x + p);
+      acc = fmaf(a.y, __ldg(x + p - si), acc);
+      acc = fmaf(a.z, __ldg(x + p + si), acc);
+      acc = fmaf(a.w, __ldg(x + p - sj), acc);
+      acc = fmaf(b.x, __ldg(x + p + sj), acc);
+      acc = fmaf(b.y, __ldg(x + p - 1), acc);
+      acc = fmaf(b.z, __ldg(x + p + 1), acc);
+      const float v = acc / b.w;
+      out = isfinite(v) ? v : 0.0f;
+    } else {
+      gen = true;
+    }
   }
-  const float d = rec.diag[p];
-  const float v = acc / d;
-  return isfinite(v) ? v : 0.0f;
+  unsigned todo = __ballot_sync(0xffffffffu, gen);
+  while (todo) {
+    const int owner = __ffs(todo) - 1;
+    todo &= todo - 1;
+    const int64_t gp = __shfl_sync(0xffffffffu, p, owner);
+    const int64_t o0 = rec.job_off[gp], o1 = rec.job_off[gp + 1];
+    const int cm = rec.cnt_m[gp], n = rec.cnt[gp];
+    float part = 0.0f;
+    for (int q = lane; q < n; q += 32) {
+      const int64_t o = q < cm ? o0 + q : o1 - n + q;  // u- jobs at the front, u+ jobs at the back
+      part = fmaf(rec.job_A[o], __ldg(x + job_node(gp, rec.job_code[o], g)), part);
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) part += __shfl_xor_sync(0xffffffffu, part, s);
+    if (lane == owner) {
+      const float v = part / rec.diag[gp];
+      out = isfinite(v) ? v : 0.0f;
+    }
+  }
+  return out;
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -92,10 +127,17 @@ __device__ __forceinline__ void block_partials(double a, double b, double c, dou
 }
 
 // residual of a nodal vector: out = K u - b (linear_only: K u)
+// rows of a warp-aligned grid-stride loop: the stride is a multiple of 32, so the warps stay whole
+#define DIPS_ROWS(p, valid, n)                                                                               \
+  for (int64_t p##0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31), p = p##0 + (threadIdx.x & 31); \
+       p##0 < (n); p##0 += (int64_t)gridDim.x * blockDim.x, p = p##0 + (threadIdx.x & 31))                   \
+    if (const bool valid = p < (n); true)
+
 __global__ void k_fv_residual(dips_records_t rec, Grid3 g, const float* __restrict__ u, int linear_only,
                               float* __restrict__ out) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < rec.n_pts; p += (int64_t)gridDim.x * blockDim.x) {
-    const float Ku = row_apply(rec, g, p, u);
+  DIPS_ROWS(p, valid, rec.n_pts) {
+    const float Ku = warp_apply(rec, g, p, valid, u);
+    if (!valid) continue;
     if (linear_only) {
       out[p] = Ku;
     } else {
@@ -123,10 +165,12 @@ struct KVecs {
 // r = b - K x, rhat = r, p = v = 0; partials (r, r), (b, b)
 __global__ void k_bicg_init(dips_records_t rec, Grid3 g, KVecs V) {
   double rr = 0.0, bb = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rec.n_pts; i += (int64_t)gridDim.x * blockDim.x) {
+  DIPS_ROWS(i, valid, rec.n_pts) {
+    const float Kx = warp_apply(rec, g, i, valid, V.x);
+    if (!valid) continue;
     const float d = rec.diag[i];
     const float b = rec.rod[i] - nan_to_num(rec.lhs0[i] / d);
-    const float r = b - row_apply(rec, g, i, V.x);
+    const float r = b - Kx;
     V.r[i] = r;
     V.rhat[i] = r;
     V.p[i] = 0.0f;
@@ -222,8 +266,9 @@ __global__ void k_bicg_rho_shift(KVecs V) {
 // v = K p; partial (rhat, v)
 __global__ void k_bicg_v(dips_records_t rec, Grid3 g, KVecs V) {
   double d = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rec.n_pts; i += (int64_t)gridDim.x * blockDim.x) {
-    const float v = row_apply(rec, g, i, V.p);
+  DIPS_ROWS(i, valid, rec.n_pts) {
+    const float v = warp_apply(rec, g, i, valid, V.p);
+    if (!valid) continue;
     V.v[i] = v;
     d += (double)V.rhat[i] * v;
   }
@@ -250,8 +295,9 @@ __global__ void k_bicg_s(int64_t n, KVecs V) {
 // t = K s; partials (t, s), (t, t)
 __global__ void k_bicg_t(dips_records_t rec, Grid3 g, KVecs V) {
   double ts = 0.0, tt = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rec.n_pts; i += (int64_t)gridDim.x * blockDim.x) {
-    const float t = row_apply(rec, g, i, V.s);
+  DIPS_ROWS(i, valid, rec.n_pts) {
+    const float t = warp_apply(rec, g, i, valid, V.s);
+    if (!valid) continue;
     V.t[i] = t;
     ts += (double)t * V.s[i];
     tt += (double)t * t;
