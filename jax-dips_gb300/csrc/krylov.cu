@@ -18,6 +18,7 @@ namespace dips {
 
 constexpr int kKThreads = 256;
 constexpr int kKGrid = 152 * 8;
+constexpr int kGenGrid = 152 * 8;  // blocks of the general-row kernels (8 warps each, a warp per row)
 
 struct Grid3 {
   int nx, ny, nz;
@@ -44,52 +45,68 @@ __device__ __forceinline__ int64_t job_node(int64_t p, uint16_t c, const Grid3& 
   return ((int64_t)i * g.ny + j) * g.nz + k;
 }
 
-// (K x)_p of the rows p of one warp (valid lanes).  Bulk rows (7 stencil jobs of one network,
-// interior) read their packed record (rec.bulk_rec: the 7 coefficients in stencil order and
-// diag) and the 7 neighbouring nodes directly; the other rows, with up to 7 x 28 jobs, are
-// taken one at a time by the whole warp, the lanes splitting the jobs.  All 32 lanes call it.
+// A bulk row: 7 stencil jobs of one network (interior), with its packed record.
+__device__ __forceinline__ bool bulk_row(const dips_records_t& rec, int64_t p) {
+  const int c = rec.cnt[p], m = rec.cnt_m[p];
+  return rec.bulk_rec && c == kStencil && (m == kStencil || m == 0);
+}
+
+// (K x)_p of a bulk row: the 7 coefficients in stencil order and diag from the packed record,
+// the 7 neighbouring nodes of the grid directly
+__device__ __forceinline__ float bulk_apply(const dips_records_t& rec, const Grid3& g, int64_t p,
+                                            const float* __restrict__ x) {
+  const float4* r4 = reinterpret_cast<const float4*>(rec.bulk_rec + p * 16);
+  const float4 a = __ldg(r4 + 1), b = __ldg(r4 + 2);  // A0..A3; A4..A6, diag
+  const int64_t sj = g.nz, si = (int64_t)g.ny * g.nz;
+  float acc = a.x * __ldg(x + p);
+  acc = fmaf(a.y, __ldg(x + p - si), acc);
+  acc = fmaf(a.z, __ldg(x + p + si), acc);
+  acc = fmaf(a.w, __ldg(x + p - sj), acc);
+  acc = fmaf(b.x, __ldg(x + p + sj), acc);
+  acc = fmaf(b.y, __ldg(x + p - 1), acc);
+  acc = fmaf(b.z, __ldg(x + p + 1), acc);
+  const float v = acc / b.w;
+  return isfinite(v) ? v : 0.0f;
+}
+
+// (K x)_gp of any row by the whole warp, the lanes splitting its jobs (up to 7 x 28); every lane
+// gets the value
+__device__ __forceinline__ float general_apply_warp(const dips_records_t& rec, const Grid3& g, int64_t gp,
+                                                    const float* __restrict__ x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t o0 = rec.job_off[gp], o1 = rec.job_off[gp + 1];
+  const int cm = rec.cnt_m[gp], n = rec.cnt[gp];
+  float part = 0.0f;
+  for (int q = lane; q < n; q += 32) {
+    const int64_t o = q < cm ? o0 + q : o1 - n + q;  // u- jobs at the front, u+ jobs at the back
+    part = fmaf(rec.job_A[o], __ldg(x + job_node(gp, rec.job_code[o], g)), part);
+  }
+#pragma unroll
+  for (int s = 16; s > 0; s >>= 1) part += __shfl_xor_sync(0xffffffffu, part, s);
+  const float v = part / rec.diag[gp];
+  return isfinite(v) ? v : 0.0f;
+}
+
+// (K x)_p of the rows p of one warp (valid lanes): bulk rows inline, the others one at a time
+// by the whole warp.  All 32 lanes call it.
 __device__ __forceinline__ float warp_apply(const dips_records_t& rec, const Grid3& g, int64_t p, bool valid,
                                             const float* __restrict__ x) {
   const int lane = threadIdx.x & 31;
   float out = 0.0f;
   bool gen = false;
   if (valid) {
-    const int c = rec.cnt[p], m = rec.cnt_m[p];
-    if (rec.bulk_rec && c == kStencil && (m == kStencil || m == 0)) {
-      const float4* r4 = reinterpret_cast<const float4*>(rec.bulk_rec + p * 16);
-      const float4 a = __ldg(r4 + 1), b = __ldg(r4 + 2);  // A0..A3; A4..A6, diag
-      const int64_t sj = g.nz, si = (int64_t)g.ny * g.nz;
-      float acc = a.x * __ldg(x + p);
-      acc = fmaf(a.y, __ldg(x + p - si), acc);
-      acc = fmaf(a.z, __ldg(x + p + si), acc);
-      acc = fmaf(a.w, __ldg(x + p - sj), acc);
-      acc = fmaf(b.x, __ldg(x + p + sj), acc);
-      acc = fmaf(b.y, __ldg(x + p - 1), acc);
-      acc = fmaf(b.z, __ldg(x + p + 1), acc);
-      const float v = acc / b.w;
-      out = isfinite(v) ? v : 0.0f;
-    } else {
+    if (bulk_row(rec, p))
+      out = bulk_apply(rec, g, p, x);
+    else
       gen = true;
-    }
   }
   unsigned todo = __ballot_sync(0xffffffffu, gen);
   while (todo) {
     const int owner = __ffs(todo) - 1;
     todo &= todo - 1;
     const int64_t gp = __shfl_sync(0xffffffffu, p, owner);
-    const int64_t o0 = rec.job_off[gp], o1 = rec.job_off[gp + 1];
-    const int cm = rec.cnt_m[gp], n = rec.cnt[gp];
-    float part = 0.0f;
-    for (int q = lane; q < n; q += 32) {
-      const int64_t o = q < cm ? o0 + q : o1 - n + q;  // u- jobs at the front, u+ jobs at the back
-      part = fmaf(rec.job_A[o], __ldg(x + job_node(gp, rec.job_code[o], g)), part);
-    }
-#pragma unroll
-    for (int s = 16; s > 0; s >>= 1) part += __shfl_xor_sync(0xffffffffu, part, s);
-    if (lane == owner) {
-      const float v = part / rec.diag[gp];
-      out = isfinite(v) ? v : 0.0f;
-    }
+    const float v = general_apply_warp(rec, g, gp, x);
+    if (lane == owner) out = v;
   }
   return out;
 }
@@ -157,28 +174,81 @@ struct KState {
 
 struct KVecs {
   float *x, *r, *rhat, *p, *v, *s, *t;
-  double* part;  // [kKGrid * 3]
+  double* part;     // [(kKGrid + kGenGrid) * 3]: bulk-row blocks, then general-row blocks
+  int32_t* glist;   // [n] the general rows (found once per solve)
+  int32_t* gcount;  // their number
   KState* st;
   float* err_part;  // [kKGrid] max |x - u_exact|
 };
 
-// r = b - K x, rhat = r, p = v = 0; partials (r, r), (b, b)
-__global__ void k_bicg_init(dips_records_t rec, Grid3 g, KVecs V) {
-  double rr = 0.0, bb = 0.0;
-  DIPS_ROWS(i, valid, rec.n_pts) {
-    const float Kx = warp_apply(rec, g, i, valid, V.x);
-    if (!valid) continue;
+
+// The rows whose product needs the warp-cooperative path, listed once per solve (the order of
+// the list depends on the warps' arrival; each row's value does not)
+__global__ void k_general_rows(dips_records_t rec, int32_t* __restrict__ list, int32_t* __restrict__ count) {
+  const int lane = threadIdx.x & 31;
+  DIPS_ROWS(p, valid, rec.n_pts) {
+    const bool gen = valid && !bulk_row(rec, p);
+    const unsigned m = __ballot_sync(0xffffffffu, gen);
+    if (!m) continue;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (gen) list[base + __popc(m & ((1u << lane) - 1))] = (int32_t)p;
+  }
+}
+
+// what a product feeds, per row i with (K x)_i = kx
+enum KMode {
+  kInit = 0,    // r = b - K x, rhat = r, p = v = 0; partials (r, r), (b, b)
+  kApplyV = 1,  // v = K p; partial (rhat, v)
+  kApplyT = 2,  // t = K s; partials (t, s), (t, t)
+};
+
+template <int MODE>
+__device__ __forceinline__ void row_done(const dips_records_t& rec, const KVecs& V, int64_t i, float kx, double& a0,
+                                         double& a1) {
+  if (MODE == kInit) {
     const float d = rec.diag[i];
     const float b = rec.rod[i] - nan_to_num(rec.lhs0[i] / d);
-    const float r = b - Kx;
+    const float r = b - kx;
     V.r[i] = r;
     V.rhat[i] = r;
     V.p[i] = 0.0f;
     V.v[i] = 0.0f;
-    rr += (double)r * r;
-    bb += (double)b * b;
+    a0 += (double)r * r;
+    a1 += (double)b * b;
+  } else if (MODE == kApplyV) {
+    V.v[i] = kx;
+    a0 += (double)V.rhat[i] * kx;
+  } else {
+    V.t[i] = kx;
+    a0 += (double)kx * V.s[i];
+    a1 += (double)kx * kx;
   }
-  block_partials(rr, bb, 0.0, V.part, 2);
+}
+
+// the bulk rows of the product (a thread per row); partials in V.part[0, kKGrid)
+template <int MODE>
+__global__ void k_apply_bulk(dips_records_t rec, Grid3 g, const float* __restrict__ x, KVecs V) {
+  double a0 = 0.0, a1 = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rec.n_pts; i += (int64_t)gridDim.x * blockDim.x)
+    if (bulk_row(rec, i)) row_done<MODE>(rec, V, i, bulk_apply(rec, g, i, x), a0, a1);
+  block_partials(a0, a1, 0.0, V.part, 2);
+}
+
+// the listed general rows (a warp per row); partials in V.part[kKGrid, kKGrid + kGenGrid)
+template <int MODE>
+__global__ void k_apply_general(dips_records_t rec, Grid3 g, const float* __restrict__ x, KVecs V) {
+  const int lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  const int64_t cnt = *V.gcount;
+  double a0 = 0.0, a1 = 0.0;
+  for (int64_t k = (int64_t)blockIdx.x * nw + (threadIdx.x >> 5); k < cnt; k += (int64_t)gridDim.x * nw) {
+    const int64_t gp = V.glist[k];
+    const float kx = general_apply_warp(rec, g, gp, x);
+    if (lane == 0) row_done<MODE>(rec, V, gp, kx, a0, a1);
+  }
+  block_partials(a0, a1, 0.0, V.part + 3 * kKGrid, 2);
 }
 
 __global__ void k_bicg_init_scalars(KVecs V, int nblk) {
@@ -263,17 +333,6 @@ __global__ void k_bicg_rho_shift(KVecs V) {
   }
 }
 
-// v = K p; partial (rhat, v)
-__global__ void k_bicg_v(dips_records_t rec, Grid3 g, KVecs V) {
-  double d = 0.0;
-  DIPS_ROWS(i, valid, rec.n_pts) {
-    const float v = warp_apply(rec, g, i, valid, V.p);
-    if (!valid) continue;
-    V.v[i] = v;
-    d += (double)V.rhat[i] * v;
-  }
-  block_partials(d, 0.0, 0.0, V.part, 1);
-}
 
 __global__ void k_bicg_alpha(KVecs V, int nblk) {
   reduce_partials(V.part, nblk, 1, &V.st->rhat_v, nullptr, nullptr);
@@ -292,18 +351,6 @@ __global__ void k_bicg_s(int64_t n, KVecs V) {
     V.s[i] = V.r[i] - a * V.v[i];
 }
 
-// t = K s; partials (t, s), (t, t)
-__global__ void k_bicg_t(dips_records_t rec, Grid3 g, KVecs V) {
-  double ts = 0.0, tt = 0.0;
-  DIPS_ROWS(i, valid, rec.n_pts) {
-    const float t = warp_apply(rec, g, i, valid, V.s);
-    if (!valid) continue;
-    V.t[i] = t;
-    ts += (double)t * V.s[i];
-    tt += (double)t * t;
-  }
-  block_partials(ts, tt, 0.0, V.part, 2);
-}
 
 __global__ void k_bicg_omega(KVecs V, int nblk) {
   reduce_partials(V.part, nblk, 2, &V.st->ts, &V.st->tt, nullptr);
@@ -378,7 +425,9 @@ static size_t kcarve(KVecs* V, char* base, int64_t n) {
   v.v = (float*)take(4 * n);
   v.s = (float*)take(4 * n);
   v.t = (float*)take(4 * n);
-  v.part = (double*)take(sizeof(double) * 3 * kKGrid);
+  v.part = (double*)take(sizeof(double) * 3 * (kKGrid + kGenGrid));
+  v.glist = (int32_t*)take(sizeof(int32_t) * n);
+  v.gcount = (int32_t*)take(sizeof(int32_t));
   v.st = (KState*)take(sizeof(KState));
   v.err_part = (float*)take(sizeof(float) * 2 * kKGrid);
   v.x = nullptr;
@@ -429,9 +478,13 @@ extern "C" int dips_bicgstab(const dips_records_t* rec, int32_t nx, int32_t ny, 
   kcarve(&V, (char*)(((uintptr_t)workspace + 255) & ~(uintptr_t)255), n);
   V.x = x;
   Grid3 g{nx, ny, nz};
-  const int G = kKGrid, T = kKThreads;
-  k_bicg_init<<<G, T, 0, stream>>>(*rec, g, V);
-  k_bicg_init_scalars<<<1, 1024, 0, stream>>>(V, G);
+  const int G = kKGrid, T = kKThreads, GP = kKGrid + kGenGrid;
+  cudaError_t ez = cudaMemsetAsync(V.gcount, 0, sizeof(int32_t), stream);
+  if (ez != cudaSuccess) return cuda_status(ez, "bicgstab general-row count");
+  k_general_rows<<<G, T, 0, stream>>>(*rec, V.glist, V.gcount);
+  k_apply_bulk<kInit><<<G, T, 0, stream>>>(*rec, g, V.x, V);
+  k_apply_general<kInit><<<kGenGrid, T, 0, stream>>>(*rec, g, V.x, V);
+  k_bicg_init_scalars<<<1, 1024, 0, stream>>>(V, GP);
   DIPS_CHECK_LAUNCH("bicgstab init");
   KState hs;
   float herr[2 * kKGrid];
@@ -478,11 +531,13 @@ extern "C" int dips_bicgstab(const dips_records_t* rec, int32_t nx, int32_t ny, 
       cudaError_t e = cudaMemcpyAsync(V.p, V.r, sizeof(float) * n, cudaMemcpyDeviceToDevice, stream);
       if (e != cudaSuccess) return cuda_status(e, "bicgstab p = r");
     }
-    k_bicg_v<<<G, T, 0, stream>>>(*rec, g, V);
-    k_bicg_alpha<<<1, 1024, 0, stream>>>(V, G);
+    k_apply_bulk<kApplyV><<<G, T, 0, stream>>>(*rec, g, V.p, V);
+    k_apply_general<kApplyV><<<kGenGrid, T, 0, stream>>>(*rec, g, V.p, V);
+    k_bicg_alpha<<<1, 1024, 0, stream>>>(V, GP);
     k_bicg_s<<<G, T, 0, stream>>>(n, V);
-    k_bicg_t<<<G, T, 0, stream>>>(*rec, g, V);
-    k_bicg_omega<<<1, 1024, 0, stream>>>(V, G);
+    k_apply_bulk<kApplyT><<<G, T, 0, stream>>>(*rec, g, V.s, V);
+    k_apply_general<kApplyT><<<kGenGrid, T, 0, stream>>>(*rec, g, V.s, V);
+    k_bicg_omega<<<1, 1024, 0, stream>>>(V, GP);
     k_bicg_xr<<<G, T, 0, stream>>>(n, V);
     k_bicg_rho<<<1, 1024, 0, stream>>>(V, G);
     DIPS_CHECK_LAUNCH("bicgstab iteration");
