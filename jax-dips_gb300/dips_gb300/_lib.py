@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import ctypes
 import hashlib
+import platform
 import os
 import shutil
 import subprocess
@@ -62,7 +63,8 @@ def _fingerprint():
             h.update(name.encode())
             with open(path, "rb") as f:
                 h.update(f.read())
-    h.update(repr((ARCH_FLAGS, COMMON_FLAGS, UNITS)).encode())
+    # the host machine too: a library built on another architecture is never reused
+    h.update(repr((ARCH_FLAGS, COMMON_FLAGS, UNITS, platform.machine())).encode())
     return h.hexdigest()
 
 
