@@ -1,8 +1,11 @@
 // Per-network-shape kernels of the residual path (included once per shape by the
 // residual_a*.cu translation units, which define DIPS_LM, DIPS_WM, DIPS_LP, DIPS_WP).
 //
-// Everything runs on the FP32 pipe.  Each network (u- and u+) gets its own launches, so a
-// kernel holds one network's fully unrolled code:
+// Everything runs on the FP32 pipe.  The shapes 3x32 and 2x16 run every launch of the step, the
+// multi-instance step and the evaluation on the register-blocked tile engine (mlp_tile.cuh),
+// which reads the weights from the parameter buffer.  The other shapes use the kernels below;
+// each network (u- and u+) gets its own launches, so a kernel holds one network's fully
+// unrolled code:
 //   forward  one thread per job; the weights are constant-bank operands of FFMA
 //   adjoint  one thread per job recomputes the activations and stages them in the warp's
 //            shared-memory tile; the output gradients propagate thread-per-job (again with
