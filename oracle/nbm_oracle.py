@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the product imports this module; only
 ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
-do, and only as the checker (or as the timed CPU restatement of the reference).
+do, and only to check results (or as the timed CPU restatement of the reference).
 
 This file restates, in numpy float32, the reference's geometry and
 interpolation for the per-point FV residual (JAX-DIPS 0.2.1, x64 disabled):

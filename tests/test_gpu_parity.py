@@ -3,7 +3,7 @@
 Bars: integer/flag outputs and the level-set interpolant bit-exact; geometry
 coefficients bit-exact where the coefficient callables are constants (the float32
 operations are the oracle's, with no FMA contraction); loss within 1e-5 relative and
-gradients within 1e-4 relative (the tolerances the benchmark spec states for the FP32 path).
+gradients within 1e-4 relative (the tolerances required of the FP32 path).
 """
 
 import numpy as np
