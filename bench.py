@@ -53,7 +53,8 @@ def net_flops(layers, width):
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    # about 0.8 s of timed steps at the headline, long enough for the clock sampler's readings
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=128)
@@ -93,7 +94,7 @@ class ClockSampler:
         self.proc = None
         try:
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "50",
                  "-i", str(index)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -159,7 +160,9 @@ def cpu_oracle_rate(n, sample, steps, seed=0, arch=ARCH, problem="sphere", n_ls=
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    steps = max(args.steps, 1)
+    # each step is a fixed sample of the workload (the per-step overheads of a smaller sample
+    # would understate the CPU rate); at most 20 of them, so that any K ends within a minute or so
+    steps = max(min(args.steps, 20), 1)
     sample = args.cpu_sample
     # warm-up (imports, allocator)
     cpu_oracle_rate(args.n, 256, max(min(args.warmup, 2), 1), arch=arch_tuple(args), problem=args.problem,
@@ -175,6 +178,7 @@ def run_reference(args, rank, world):
         "unit": UNIT,
         "n_gpus": args.gpus,
         "steps": steps,
+        "steps_requested": args.steps,
         "warmup": args.warmup,
         "ms_per_step": 1e3 * sum(times) / len(times),
         "higher_is_better": True,
