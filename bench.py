@@ -538,6 +538,7 @@ def run_instances(args, rank, world):
                                    "instance's tiles)",
                        "global_batch": pts * world, "points": int(sum(it.level.n for it in ib.items)),
                        "batch_per_instance": args.batch, "jobs_per_step": jobs, "setup_s": setup_s,
+                       "autotuned_cta_warps": ib.cta_warps,
                        "l2": "flushed (256 MB write) between timed steps", "cuda_graph": True},
             "roofline": {"bound": "fp32", "kernel": (f"whole batched step ({ib.kernels_per_step} launches for all "
                                                      "instances: dips_train_step_instances)" if ib.persistent else

@@ -53,7 +53,7 @@ class InstanceBatch:
     """
 
     def __init__(self, instances, arch: nn.Arch, batch: int = 1 << 15, lr: float = 1e-3, seed: int = 0,
-                 device="cuda", streams: int = 8, persistent=None):
+                 device="cuda", streams: int = 8, persistent=None, autotune: bool = True):
         if not torch.cuda.is_available():
             raise RuntimeError("dips_gb300 runs on a CUDA GPU; none is available")
         lib = _lib.load()
@@ -73,6 +73,12 @@ class InstanceBatch:
             raise NotImplementedError("the persistent multi-instance step needs a 3x32 or 2x16 shape")
         self.max_batch = max(it.batch for it in self.items)
         self._tables = {}
+        self.cta_warps = 0
+        if tile and autotune:
+            # the tile engine's CTA width, timed on the largest instance (process-wide per device)
+            big = self.items[self.order[0]]
+            ids = ops.batch_ids(big.level.n, big.batch, epoch=0, batch_index=0, seed=big.seed, device=device)
+            self.cta_warps = ops.autotune(arch, big.params, big.level, ids, big.ws)
         if self.persistent:
             self._table(ids_mode=1)
 
