@@ -69,7 +69,7 @@ __device__ __forceinline__ float bulk_apply(const dips_records_t& rec, const Gri
   return isfinite(v) ? v : 0.0f;
 }
 
-// (K x)_gp of any row by the whole warp, the lanes splitting its jobs (up to 7 x 28); every lane
+// (K x)_gp of any row by the whole warp, the lanes splitting its jobs (up to 7 x 27); every lane
 // gets the value
 __device__ __forceinline__ float general_apply_warp(const dips_records_t& rec, const Grid3& g, int64_t gp,
                                                     const float* __restrict__ x) {

@@ -239,6 +239,9 @@ __global__ void k_pack_bulk(dips_records_t rec, float* __restrict__ out) {
   }
 }
 
+// a point has at most 7 x 27 jobs (each stencil point: its cube's centre and 26 neighbours)
+constexpr int kMaxJobRounds = (kStencil * kCube + 31) / 32;  // a point's jobs over 32 lanes
+
 __device__ __forceinline__ void emit_body(const int32_t* __restrict__ ids, int64_t B, const dips_records_t& rec,
                                           const Workspace& w, int bx) {
   const int64_t b = bx * (int64_t)blockDim.x + threadIdx.x;
@@ -279,7 +282,7 @@ __device__ __forceinline__ void emit_body(const int32_t* __restrict__ ids, int64
   }
   // general points: their u- jobs go to [om, om + cm), their u+ jobs to [op, op + cp); the
   // source jobs are the first cm and the last cp of [job_off[pid], job_off[pid + 1]) (the
-  // capacity may exceed the count).  A point has up to 7 x 28 jobs, so each warp expands its
+  // capacity may exceed the count).  A point has up to 7 x 27 jobs, so each warp expands its
   // general points one at a time with the 32 lanes taking the jobs.
   const bool gen = kind == 0;
   int64_t om = 0, op = 0, src = 0, srcp = 0;
@@ -311,20 +314,41 @@ __device__ __forceinline__ void emit_body(const int32_t* __restrict__ ids, int64
     const int32_t g_b = (int32_t)__shfl_sync(0xffffffffu, b, l);
     const float p[3] = {__shfl_sync(0xffffffffu, p0, l), __shfl_sync(0xffffffffu, p1, l),
                         __shfl_sync(0xffffffffu, p2, l)};
-    for (int q = lane; q < g_n; q += 32) {
-      const int64_t dst = q < g_cm ? g_om + q : g_op + (q - g_cm);
-      const int64_t sq = (q < g_cm ? g_src : g_srcp) + q;
-      const uint16_t code = rec.job_code[sq];
-      float x[3];
-      job_coords(p, h, code, x);
-      w.jslot[dst] = g_b;
-      w.jcode[dst] = code;
-      w.jA[dst] = rec.job_A[sq];
-      w.jx[dst] = make_float4(x[0], x[1], x[2], 0.0f);
+    // all of the point's source jobs are loaded before the first store, so that a point costs
+    // one memory round trip rather than one per 32 jobs (the stores may alias the loads as
+    // far as the compiler knows)
+    uint16_t code[kMaxJobRounds];
+    float a[kMaxJobRounds];
+#pragma unroll
+    for (int k = 0; k < kMaxJobRounds; ++k) {
+      const int q = lane + 32 * k;
+      code[k] = 0;
+      a[k] = 0.0f;
+      if (q < g_n) {
+        const int64_t sq = (q < g_cm ? g_src : g_srcp) + q;
+        code[k] = __ldg(rec.job_code + sq);
+        a[k] = __ldg(rec.job_A + sq);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxJobRounds; ++k) {
+      const int q = lane + 32 * k;
+      if (q < g_n) {
+        const int64_t dst = q < g_cm ? g_om + q : g_op + (q - g_cm);
+        float x[3];
+        job_coords(p, h, code[k], x);
+        w.jslot[dst] = g_b;
+        w.jcode[dst] = code[k];
+        w.jA[dst] = a[k];
+        w.jx[dst] = make_float4(x[0], x[1], x[2], 0.0f);
+      }
     }
   }
 }
 
+// Measured: capping k_emit (and k_residual) at 32 registers for full occupancy did not shorten
+// them (the spills cost what the occupancy gained); the batched job loads above did (expansion
+// of a 2^18 batch at 128^3: 61 -> 55 us).
 __global__ void k_emit(const int32_t* __restrict__ ids, int64_t B, const __grid_constant__ dips_records_t rec,
                        const __grid_constant__ Workspace w) {
   emit_body(ids, B, rec, w, blockIdx.x);
@@ -357,10 +381,9 @@ __device__ __forceinline__ double block_sum_d(double v) {
 }
 
 // One warp handles its general points one at a time, the 32 lanes splitting the point's jobs
-// (up to 7 x 28): lhs = lhs0 + sum_j A_j u_j, r = P (lhs/diag - rhs/diag), dL/du_j = dL/dlhs A_j.
+// (up to 7 x 27): lhs = lhs0 + sum_j A_j u_j, r = P (lhs/diag - rhs/diag), dL/du_j = dL/dlhs A_j.
 // Each lane first loads its own point's records, so that a point's turn costs one round trip
 // for its jobs.
-constexpr int kMaxJobRounds = (kStencil * kCube + 31) / 32;  // a point's jobs over 32 lanes
 
 __device__ __forceinline__ void residual_body(const int32_t* __restrict__ ids, int64_t B, const dips_records_t& rec,
                                               const Workspace& w, float* __restrict__ residual_out, int bx) {
