@@ -130,20 +130,53 @@ __device__ __forceinline__ void ldrow(float (&v)[NT], const float* p) {
   }
 }
 
-// z[q][t] += sum_k A[k][jc + q] * Bm[k][bc + t] over k < K (A row stride AS, Bm row stride 4 NT)
+// Two FP32 fused multiply-adds in one instruction (fma.rn.f32x2, sm_100 and later).  Each half
+// rounds like fmaf, so a loop written with it gives bit-identical results to the scalar loop
+// in half the issue slots.
+using f32x2 = unsigned long long;
+__device__ __forceinline__ f32x2 pk2(float lo, float hi) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void upk2(f32x2 v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+// z[q][t] += sum_k A[k][jc + q] * Bm[k][bc + t] over k < K (A row stride AS, Bm row stride 4 NT).
+// The features of a lane come in adjacent pairs (t, t + 1), one packed FMA per pair and job.
 template <int K, int AS, int NT>
 __device__ __forceinline__ void gemm(float (&z)[4][NT], const float* A, int jc, const float* Bm, int bc) {
+  f32x2 zz[4][NT / 2];
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int t = 0; t < NT / 2; ++t) zz[q][t] = pk2(z[q][2 * t], z[q][2 * t + 1]);
 #pragma unroll 4
   for (int k = 0; k < K; ++k) {
     const float4 a = ld4(A + k * AS + jc);
     const float av[4] = {a.x, a.y, a.z, a.w};
     float bv[NT];
     ldrow(bv, Bm + k * 4 * NT + bc);
+    f32x2 bp[NT / 2];
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
+    for (int t = 0; t < NT / 2; ++t) bp[t] = pk2(bv[2 * t], bv[2 * t + 1]);
 #pragma unroll
-      for (int t = 0; t < NT; ++t) z[q][t] = fmaf(av[q], bv[t], z[q][t]);
+    for (int q = 0; q < 4; ++q) {
+      const f32x2 aq = pk2(av[q], av[q]);
+#pragma unroll
+      for (int t = 0; t < NT / 2; ++t) zz[q][t] = fma2(aq, bp[t], zz[q][t]);
+    }
   }
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int t = 0; t < NT / 2; ++t) upk2(zz[q][t], z[q][2 * t], z[q][2 * t + 1]);
 }
 
 template <int NT>
