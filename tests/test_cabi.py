@@ -62,3 +62,19 @@ def test_argument_errors_are_reported_without_a_gpu():
     a = _lib.ArchT(5, 5, 5, 5)
     st = lib.dips_mlp_eval(a, _lib.c_void_p(8), _lib.c_void_p(8), _lib.c_void_p(8), 4, _lib.c_void_p(8), None, None)
     assert st == 4 and b"no kernel compiled" in lib.dips_last_error()
+
+
+def test_noalloc_step_rejects_bad_sizes_on_the_host():
+    """dips_train_step_noalloc checks the batch and its built-in scratch limit before any CUDA
+    call, so both rejections are visible without a GPU."""
+    from dips_gb300 import _lib
+
+    lib = _lib.load()
+    a = _lib.ArchT(3, 32, 3, 32)
+    p = _lib.c_void_p(8)
+    st = lib.dips_train_step_noalloc(a, None, p, p, p, p, None, None, 0, 0, p, None, None)
+    assert st == 1 and b"bad batch" in lib.dips_last_error()
+    need = lib.dips_step_workspace_bytes(a, 4096, 10**8)
+    assert need > 64 << 20
+    st = lib.dips_train_step_noalloc(a, None, p, p, p, p, None, None, 4096, 10**8, p, None, None)
+    assert st == 3 and b"built-in" in lib.dips_last_error()
