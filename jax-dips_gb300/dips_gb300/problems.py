@@ -192,6 +192,164 @@ def star_problem():
                      lambda r: _xyz(r)[3].full(1.0), f_m, f_p, beta)
 
 
+# ----------------------------------------------------------------------------------------
+# the reference's own manufactured problems (tests/confs/experiment_configs.py)
+# ----------------------------------------------------------------------------------------
+def reference_sphere_problem():
+    """``sphere()`` of tests/confs/experiment_configs.py:21-186: phi = |x| - 0.5,
+    u- = e^z, u+ = sin y cos x, mu- = y^2 ln(x + 2) + 4, mu+ = e^-z, k = 0, g = u+,
+    f from its hand-written f_m_fn/f_p_fn (:158-172), beta = -(mu+ grad u+ - mu- grad u-) . grad phi
+    (:84-96, grad phi not normalised; it is a unit vector for this phi).  mu- > mu+ everywhere in
+    [-1, 1]^3, so every interface point takes the reference's mu- > mu+ extrapolation branch
+    (solvers/poisson/discretization.py:464-486)."""
+
+    def phi(r):
+        x, y, z, xp = _xyz(r)
+        return xp.sqrt(x * x + y * y + z * z) - 0.5
+
+    def u_m(r):
+        x, y, z, xp = _xyz(r)
+        return xp.exp(z)
+
+    def u_p(r):
+        x, y, z, xp = _xyz(r)
+        return xp.sin(y) * xp.cos(x)
+
+    def mu_m(r):
+        x, y, z, xp = _xyz(r)
+        return y * y * xp.log(x + 2.0) + 4.0
+
+    def mu_p(r):
+        x, y, z, xp = _xyz(r)
+        return xp.exp(-1.0 * z)
+
+    def beta(r):
+        # grad phi = x / |x|: 0/0 = NaN at the origin, as jax.grad of the reference's phi gives
+        # there; the reference integrates beta at the origin (its zero-padding triangles), so a
+        # crossed cell's interface integral, and then its rhs/diag, come out NaN -> 0
+        x, y, z, xp = _xyz(r)
+        n = xp.sqrt(x * x + y * y + z * z)
+        nx, ny, nz = x / n, y / n, z / n
+        mp, mm = mu_p(r), mu_m(r)
+        gpx, gpy = -xp.sin(y) * xp.sin(x), xp.cos(y) * xp.cos(x)
+        gmz = xp.exp(z)
+        return ((mp * gpx) * nx + (mp * gpy) * ny + (0.0 - mm * gmz) * nz) * (-1.0)
+
+    def f_m(r):
+        x, y, z, xp = _xyz(r)
+        return -1.0 * xp.exp(z) * (y * y * xp.log(x + 2.0) + 4.0)
+
+    def f_p(r):
+        x, y, z, xp = _xyz(r)
+        return 2.0 * xp.exp(-1.0 * z) * xp.cos(x) * xp.sin(y)
+
+    zero = lambda r: _xyz(r)[3].full(0.0)  # noqa: E731
+    return _assemble(phi, u_m, u_p, mu_m, mu_p, zero, zero, f_m, f_p, beta)
+
+
+def reference_star_problem():
+    """``star()`` of tests/confs/experiment_configs.py:196-412: a three-mode star
+    phi = |x| - r0 (1 + ((x^2+y^2)/|x|^2)^2 core(atan2(y, x))), u- = sin 2x cos 2y e^z,
+    u+ = (16 t^5 - 20 t^3 + 5 t) ln(x + y + 3) cos z with t = (y - x)/3,
+    mu- = 10 (1 + 0.2 cos 2pi(x+y) sin 2pi(x-y) cos z), mu+ = 1, k = 0, g = u+, f from the
+    hand-written f_m_fn/f_p_fn (:355-397), beta = nan_to_num(-(mu+ grad u+ - mu- grad u-) . grad phi)
+    with the unnormalised grad phi (:280-292).  mu- > mu+ everywhere (mu- >= 8)."""
+    r0 = 0.483
+    modes = ((3.0, 0.1, 0.5), (4.0, -0.1, 1.8), (7.0, 0.15, 0.0))
+
+    def _core(r):
+        x, y, z, xp = _xyz(r)
+        th = xp.arctan2(y, x)
+        c = 0.0
+        dc = 0.0
+        for n_i, b_i, t_i in modes:
+            c = c + b_i * xp.cos(n_i * (th - t_i))
+            dc = dc - b_i * n_i * xp.sin(n_i * (th - t_i))
+        return c, dc
+
+    def phi(r):
+        x, y, z, xp = _xyz(r)
+        s = x * x + y * y
+        rho2 = s + z * z
+        c, _ = _core(r)
+        q = s / rho2  # 0/0 = NaN at the origin, where nan_to_num gives 0 (experiment_configs.py:248)
+        v = xp.sqrt(rho2) - r0 * (1.0 + q * q * c)
+        return xp.nan_to_num(v)
+
+    def grad_phi(r):
+        x, y, z, xp = _xyz(r)
+        s = x * x + y * y
+        rho2 = s + z * z
+        rho = xp.sqrt(rho2)
+        c, dc = _core(r)
+        q = xp.safe_div(s, rho2)
+        rho4 = rho2 * rho2
+        dq = (xp.safe_div(2.0 * x * z * z, rho4), xp.safe_div(2.0 * y * z * z, rho4), xp.safe_div(-2.0 * s * z, rho4))
+        dth = (xp.safe_div(-y, s), xp.safe_div(x, s), 0.0)
+        out = []
+        for a, u in enumerate((x, y, z)):
+            out.append(xp.safe_div(u, rho) - r0 * (2.0 * q * dq[a] * c + q * q * dc * dth[a]))
+        return out
+
+    def u_m(r):
+        x, y, z, xp = _xyz(r)
+        return xp.sin(2.0 * x) * xp.cos(2.0 * y) * xp.exp(z)
+
+    def _poly(t):
+        return 16.0 * t ** 5 - 20.0 * t ** 3 + 5.0 * t
+
+    def u_p(r):
+        x, y, z, xp = _xyz(r)
+        return _poly((y - x) / 3.0) * xp.log(x + y + 3.0) * xp.cos(z)
+
+    def mu_m(r):
+        x, y, z, xp = _xyz(r)
+        pi = math.pi
+        return 10.0 * (1.0 + 0.2 * xp.cos(2.0 * pi * (x + y)) * xp.sin(2.0 * pi * (x - y)) * xp.cos(z))
+
+    def mu_p(r):
+        return _xyz(r)[3].full(1.0)
+
+    def f_m(r):
+        x, y, z, xp = _xyz(r)
+        pi = math.pi
+        e = xp.exp(z)
+        return (-1.0 * mu_m(r) * (-7.0 * xp.sin(2.0 * x) * xp.cos(2.0 * y) * e)
+                + -4.0 * pi * xp.cos(z) * xp.cos(4.0 * pi * x) * 2.0 * xp.cos(2.0 * x) * xp.cos(2.0 * y) * e
+                + -4.0 * pi * xp.cos(z) * xp.cos(4.0 * pi * y) * (-2.0) * xp.sin(2.0 * x) * xp.sin(2.0 * y) * e
+                + 2.0 * xp.cos(2.0 * pi * (x + y)) * xp.sin(2.0 * pi * (x - y)) * xp.sin(z) * xp.sin(2.0 * x)
+                * xp.cos(2.0 * y) * e)
+
+    def f_p(r):
+        x, y, z, xp = _xyz(r)
+        t = (y - x) / 3.0
+        L = xp.log(x + y + 3.0)
+        cz = xp.cos(z)
+        return -1.0 * (_poly(t) * (-2.0) * cz / (x + y + 3.0) ** 2
+                       + 2.0 * (16.0 * 5.0 * 4.0 * (1.0 / 9.0) * t ** 3 - 20.0 * 3.0 * 2.0 * (1.0 / 9.0) * t) * L * cz
+                       + -1.0 * _poly(t) * L * cz)
+
+    def beta(r):
+        x, y, z, xp = _xyz(r)
+        gx, gy, gz = grad_phi(r)
+        t = (y - x) / 3.0
+        P = _poly(t)
+        dP = (80.0 * t ** 4 - 60.0 * t ** 2 + 5.0) / 3.0  # d/dy; d/dx = -dP
+        L = xp.log(x + y + 3.0)
+        s3 = x + y + 3.0
+        cz, sz = xp.cos(z), xp.sin(z)
+        gup = (-dP * L * cz + P * cz / s3, dP * L * cz + P * cz / s3, -P * L * sz)
+        e = xp.exp(z)
+        s2x, c2x, s2y, c2y = xp.sin(2.0 * x), xp.cos(2.0 * x), xp.sin(2.0 * y), xp.cos(2.0 * y)
+        gum = (2.0 * c2x * c2y * e, -2.0 * s2x * s2y * e, s2x * c2y * e)
+        mp, mm = 1.0, mu_m(r)
+        d = (mp * gup[0] - mm * gum[0]) * gx + (mp * gup[1] - mm * gum[1]) * gy + (mp * gup[2] - mm * gum[2]) * gz
+        return xp.nan_to_num(d * (-1.0))
+
+    zero = lambda r: _xyz(r)[3].full(0.0)  # noqa: E731
+    return _assemble(phi, u_m, u_p, mu_m, mu_p, zero, zero, f_m, f_p, beta)
+
+
 def _assemble(phi, u_m, u_p, mu_m, mu_p, k_m, k_p, f_m, f_p, beta):
     def alpha(r):
         return u_p(r) - u_m(r)

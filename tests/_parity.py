@@ -32,18 +32,21 @@ def make_problem(name):
 class Case:
     """A grid problem at one stencil level with a fixed parameter vector."""
 
-    def __init__(self, name="sphere", n=16, arch=(1, 1, 2, 10), level=0, seed=0, batch=None, batch_seed=0):
+    def __init__(self, name="sphere", n=16, arch=(1, 1, 2, 10), level=0, seed=0, batch=None, batch_seed=0,
+                 fns=None, phi=None, params=None, ids=None):
         self.name = name
-        self.fns = make_problem(name)
+        self.fns = fns if fns is not None else make_problem(name)
         self.grid = mesh.uniform_grid(n)
         g = self.grid
-        self.phi = O.perturb(np.asarray(self.fns["phi"](g.R.T), F32))
+        self.phi = phi if phi is not None else O.perturb(np.asarray(self.fns["phi"](g.R.T), F32))
         self.h = np.array([g.dx, g.dy, g.dz], F32) * F32(0.5**level)
         self.arch = L.Arch(*arch)
-        self.params = L.init_params(self.arch, seed)
+        self.params = params if params is not None else L.init_params(self.arch, seed)
         self.pts = g.R
         self.batch = None
-        if batch is not None:
+        if ids is not None:
+            self.batch = np.asarray(ids, np.int32)
+        elif batch is not None:
             rng = np.random.default_rng(batch_seed)
             self.batch = np.sort(rng.choice(g.R.shape[0], batch, replace=False)).astype(np.int32)
         self._rg = None
@@ -123,3 +126,26 @@ class Case:
 
 def build_case(name="sphere", n=16, arch=(1, 1, 2, 10), level=0, **kw):
     return Case(name, n, arch, level, **kw)
+
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def reference_fixtures():
+    """Names of the fixtures written by the reference's own code (tests/golden/ref_*.npz)."""
+    return sorted(f[4:-4] for f in os.listdir(GOLDEN) if f.startswith("ref_") and f.endswith(".npz"))
+
+
+def load_reference_fixture(key):
+    return dict(np.load(os.path.join(GOLDEN, f"ref_{key}.npz")))
+
+
+def reference_case(key):
+    """The parity case of a reference fixture: its problem, grid, level, network, phi samples,
+    parameters and batch, fed unchanged to the oracle and to the CUDA path."""
+    from golden import make_reference_golden as M
+
+    fx = load_reference_fixture(key)
+    prob = str(fx["problem"])
+    return Case(prob, int(fx["n"]), tuple(int(v) for v in fx["arch"]), int(fx["level"]), fns=M.problem(prob),
+                phi=fx["phi"], params=fx["params"], ids=fx["ids"]), fx

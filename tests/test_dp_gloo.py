@@ -99,6 +99,7 @@ def test_two_rank_gradient_sum_and_update():
         ref_l += l
     for r in range(world):
         g, lo, new, _, _ = res[r]
-        np.testing.assert_allclose(g, ref_g, rtol=1e-6, atol=1e-9)
+        # float32 sums in the ranks' processes may use another thread split than this one's
+        np.testing.assert_allclose(g, ref_g, rtol=1e-5, atol=1e-8)
         assert abs(lo - ref_l) <= 1e-6 * abs(ref_l)
     np.testing.assert_array_equal(res[0][2], res[1][2])  # both ranks apply the same update
