@@ -229,6 +229,39 @@ int dips_train_step_profiled(const dips_arch_t* arch, const dips_adam_t* hp, flo
 int dips_train_step_noalloc(const dips_arch_t* arch, const dips_adam_t* hp, float* params, float* mu, float* nu,
                             int64_t* count, const dips_records_t* rec, const int32_t* batch_ids, int64_t batch,
                             int64_t max_jobs, double* loss_out, float* grad_out, cudaStream_t stream);
+/* ---- XLA custom calls: replace Trainer.loss (trainer.py:892-912) and its value_and_grad in
+        Trainer.update (:783-789) inside a jitted JAX program, as the forward and backward of a
+        jax.custom_vjp.  XLA's GPU custom-call ABI with a status argument
+        (API_VERSION_STATUS_RETURNING); buffers are device pointers XLA planned:
+          dips_xla_loss_fwd  operands: params f32[P], batch ids i32[B]
+                             results:  loss f32[], residual f32[B], workspace u8[ws_bytes]
+          dips_xla_loss_bwd  operands: params f32[P], batch ids i32[B], cotangent of the loss f32[]
+                             results:  d loss/d params (times the cotangent) f32[P], workspace u8[ws_bytes]
+        opaque = the bytes of a dips_xla_desc_t.  The handlers allocate nothing (the workspace is
+        an XLA result the caller discards); the backward recomputes the forward.  A failure is
+        reported through XlaCustomCallStatusSetFailure (found in the process's global symbol
+        scope, or set with dips_xla_set_status_fn) and dips_last_error. ------------------------ */
+typedef struct XlaCustomCallStatus_ XlaCustomCallStatus; /* opaque, owned by XLA */
+typedef void (*dips_xla_status_fn)(XlaCustomCallStatus* status, const char* message, size_t message_len);
+#define DIPS_XLA_MAGIC 0x44495053u /* "DIPS" */
+typedef struct {
+  uint32_t magic;               /* DIPS_XLA_MAGIC */
+  uint32_t version;             /* 1 */
+  dips_arch_t arch;
+  const dips_records_t* rec;    /* host pointer to the level's records, alive while the program runs */
+  int64_t batch;                /* B */
+  int64_t max_jobs;             /* job bound of any batch of B points of this level */
+  uint64_t ws_bytes;            /* size of the workspace result (dips_xla_workspace_bytes) */
+} dips_xla_desc_t;
+size_t dips_xla_workspace_bytes(const dips_arch_t* arch, int64_t batch, int64_t max_jobs);
+int dips_xla_make_desc(const dips_arch_t* arch, const dips_records_t* rec, int64_t batch, int64_t max_jobs,
+                       dips_xla_desc_t* out);
+void dips_xla_set_status_fn(dips_xla_status_fn fn);
+void dips_xla_loss_fwd(cudaStream_t stream, void** buffers, const char* opaque, size_t opaque_len,
+                       XlaCustomCallStatus* status);
+void dips_xla_loss_bwd(cudaStream_t stream, void** buffers, const char* opaque, size_t opaque_len,
+                       XlaCustomCallStatus* status);
+
 /* ---- many instances trained together (configuration 4; no counterpart in the reference,
         whose LPBE example trains its molecules one after another): each instance has its own
         records, batch, parameters, optimizer state and workspace; all share the network shape

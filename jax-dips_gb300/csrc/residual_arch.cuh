@@ -6,10 +6,10 @@
 // which reads the weights from the parameter buffer.  The other shapes use the kernels below;
 // each network (u- and u+) gets its own launches, so a kernel holds one network's fully
 // unrolled code:
-//   forward  one thread per job; the weights are constant-bank operands of FFMA
+//   forward  one thread per job; the weights are broadcast shared-memory operands
 //   adjoint  one thread per job recomputes the activations and stages them in the warp's
 //            shared-memory tile; the output gradients propagate thread-per-job (again with
-//            constant operands) and overwrite the tile in place; each layer's dW is a warp
+//            broadcast shared-memory weights) and overwrite the tile in place; each layer's dW is a warp
 //            GEMM over the tile's 32 jobs (lane = output unit, broadcast float4 rows)
 //            accumulated with shared-memory atomics into one CTA accumulator, written out
 //            as one partial gradient row per CTA.
@@ -26,8 +26,23 @@
 namespace dips {
 namespace DIPS_NS {
 
-constexpr int kMaxConstParams = 15360;  // 60 KB of the 64 KB constant bank
-static __constant__ float c_w[kMaxConstParams];
+// The weights of both networks, copied from the call's parameter buffer (Workspace::params, or
+// the evaluation's params argument) into shared memory by every kernel that reads them, before
+// anything else (load_weights).  Two copies: forward operands at 0 and backward operands at
+// kParams, the offsets the device functions below index.  Each launch reads its own call's
+// parameters, so calls on different streams or threads share no state.
+constexpr int kArchParams = (3 * DIPS_WM + DIPS_WM + (DIPS_LM - 1) * (DIPS_WM * DIPS_WM + DIPS_WM) + DIPS_WM + 1) +
+                            (3 * DIPS_WP + DIPS_WP + (DIPS_LP - 1) * (DIPS_WP * DIPS_WP + DIPS_WP) + DIPS_WP + 1);
+static __shared__ float c_w[2 * kArchParams];
+
+__device__ __forceinline__ void load_weights(const float* __restrict__ params) {
+  for (int i = threadIdx.x; i < kArchParams; i += blockDim.x) {
+    const float v = __ldg(params + i);
+    c_w[i] = v;
+    c_w[kArchParams + i] = v;
+  }
+  __syncthreads();
+}
 
 constexpr int kThreads = kAdjThreads;
 constexpr int kWarps = kThreads / 32;
@@ -215,7 +230,7 @@ __device__ __forceinline__ void tile_gemm(const float* H, const float* D, float*
 
 // Backward half of a tile whose activations are staged in `tile` (h = last hidden layer of
 // this lane's job, g = d loss / d u of this lane's job): output-layer grads, then for each
-// hidden layer the delta (thread per job, constant operands) and the dW warp GEMM.
+// hidden layer the delta (thread per job, shared-memory weights) and the dW warp GEMM.
 template <class N, int OFF, int BOFF>
 __device__ __forceinline__ void net_backward_tile(const float h[N::kW], float g, float* tile, float* acc, int lane) {
   constexpr int W = N::kW, L = N::kL, BUF = 32 * N::kRow;
@@ -286,6 +301,7 @@ __device__ __forceinline__ void net_adjoint_tile(const float x[3], float g, floa
 
 template <class N, int OFF>
 __global__ void __launch_bounds__(256) k_job_forward(PtsH ph, const int32_t* __restrict__ ids, Workspace w, int net_p) {
+  load_weights(w.params);
   const Ctl ctl = *w.ctl;
   const int64_t begin = net_p ? ctl.jm_pad : 0;
   const int64_t end = net_p ? ctl.total : ctl.jm;
@@ -310,7 +326,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_job_adjoint(PtsH ph, const int3
   float* acc = smem;
   float* tile = smem + (N::kParams + 3) / 4 * 4 + warp * N::kTileFloats;
   for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) acc[i] = 0.0f;
-  __syncthreads();
+  load_weights(w.params);
   const Ctl ctl = *w.ctl;
   const int64_t begin = net_p ? ctl.jm_pad : 0;
   const int64_t end = net_p ? ctl.total : ctl.jm;
@@ -357,7 +373,7 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_bulk_fused(PtsH ph, const 
   float* sU = smem + (N::kParams + 3) / 4 * 4 + kStencil * N::kTileFloats;  // [7][32] A_j u_j
   if (BWD)
     for (int i = threadIdx.x; i < N::kParams; i += blockDim.x) acc[i] = 0.0f;
-  __syncthreads();
+  load_weights(w.params);
   const int64_t nb = net_p ? w.ctl->nbp : w.ctl->nbm;
   const int32_t* list = w.bulk + (net_p ? w.B : 0);
   const float Bf = (float)w.B;
@@ -485,9 +501,10 @@ __device__ __forceinline__ float net_eval_grad(const float x[3], float gx[3]) {
 }
 
 template <class N, int OFF, int BOFF>
-__global__ void __launch_bounds__(128) k_mlp_eval(const float* __restrict__ pts, const float* __restrict__ phi,
-                                                  int64_t n, float* __restrict__ u_out, float* __restrict__ g_out,
-                                                  int net_p) {
+__global__ void __launch_bounds__(128) k_mlp_eval(const float* __restrict__ params, const float* __restrict__ pts,
+                                                  const float* __restrict__ phi, int64_t n, float* __restrict__ u_out,
+                                                  float* __restrict__ g_out, int net_p) {
+  load_weights(params);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     if ((phi[i] >= 0.0f) != (net_p != 0)) continue;
     const float x[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
@@ -508,19 +525,11 @@ using A = Arch<DIPS_LM, DIPS_WM, DIPS_LP, DIPS_WP>;
 constexpr bool kTileArch = tile::supported<typename A::M>() && tile::supported<typename A::P>() &&
                            A::M::kW == A::P::kW && A::M::kL == A::P::kL;
 
-static int load_params(const float* params, int for_eval, cudaStream_t s) {
-  static_assert(2 * A::kParams <= kMaxConstParams, "network too large for the constant bank");
-  // the tile engine (training and evaluation) reads the parameters from global memory
-  (void)for_eval;
-  if (kTileArch) return DIPS_OK;
-  // two copies: forward-pass operands at 0, backward-pass operands at kParams (with one
-  // copy the compiler keeps every weight used by both passes in registers)
-  cudaError_t e = cudaMemcpyToSymbolAsync(c_w, params, sizeof(float) * A::kParams, 0, cudaMemcpyDeviceToDevice, s);
-  if (e == cudaSuccess)
-    e = cudaMemcpyToSymbolAsync(c_w, params, sizeof(float) * A::kParams, sizeof(float) * A::kParams,
-                                cudaMemcpyDeviceToDevice, s);
-  return e == cudaSuccess ? DIPS_OK : cuda_status(e, "cudaMemcpyToSymbolAsync(params)");
-}
+// Every kernel reads the parameters of its own call (Workspace::params or an argument): nothing
+// to stage per call, and no state shared between calls.
+static_assert(kArchParams == A::kParams, "parameter count");
+static_assert(kTileArch || 2 * A::kParams * sizeof(float) <= 16 * 1024, "per-job kernels: weights in shared memory");
+static int load_params(const float*, int, cudaStream_t) { return DIPS_OK; }
 
 
 // CTA widths of the tile engine (warps per CTA): width 32 fills an SM with one CTA of 12, 10 or 8
@@ -636,7 +645,7 @@ static int job_forward(const PtsH& ph, const int32_t* ids, const Workspace& w, c
     const dips_records_t none{};
     const int st = tile_launch<tile::kForwardGeneral>(ph, ids, w, none, nullptr, s);
     if (st) return st;
-  } else {  // one thread per job, the weights as constant-bank operands
+  } else {  // one thread per job, the weights in shared memory
     k_job_forward<typename A::M, 0><<<152 * 24, 256, 0, s>>>(ph, ids, w, 0);
     mark(mk, kMarkFwdM, s);
     k_job_forward<typename A::P, A::kOffP><<<152 * 24, 256, 0, s>>>(ph, ids, w, 1);
@@ -743,8 +752,8 @@ static int mlp_eval(const float* params, const float* pts, const float* phi, int
   if constexpr (kTileArch) return tile_eval(params, pts, phi, n, u, g, s);
   int64_t grid = (n + 127) / 128;
   if (grid > 152 * 16) grid = 152 * 16;
-  k_mlp_eval<typename A::M, 0, A::kParams><<<(int)grid, 128, 0, s>>>(pts, phi, n, u, g, 0);
-  k_mlp_eval<typename A::P, A::kOffP, A::kParams><<<(int)grid, 128, 0, s>>>(pts, phi, n, u, g, 1);
+  k_mlp_eval<typename A::M, 0, A::kParams><<<(int)grid, 128, 0, s>>>(params, pts, phi, n, u, g, 0);
+  k_mlp_eval<typename A::P, A::kOffP, A::kParams><<<(int)grid, 128, 0, s>>>(params, pts, phi, n, u, g, 1);
   DIPS_CHECK_LAUNCH("mlp eval");
   return DIPS_OK;
 }

@@ -38,6 +38,7 @@ UNITS = {
     "residual_static.cu": [],
     "residual_tc.cu": [],
     "precond.cu": [],
+    "xla_shim.cu": [],
 }
 
 _lock = threading.Lock()
@@ -206,6 +207,14 @@ class KrylovStatsT(ctypes.Structure):
                 ("rel_residual", ctypes.c_double), ("rel_linf", c_f32)]
 
 
+class XlaDescT(ctypes.Structure):
+    _fields_ = [("magic", ctypes.c_uint32), ("version", ctypes.c_uint32), ("arch", ArchT), ("rec", c_void_p),
+                ("batch", c_i64), ("max_jobs", c_i64), ("ws_bytes", ctypes.c_uint64)]
+
+
+# void (*)(XlaCustomCallStatus*, const char*, size_t)
+XlaStatusFn = ctypes.CFUNCTYPE(None, c_void_p, ctypes.c_char_p, ctypes.c_size_t)
+
 P = ctypes.POINTER
 _SIGS = {
     "dips_last_error": (ctypes.c_char_p, []),
@@ -285,6 +294,11 @@ _SIGS = {
          ctypes.c_size_t, P(KrylovStatsT), c_void_p],
     ),
     "dips_bicgstab_workspace_bytes": (ctypes.c_size_t, [c_i64]),
+    "dips_xla_workspace_bytes": (ctypes.c_size_t, [P(ArchT), c_i64, c_i64]),
+    "dips_xla_make_desc": (c_i32, [P(ArchT), P(RecordsT), c_i64, c_i64, P(XlaDescT)]),
+    "dips_xla_set_status_fn": (None, [XlaStatusFn]),
+    "dips_xla_loss_fwd": (None, [c_void_p, P(c_void_p), c_void_p, ctypes.c_size_t, c_void_p]),
+    "dips_xla_loss_bwd": (None, [c_void_p, P(c_void_p), c_void_p, ctypes.c_size_t, c_void_p]),
 }
 
 

@@ -20,6 +20,7 @@ MIRRORS = {
     "dips_adam_t": _lib.AdamT,
     "dips_instance_t": _lib.InstanceT,
     "dips_krylov_stats_t": _lib.KrylovStatsT,
+    "dips_xla_desc_t": _lib.XlaDescT,
 }
 
 
