@@ -219,13 +219,21 @@ int dips_train_step_profiled(const dips_arch_t* arch, const dips_adam_t* hp, flo
                              int64_t* count, const dips_records_t* rec, const int32_t* batch_ids, int64_t batch,
                              void* workspace, size_t ws_bytes, double* loss_out, float* grad_out,
                              cudaEvent_t* events, int32_t n_events, cudaStream_t stream);
+/* Polls of the 4x64 tensor-core engine's mbarrier waits before a CTA gives up (default 2^24);
+   returns the previous value.  A give-up sets the step's error flag: the loss and gradient come
+   out NaN, the CTA waits (with the default bound) for its MMAs in flight and frees its tensor
+   memory, and the next call starts clean.  For tests of that path; it applies to launches made
+   after the call, from any thread.  No counterpart in the reference. */
+uint32_t dips_tc_set_wait_limit(uint32_t polls);
 /* dips_train_step without a workspace argument, for callers that cannot allocate device
    memory (e.g. an XLA custom-call handler, which gets only the buffers XLA planned for it).
    No counterpart in the reference.  The scratch is a 64 MiB device array inside the library:
    every GPU that loads it keeps the 64 MiB until exit; batches whose workspace for max_jobs
    jobs (dips_step_workspace_bytes) exceeds it fail with DIPS_E_WORKSPACE; the first call on a
-   device resolves the array's address (make it before any stream capture); all calls share
-   the array, so calls that overlap on the GPU race.  Allocates nothing. */
+   device resolves the array's address (make it before any stream capture) and keeps it for the
+   life of the process, so it is invalid after cudaDeviceReset (or any other teardown of the
+   device's primary context): do not reset a device between calls; all calls share the array,
+   so calls that overlap on the GPU race.  Allocates nothing. */
 int dips_train_step_noalloc(const dips_arch_t* arch, const dips_adam_t* hp, float* params, float* mu, float* nu,
                             int64_t* count, const dips_records_t* rec, const int32_t* batch_ids, int64_t batch,
                             int64_t max_jobs, double* loss_out, float* grad_out, cudaStream_t stream);

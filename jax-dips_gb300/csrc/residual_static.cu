@@ -15,7 +15,9 @@
 //  * Every GPU that loads this module keeps the 64 MiB until the process exits.
 //  * The first call on a device resolves the array's device address with
 //    cudaGetSymbolAddress (with that device current); make that first call before any
-//    stream capture.
+//    stream capture.  The address is kept for the life of the process: after cudaDeviceReset
+//    (or any other teardown of the device's primary context) the module is loaded again and
+//    the cached address is stale, so do not reset a device between calls.
 //  * All calls share the one array and it keeps the previous call's contents.  The step
 //    writes every scratch byte it later reads within the same call, so nothing has to be
 //    cleared; but two calls that overlap on the GPU (different streams, no ordering between

@@ -27,7 +27,10 @@
 //
 // Operands are rounded to TF32 (cvt.rna) when written; the accumulators are FP32.  Every wait
 // on an mbarrier is bounded: on a timeout the CTA records Ctl::engine_error (the loss and the
-// gradient then come out NaN), stops at the next barrier and frees its TMEM.
+// gradient then come out NaN), stops at the next barrier, waits (bounded) for the MMAs it has in
+// flight and frees its TMEM.
+
+#include <atomic>
 
 #include "residual_common.cuh"
 
@@ -44,6 +47,9 @@ constexpr int kThreads = 256;  // two threads per job: features [0, 32) and [32,
 constexpr int kTile = 128;
 constexpr int kHalf = 32;
 constexpr int kGrid = kTileGrid;
+// polls of an mbarrier wait before the CTA gives up (kernel argument; dips_tc_set_wait_limit
+// changes it for tests of the timeout path); the wait for MMAs still in flight after a give-up
+// always uses kWaitLimit
 constexpr uint32_t kWaitLimit = 1u << 24;
 
 // ---- shared-memory operand layouts ---------------------------------------------------------
@@ -93,9 +99,9 @@ __device__ __forceinline__ void mma_ts(uint32_t d, uint32_t a, uint64_t b, uint3
 __device__ __forceinline__ void commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar)));
 }
-__device__ __forceinline__ bool wait_phase(uint64_t* bar, uint32_t phase) {
+__device__ __forceinline__ bool wait_phase(uint64_t* bar, uint32_t phase, uint32_t limit) {
   uint32_t done = 0;
-  for (uint32_t it = 0; it < kWaitLimit && !done; ++it)
+  for (uint32_t it = 0; it < limit && !done; ++it)
     asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
                  : "=r"(done)
                  : "r"(saddr(bar)), "r"(phase));
@@ -180,6 +186,16 @@ __device__ __forceinline__ void tmem_free(uint32_t base, uint32_t cols) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(base), "r"(cols));
 }
 
+// After a give-up (s_abort): every thread left its loop at the barrier before the next issue,
+// so at most one commit group is in flight, the one of the wait that gave up, whose parity is
+// phase ^ 1 (each wait flips phase).  Thread 0 waits for it (bounded, kWaitLimit polls; a
+// completed phase returns at once) before the CTA frees its TMEM.
+__device__ __forceinline__ void drain_after_abort(uint64_t* bar, uint32_t phase, const int& s_abort) {
+  __syncthreads();
+  if (s_abort && threadIdx.x == 0) (void)wait_phase(bar, phase ^ 1u, kWaitLimit);
+  __syncthreads();
+}
+
 // h1 = tanh(W1^T x + b1) for features [f0, f0 + 32), on the FP32 pipe
 __device__ __forceinline__ void layer1(const float* small, const float x[3], float* h, int f0) {
 #pragma unroll
@@ -250,7 +266,7 @@ __device__ __forceinline__ void issue_dw(uint32_t d, const unsigned char* a, uin
 constexpr size_t kFwdSmem = 3 * kWBytes + sizeof(float) * kSmallFloats + 64;
 
 __global__ void __launch_bounds__(kThreads, kFwdCtasPerSm) k_tc_forward(const float* __restrict__ params, int off,
-                                                                        Workspace w, int net_p) {
+                                                                        Workspace w, int net_p, uint32_t wait_limit) {
   extern __shared__ __align__(1024) unsigned char sm[];
   unsigned char* wf = sm;
   float* small = reinterpret_cast<float*>(sm + 3 * kWBytes);
@@ -293,7 +309,7 @@ __global__ void __launch_bounds__(kThreads, kFwdCtasPerSm) k_tc_forward(const fl
         issue_fwd(tb, wf + l * kWBytes);
         commit(bar);
       }
-      if (!wait_phase(bar, phase)) {
+      if (!wait_phase(bar, phase, wait_limit)) {
         s_abort = 1;
         w.ctl->engine_error = 1;
       }
@@ -311,6 +327,7 @@ __global__ void __launch_bounds__(kThreads, kFwdCtasPerSm) k_tc_forward(const fl
     __syncthreads();
     if (!f0 && j < jend) w.ju[j] = u + s_u[job] + small[8 * W];
   }
+  drain_after_abort(bar, phase, s_abort);
   fence_before();
   __syncthreads();
   fence_after();
@@ -336,7 +353,8 @@ constexpr int kBulkPts = 18;
 
 template <bool BWD>
 __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restrict__ params, int off, Workspace w,
-                                                            int net_p, PtsH ph, float* __restrict__ residual_out) {
+                                                            int net_p, PtsH ph, float* __restrict__ residual_out,
+                                                            uint32_t wait_limit) {
   extern __shared__ __align__(1024) unsigned char sm[];
   unsigned char* wf = sm + kOffWF;
   unsigned char* wb = sm + kOffWB;
@@ -384,7 +402,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
   uint32_t phase = 0;
   bool first = true;
   auto wait = [&]() {
-    if (!wait_phase(bar, phase)) {
+    if (!wait_phase(bar, phase, wait_limit)) {
       s_abort = 1;
       w.ctl->engine_error = 1;
     }
@@ -588,6 +606,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     wait();
     first = false;
   }
+  drain_after_abort(bar, phase, s_abort);
   // ---- loss partial of the bulk points of this CTA
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
@@ -702,6 +721,7 @@ __global__ void __launch_bounds__(128) k_tc_eval(const float* __restrict__ param
 // passes them through load_params, which records the pointer for the launches that follow on
 // the calling thread.
 thread_local const float* t_params = nullptr;
+std::atomic<uint32_t> g_wait_limit{kWaitLimit};
 
 static int load_params(const float* params, int, cudaStream_t) {
   t_params = params;
@@ -720,9 +740,10 @@ static int job_forward(const PtsH&, const int32_t*, const Workspace& w, const Ma
   static bool attr = false;
   int st = set_smem((const void*)k_tc_forward, kFwdSmem, &attr);
   if (st) return st;
-  k_tc_forward<<<kGrid * kFwdCtasPerSm, kThreads, kFwdSmem, s>>>(t_params, 0, w, 0);
+  const uint32_t lim = g_wait_limit.load();
+  k_tc_forward<<<kGrid * kFwdCtasPerSm, kThreads, kFwdSmem, s>>>(t_params, 0, w, 0, lim);
   mark(mk, kMarkFwdM, s);
-  k_tc_forward<<<kGrid * kFwdCtasPerSm, kThreads, kFwdSmem, s>>>(t_params, kNetParams, w, 1);
+  k_tc_forward<<<kGrid * kFwdCtasPerSm, kThreads, kFwdSmem, s>>>(t_params, kNetParams, w, 1, lim);
   mark(mk, kMarkFwdP, s);
   DIPS_CHECK_LAUNCH("tcgen05 forward");
   return DIPS_OK;
@@ -740,9 +761,10 @@ static int adjoint_pair(const PtsH& ph, const Workspace& w, float* residual_out,
   static bool attr = false;
   int st = set_smem((const void*)k_tc_adjoint<BWD>, kAdjSmem, &attr);
   if (st) return st;
-  k_tc_adjoint<BWD><<<kGrid, kThreads, kAdjSmem, s>>>(t_params, 0, w, 0, ph, residual_out);
+  const uint32_t lim = g_wait_limit.load();
+  k_tc_adjoint<BWD><<<kGrid, kThreads, kAdjSmem, s>>>(t_params, 0, w, 0, ph, residual_out, lim);
   mark(mk, kMarkFusedM, s);
-  k_tc_adjoint<BWD><<<kGrid, kThreads, kAdjSmem, s>>>(t_params, kNetParams, w, 1, ph, residual_out);
+  k_tc_adjoint<BWD><<<kGrid, kThreads, kAdjSmem, s>>>(t_params, kNetParams, w, 1, ph, residual_out, lim);
   mark(mk, kMarkFusedP, s);
   DIPS_CHECK_LAUNCH("tcgen05 bulk / adjoint");
   return DIPS_OK;
@@ -764,6 +786,10 @@ static int mlp_eval(const float*, const float* pts, const float* phi, int64_t n,
 }
 
 }  // namespace tcnet
+
+// Polls of the tensor-core engine's mbarrier waits (default 2^24), for tests of the timeout
+// path; returns the previous value.  Affects launches made after the call, from any thread.
+extern "C" uint32_t dips_tc_set_wait_limit(uint32_t polls) { return tcnet::g_wait_limit.exchange(polls); }
 
 const ArchOps* arch_ops_4_64_4_64() {
   static const ArchOps ops = {4, 64, 4, 64, tcnet::kParams, 1, tcnet::load_params, tcnet::job_forward,

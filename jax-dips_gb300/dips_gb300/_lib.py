@@ -294,6 +294,7 @@ _SIGS = {
          ctypes.c_size_t, P(KrylovStatsT), c_void_p],
     ),
     "dips_bicgstab_workspace_bytes": (ctypes.c_size_t, [c_i64]),
+    "dips_tc_set_wait_limit": (ctypes.c_uint32, [ctypes.c_uint32]),
     "dips_xla_workspace_bytes": (ctypes.c_size_t, [P(ArchT), c_i64, c_i64]),
     "dips_xla_make_desc": (c_i32, [P(ArchT), P(RecordsT), c_i64, c_i64, P(XlaDescT)]),
     "dips_xla_set_status_fn": (None, [XlaStatusFn]),

@@ -6,6 +6,7 @@ from __future__ import annotations
 
 import ctypes
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -167,3 +168,50 @@ def batch_ids(n: int, batch: int, epoch: int, batch_index: int, seed: int = 0, o
     _lib.check(lib.dips_batch_ids(n, epoch, seed, batch_index, batch, _lib.ptr(out), _lib.stream_handle()),
                "dips_batch_ids")
     return out
+
+
+class LbfgsResult:
+    def __init__(self, params, loss, iterations, evaluations, message, stopped):
+        self.params, self.loss, self.iterations, self.evaluations = params, loss, iterations, evaluations
+        self.message, self.stopped = message, stopped
+
+
+def lbfgs_minimize(arch: Arch, params: torch.Tensor, level: FVLevel, batch_ids=None, maxiter: int = 1000,
+                   tol: float = 1e-15, callback=None, ws: StepWorkspace = None) -> LbfgsResult:
+    """The reference's full-batch L-BFGS path (optimizer_name "lbfgs": trainer.py:204-206 and
+    ``solve_jaxopt`` :354-420, i.e. ``jaxopt.ScipyMinimize(method="l-bfgs-b", tol=1e-15,
+    maxiter=num_epochs)`` on the loss of one batch): scipy's L-BFGS-B over the flat parameter
+    vector in float64, with the loss and its gradient from this library's kernels
+    (``dips_residual_fwd`` / ``dips_residual_bwd``).  ``params`` is updated in place.
+
+    ``callback(params, loss)`` runs after every iteration with the current parameters on the
+    device and their loss; returning True stops the minimisation (scipy's StopIteration)."""
+    from scipy.optimize import minimize
+
+    B = level.n if batch_ids is None else int(batch_ids.numel())
+    if ws is None or not ws.fits(arch, B, level.max_jobs(B)):
+        ws = StepWorkspace(arch, B, level.max_jobs(B), params.device)
+    host = torch.empty(params.numel(), dtype=torch.float32, pin_memory=True)
+    counts = {"evals": 0, "iters": 0, "stopped": False, "last": float("nan")}
+
+    def fun(x):
+        host.copy_(torch.from_numpy(x.astype(np.float32)))
+        params.copy_(host, non_blocking=True)
+        loss, _, _ = residual_forward(arch, params, level, batch_ids, ws)
+        grad = residual_backward(arch, params, level, batch_ids, ws)
+        counts["evals"] += 1
+        counts["last"] = float(loss)
+        return counts["last"], grad.double().cpu().numpy()
+
+    def cb(xk):
+        counts["iters"] += 1
+        if callback is not None:
+            params.copy_(torch.from_numpy(xk.astype(np.float32)))
+            if callback(params, counts["last"]):
+                counts["stopped"] = True
+                raise StopIteration
+
+    x0 = params.detach().double().cpu().numpy()
+    res = minimize(fun, x0, jac=True, method="L-BFGS-B", tol=tol, options={"maxiter": int(maxiter)}, callback=cb)
+    params.copy_(torch.from_numpy(np.asarray(res.x, np.float32)))
+    return LbfgsResult(params, float(res.fun), counts["iters"], counts["evals"], str(res.message), counts["stopped"])

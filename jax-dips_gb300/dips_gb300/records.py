@@ -3,7 +3,7 @@
 The reference recomputes the whole parameter-independent part of the residual --
 cell decomposition, face areas, interface quadrature, regression extrapolation --
 for every point at every step (solvers/poisson/discretization.py:299-519).  Here it
-is computed once per (point, h) by three HBM-streaming kernels:
+is computed once per (point, h) by the geometry kernels:
 
 1. ``dips_geometry_classify``  flags and counts per point
 2. ``dips_geometry_queries``   the points where coefficient callables are needed
@@ -14,6 +14,8 @@ is computed once per (point, h) by three HBM-streaming kernels:
 """
 
 from __future__ import annotations
+
+import time
 
 import numpy as np
 import torch
@@ -44,9 +46,21 @@ def _excl_scan(counts: torch.Tensor) -> torch.Tensor:
 class FVLevel:
     """Residual records of the points ``pts`` at stencil spacing ``h`` (device tensors)."""
 
-    def __init__(self, ls: LevelSetGrid, coeff_fns: dict, pts: torch.Tensor, h, keep_geometry=False):
+    def __init__(self, ls: LevelSetGrid, coeff_fns: dict, pts: torch.Tensor, h, keep_geometry=False, profile=False):
         lib = _lib.load()
         dev = pts.device
+        # profile: host seconds per set-up phase (device synchronised at each boundary)
+        self.timings = {} if profile else None
+        _t = [time.perf_counter()]
+
+        def mark(name):
+            if profile:
+                torch.cuda.synchronize(dev)
+                now = time.perf_counter()
+                self.timings[name] = now - _t[0]
+                _t[0] = now
+
+        mark("start")
         self.ls = ls
         self.pts = pts.to(torch.float32).contiguous()
         n = self.pts.shape[0]
@@ -64,6 +78,7 @@ class FVLevel:
             lib.dips_geometry_classify(ls.desc, P(self.pts), n, hc, P(flags), P(n_tri), P(n_xs), P(cap), st),
             "dips_geometry_classify",
         )
+        mark("classify")
         tri_off = _excl_scan(n_tri)
         xs_off = _excl_scan(n_xs)
         self.job_off = _excl_scan(cap)
@@ -82,6 +97,7 @@ class FVLevel:
         tri_pts = tri_pts[: 3 * n_tri_tot]
         xs_pts = xs_pts[:n_xs_tot]
         xr_pts = xr_pts[:n_xs_tot]
+        mark("scans_and_queries")
 
         # ---- coefficient callables (reference semantics: evaluated at exactly these points)
         fn = coeff_fns
@@ -112,6 +128,7 @@ class FVLevel:
             if v.numel() == 0:
                 vals[k] = torch.zeros(1, **f32)
         co = _lib.CoeffsT(*[P(vals[k]) for k, _ in _lib.CoeffsT._fields_[:-1]], beta0)
+        mark("coefficient_callables")
 
         self.lhs0 = torch.empty(n, **f32)
         self.diag = torch.empty(n, **f32)
@@ -128,6 +145,7 @@ class FVLevel:
                                        P(self.job_code), P(self.job_A), P(self.coeff26), P(self.beta_int), st),
             "dips_geometry_assemble",
         )
+        mark("assemble")
         self.flags = flags if keep_geometry else None
         self.n_tri, self.n_xs = (n_tri, n_xs) if keep_geometry else (None, None)
         self._vals = vals if keep_geometry else None
@@ -144,6 +162,7 @@ class FVLevel:
         if n:
             _lib.check(lib.dips_pack_bulk_records(self.desc, P(self.bulk_rec), st), "dips_pack_bulk_records")
         self.desc.bulk_rec = P(self.bulk_rec)
+        mark("pack_bulk_records")
 
     def coefficient_tangent(self, dfns: dict) -> "TangentRecords":
         """Derivative of the records along a direction in coefficient space.

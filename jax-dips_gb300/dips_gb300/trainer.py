@@ -20,6 +20,7 @@ import dataclasses
 import logging
 import os
 import pickle
+import re
 from typing import Callable
 
 import numpy as np
@@ -91,7 +92,9 @@ def adam_state_from_dict(n_params, optimizer_dict, device):
     if name == "adam":  # optax.adam: no clipping, constant rate
         return ops.AdamState(n_params, lr=lr, decay_rate=1.0, transition_steps=1000, max_norm=float("inf"),
                              device=device)
-    if name in ("rmsprop", "lbfgs"):
+    if name == "lbfgs":  # Trainer.solve runs scipy's L-BFGS-B instead (solve_jaxopt, trainer.py:354-420)
+        return None
+    if name == "rmsprop":
         raise NotImplementedError(f"optimizer {name!r} is outside the GB300 path")
     raise ValueError(f"Unknown optimizer: {name}")
 
@@ -168,7 +171,10 @@ class Trainer:
         # ---- params and optimizer
         P = nn.n_params(self.arch)
         self.params = torch.as_tensor(nn.init_params(self.arch, 42 if seed is None else seed), device=device)
+        self.optimizer_name = (optimizer_dict or DEFAULT_OPTIMIZER).get("optimizer_name", "custom")
         self.opt = adam_state_from_dict(P, optimizer_dict or DEFAULT_OPTIMIZER, device)
+        if self.opt is None:  # L-BFGS: no optimizer state on the device; the checkpoint keeps a zero one
+            self.opt = ops.AdamState(P, device=device)
         self.epoch_start = 0
         if restart:
             self._restore(restart_checkpoint_dir)
@@ -240,8 +246,33 @@ class Trainer:
             self._step(lvl, ws)
         return g.replay, ws
 
+    def solve_lbfgs(self, print_rate=1, callback=None):
+        """``solve_jaxopt`` (trainer.py:354-420): scipy's L-BFGS-B (tol 1e-15, at most num_epochs
+        iterations) on the loss of the first batch at the training spacing h = dx, the loss and
+        gradient from the GPU kernels.  Returns the iteration numbers and the loss after each."""
+        lvl = self.level(0)
+        ids = torch.arange(self.batch, dtype=torch.int32, device=self.device)  # DatasetDict batch 0
+        losses = []
+
+        def cb(p, loss):
+            losses.append(loss)
+            if print_rate and (len(losses) - 1) % print_rate == 0:
+                logger.info("lbfgs iteration %d loss %.6e", len(losses) - 1, losses[-1])
+            return bool(callback(len(losses) - 1, losses[-1])) if callback is not None else False
+
+        res = ops.lbfgs_minimize(self.arch, self.params, lvl, ids, maxiter=self.num_epochs, tol=1e-15, callback=cb)
+        self.lbfgs_result = res
+        self.epoch_store = np.arange(len(losses))
+        self.loss_epochs = np.asarray(losses)
+        if self.checkpoint_dir:
+            self.save_checkpoint(self.checkpoint_dir, len(losses))
+        return self.epoch_store, self.loss_epochs
+
     def solve(self, print_rate=1, callback=None):
-        """Epoch loop (single_GPU_train, trainer.py:501-591)."""
+        """Epoch loop (single_GPU_train, trainer.py:501-591); with optimizer_name "lbfgs" the
+        reference's solve_jaxopt instead (trainer.py:204-206)."""
+        if self.optimizer_name == "lbfgs":
+            return self.solve_lbfgs(print_rate, callback)
         loss_epochs = np.zeros(self.num_epochs - self.epoch_start)
         q = max(self.num_epochs // 4, 1)
         cur, run = None, None
@@ -297,7 +328,12 @@ class Trainer:
         return io.write_vtk_manual(gstate, fields, filename)
 
     def save_checkpoint(self, checkpoint_dir, epoch):
-        """pickle of {opt_state, params, epoch, batch_size, resolution} (trainer.py:340-351)."""
+        """pickle of {opt_state, params, epoch, batch_size, resolution} (trainer.py:340-351).
+
+        ``params`` is the haiku parameter tree, as the reference stores it.  ``opt_state`` is
+        this library's flat layout {mu, nu, count} (flat float32 moments in the parameter
+        vector's order), not optax's ScaleByAdamState tree: a reference checkpoint's params load
+        here, its optimizer state does not, and the reverse holds as well."""
         os.makedirs(checkpoint_dir, exist_ok=True)
         state = {
             "opt_state": {"mu": self.opt.mu.cpu().numpy(), "nu": self.opt.nu.cpu().numpy(),
@@ -318,12 +354,20 @@ class Trainer:
         number is compared numerically and training resumes at the stored epoch."""
         if not checkpoint_dir or not os.path.isdir(checkpoint_dir):
             return
-        cks = [p for p in os.listdir(checkpoint_dir) if p.startswith("checkpoint_")]
+        # only names this trainer writes ("checkpoint_<epoch>"): a stray "checkpoint_100.tmp" or a
+        # backup copy beside them is skipped, not parsed
+        cks = [p for p in os.listdir(checkpoint_dir) if re.fullmatch(r"checkpoint_(\d+)", p)]
         if not cks:
             return
         best = max(cks, key=lambda p: int(p.split("_")[-1]))
         with open(os.path.join(checkpoint_dir, best), "rb") as f:
             state = pickle.load(f)
+        stored = int(state.get("batch_size", self.batch))
+        if stored != self.batch:
+            # the reference resumes with the checkpoint's batch size (trainer.py:215); the batches
+            # of this trainer are laid out already, so a different size is refused, not adopted
+            raise ValueError(f"checkpoint {best} was written with batch_size {stored}, this trainer uses "
+                             f"{self.batch}; construct it with batch_size={stored} to resume")
         self.params.copy_(nn.tree_to_params(state["params"], self.arch, self.device))
         self.opt.mu.copy_(torch.as_tensor(state["opt_state"]["mu"], device=self.device))
         self.opt.nu.copy_(torch.as_tensor(state["opt_state"]["nu"], device=self.device))

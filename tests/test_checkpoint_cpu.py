@@ -67,3 +67,19 @@ def test_restore_without_checkpoints_changes_nothing(tmp_path):
     Trainer._restore(t, str(tmp_path))
     Trainer._restore(t, "")
     assert torch.equal(t.params, before) and int(t.opt.count) == 5 and t.epoch_start == 0
+
+
+def test_restore_skips_stray_files_and_refuses_another_batch_size(tmp_path):
+    t = _trainer(4, 12)
+    Trainer.save_checkpoint(t, str(tmp_path), 40)
+    for stray in ("checkpoint_100.tmp", "checkpoint_90.bak", "checkpoint_final"):
+        (tmp_path / stray).write_bytes(b"not a pickle")
+    r = _trainer(0, 0)
+    Trainer._restore(r, str(tmp_path))
+    np.testing.assert_array_equal(r.params.numpy(), t.params.numpy())
+    assert r.epoch_start == 40 and int(r.opt.count) == 12
+    other = _trainer(0, 0)
+    other.batch = 2048
+    with pytest.raises(ValueError, match="batch_size 4096"):
+        Trainer._restore(other, str(tmp_path))
+    assert int(other.opt.count) == 0

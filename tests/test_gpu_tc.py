@@ -83,3 +83,34 @@ def test_mlp_eval_4x64():
     (gref,) = torch.autograd.grad(ref.sum(), x)
     np.testing.assert_allclose(u.cpu().numpy(), ref.detach().numpy(), rtol=1e-5, atol=1e-6)
     np.testing.assert_allclose(g.cpu().numpy(), gref.numpy(), rtol=1e-4, atol=1e-5)
+
+
+def test_wait_timeout_gives_nan_and_the_next_call_is_clean():
+    """The bounded mbarrier waits, made to run out: with a limit of 0 polls every wait gives up at
+    once (the MMAs it waited for still complete).  The call must report it -- loss and gradient
+    NaN -- after each CTA waited for its MMAs in flight and freed its tensor memory; the next call
+    at the default limit must give the normal result (an allocation left behind would stall it)."""
+    from dips_gb300 import _lib, ops
+
+    lib = _lib.load()
+    case = _parity.build_case("sphere", n=12, arch=ARCH, level=0)
+    lvl = case.gpu_level()
+    a = case.gpu_arch()
+    params = torch.as_tensor(case.params, device="cuda")
+    l0, _, ws = ops.residual_forward(a, params, lvl)
+    g0 = ops.residual_backward(a, params, lvl, None, ws)
+    torch.cuda.synchronize()
+    old = lib.dips_tc_set_wait_limit(0)
+    try:
+        l1, _, ws = ops.residual_forward(a, params, lvl, ws=ws)
+        g1 = ops.residual_backward(a, params, lvl, None, ws)
+        torch.cuda.synchronize()
+    finally:
+        assert lib.dips_tc_set_wait_limit(old) == 0
+    assert old == 1 << 24
+    assert np.isnan(float(l1)) and torch.isnan(g1).all()
+    l2, _, ws = ops.residual_forward(a, params, lvl, ws=ws)
+    g2 = ops.residual_backward(a, params, lvl, None, ws)
+    torch.cuda.synchronize()
+    assert float(l2) == float(l0)
+    np.testing.assert_allclose(g2.cpu().numpy(), g0.cpu().numpy(), rtol=1e-5, atol=1e-7)
