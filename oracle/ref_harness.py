@@ -201,6 +201,16 @@ def make_harness(mods):
             jax = sys.modules["jax"]
             return jax.vmap(self.compute_Ax_and_b_fn, (None, 0, None, None, None))(params, points, dx, dy, dz)
 
+        # trainer.py:883-890 at chosen rows: lhs/diag - rhs/diag of compute_Ax_and_b_discrete_fn
+        # (discretization.py:522-741) for the nodal vector u on eval_gstate
+        def residual_vector_rows(self, eval_gstate, u, points, dx, dy, dz):
+            jax = sys.modules["jax"]
+            lr = jax.vmap(self.compute_Ax_and_b_discrete_fn, (None, None, 0, None, None, None))(
+                eval_gstate, u, points, dx, dy, dz)
+            lr = np.asarray(refjax._raw(lr))
+            lr = lr.reshape(lr.shape[0], 2)
+            return lr[:, 0] - lr[:, 1]
+
         # trainer.py:892-912
         def loss(self, params, points, dx, dy, dz):
             lr = np.asarray(refjax._raw(self.lhs_rhs(params, points, dx, dy, dz)))

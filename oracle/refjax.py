@@ -18,8 +18,9 @@ code (``tests/golden/make_reference_golden.py``).
 What is restated, and how (jax 0.4.13 semantics, x64 disabled unless ``install(x64=True)``):
 
 * arrays: ``JArray``, an immutable-by-convention ``numpy.ndarray`` subclass with ``.at[].set``
-  and ``.at[].add`` returning copies, indexing that returns 0-d arrays, and augmented
-  assignment that rebinds instead of writing in place;
+  and ``.at[].add`` returning copies, indexing that returns 0-d arrays and clamps
+  out-of-range integer indices as jax's gathers do, and augmented assignment that rebinds
+  instead of writing in place;
 * dtypes: every value is canonicalised to 32-bit types (float32/int32) with x64 off, as jax
   does; the promotion of a binary operation follows jax's lattice with weakly typed Python
   scalars (bool < int < float; a Python float with an int array gives the default float);
@@ -141,6 +142,32 @@ def _unwrap_index(idx):
     return idx
 
 
+def _clamp_index(idx, shape):
+    """jax's gather semantics for integer indices: a negative index counts from the end, then an
+    out-of-range index is clamped into [0, size - 1] (numpy would raise).  Applied to integer and
+    integer-array entries of an index without an Ellipsis; slices and None pass unchanged."""
+    t = idx if isinstance(idx, tuple) else (idx,)
+    if any(e is Ellipsis for e in t):
+        return idx
+    out, axis = [], 0
+    for e in t:
+        if e is None:
+            out.append(e)
+            continue
+        if axis < len(shape) and (isinstance(e, (int, np.integer)) and not isinstance(e, bool)):
+            n = shape[axis]
+            e = int(e)
+            e = e + n if e < 0 else e
+            out.append(min(max(e, 0), n - 1))
+        elif axis < len(shape) and isinstance(e, np.ndarray) and e.dtype.kind in "iu":
+            n = shape[axis]
+            out.append(np.clip(np.where(e < 0, e + n, e), 0, n - 1))
+        else:
+            out.append(e)
+        axis += 1
+    return tuple(out) if isinstance(idx, tuple) else out[0]
+
+
 def _wrap(r):
     """Any numpy result -> JArray with a canonical dtype."""
     if isinstance(r, tuple):
@@ -202,7 +229,8 @@ class JArray(np.ndarray):
         return _At(self)
 
     def __getitem__(self, idx):
-        r = np.ndarray.__getitem__(self.view(np.ndarray), _unwrap_index(idx))
+        raw = self.view(np.ndarray)
+        r = np.ndarray.__getitem__(raw, _clamp_index(_unwrap_index(idx), raw.shape))
         return _wrap(r)
 
     def __setitem__(self, idx, v):  # jax arrays are immutable

@@ -131,9 +131,11 @@ def build_case(name="sphere", n=16, arch=(1, 1, 2, 10), level=0, **kw):
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
-def reference_fixtures():
-    """Names of the fixtures written by the reference's own code (tests/golden/ref_*.npz)."""
-    return sorted(f[4:-4] for f in os.listdir(GOLDEN) if f.startswith("ref_") and f.endswith(".npz"))
+def reference_fixtures(kind="loss"):
+    """Names of the fixtures written by the reference's own code (tests/golden/ref_*.npz):
+    kind "loss" for the network residual cases, "fvop" for the discrete operator of a nodal vector."""
+    names = sorted(f[4:-4] for f in os.listdir(GOLDEN) if f.startswith("ref_") and f.endswith(".npz"))
+    return [k for k in names if k.startswith("fvop_") == (kind == "fvop")]
 
 
 def load_reference_fixture(key):

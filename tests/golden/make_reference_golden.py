@@ -193,9 +193,79 @@ def run_case(args):
     return name, pts.shape[0], float(loss32), out["loss64"], time.time() - t0, t1 - t0
 
 
+# the discrete FV operator of a nodal vector (the plain method's system): name -> (problem, n)
+FV_CASES = {
+    "fvop_sphere16": ("sphere", 16),
+    "fvop_refsphere16": ("refsphere", 16),
+}
+
+
+def fv_rows(n, phi, dx, seed=0):
+    """Rows of the discrete-operator fixture: 96 in the two lowest node layers of some axis
+    (where the reference's interpolant extrapolates the first cell), 96 within 2.5 dx of the
+    interface, 64 others."""
+    rng = np.random.default_rng(seed)
+    ijk = np.stack(np.unravel_index(np.arange(n ** 3), (n, n, n)), 1)
+    low = np.nonzero((ijk <= 1).any(1))[0]
+    near = np.nonzero((np.abs(phi) < 2.5 * dx) & ~(ijk <= 1).any(1))[0]
+    a = rng.choice(low, 96, replace=False)
+    b = rng.choice(near, min(96, near.size), replace=False)
+    rest = np.setdiff1d(np.arange(n ** 3), np.concatenate([a, b]))
+    c = rng.choice(rest, 64, replace=False)
+    return np.sort(np.concatenate([a, b, c])).astype(np.int32)
+
+
+def run_fv_case(args):
+    """``Trainer.residual_vector`` (trainer.py:883-890) of two nodal vectors -- seeded normal
+    values and the exact solution at the nodes -- at a seeded set of rows, float32."""
+    ref_root, name = args
+    import ref_harness as H
+
+    import nbm_loss as L
+    import nbm_oracle as O
+
+    prob_name, n = FV_CASES[name]
+    t0 = time.time()
+    mods = H.load(ref_root, x64=False)
+    import jax.numpy as jnp
+
+    from dips_gb300 import problems
+
+    prob = problem(prob_name)
+    x = jnp.linspace(-1.0, 1.0, n, dtype=jnp.float32)
+    gs = mods["mesh"].construct(3)[0](x, x, x)
+    R = np.asarray(gs.R, F32)
+    phi = O.perturb(np.asarray(prob["phi"](R.T), F32))
+    dx = F32(np.asarray(gs.dx))
+    rows = fv_rows(n, phi, dx)
+    phi_fn = mods["interpolate"].multilinear_interpolation(jnp.asarray(phi), gs)
+    fns = {k: H.per_point(prob[k], F32) for k in ("mu_m", "mu_p", "k_m", "k_p", "f_m", "f_p", "alpha", "beta", "g")}
+    fns["u0"] = lambda r: 0.0
+    hz = H.make_harness(mods)(gs, H.sim_state_fn_from(mods, fns, phi_fn), L.Arch(1, 1, 2, 10))
+    u_rand = np.random.default_rng(5).standard_normal(n ** 3).astype(F32)
+    u_exact = problems.exact_solution(prob, R).astype(F32)
+    out = dict(name=np.array(name), problem=np.array(prob_name), n=np.int32(n), phi=phi, rows=rows,
+               u_rand=u_rand, u_exact=u_exact)
+    P = jnp.asarray(R[rows])
+    for key, u in (("res_rand", u_rand), ("res_exact", u_exact)):
+        out[key] = hz.residual_vector_rows(gs, jnp.asarray(u), P, dx, dx, dx).astype(F32)
+    np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **out)
+    return name, rows.size, float(np.abs(out["res_rand"]).max()), float(np.abs(out["res_exact"]).max()), \
+        time.time() - t0
+
+
 def main(argv):
     ref_root = argv[1] if len(argv) > 1 else DEFAULT_REFERENCE
-    names = argv[2:] or list(CASES)
+    names = argv[2:] or (list(CASES) + list(FV_CASES))
+    fv = [nm for nm in names if nm in FV_CASES]
+    names = [nm for nm in names if nm in CASES]
+    ctx = mp.get_context("spawn")
+    if fv:
+        with ctx.Pool(len(fv)) as pool:
+            for r in pool.imap_unordered(run_fv_case, [(ref_root, nm) for nm in fv]):
+                print("%-28s rows %4d  max|r(u_rand)| %.4e  max|r(u_exact)| %.4e  %.0f s" % r, flush=True)
+    if not names:
+        return
     ctx = mp.get_context("spawn")
     with ctx.Pool(min(len(names), max(1, (os.cpu_count() or 2) - 1))) as pool:
         for r in pool.imap_unordered(run_case, [(ref_root, nm) for nm in names]):

@@ -82,3 +82,38 @@ def test_bicgstab_solves_the_fv_system():
     assert np.abs(x - sol).max() <= 1e-4 * np.abs(sol).max()
     err = np.abs(sol - ex).max() / np.abs(ex).max()
     assert abs(res.rel_linf - err) <= 1e-3
+
+
+@pytest.mark.parametrize("key", _parity.reference_fixtures("fvop"))
+def test_fv_residual_against_the_references_residual_vector(key):
+    """dips_fv_residual against the reference's own residual_vector (trainer.py:883-890, via
+    tests/golden/make_reference_golden.py) for a random nodal vector and the exact solution.
+
+    The reference reads u through its non-oscillatory quadratic interpolant
+    (interpolate.py:572-759).  At a node that is the nodal value, except in the first cell of an
+    axis: its lower-left index is clamped to the second cell, so a node of the lowest layer gets
+    2 u_1 - u_2 + min|second difference| -- not linear in u.  The library's operator reads the
+    nodal values everywhere (a linear operator, which BiCGSTAB needs).  So rows whose stencil or
+    regression cube reaches a node of the lowest layer of some axis -- the rows of the two lowest
+    layers -- may differ; every other row must agree."""
+    from golden import make_reference_golden as M
+
+    from dips_gb300 import krylov
+
+    fx = _parity.load_reference_fixture(key)
+    prob = str(fx["problem"])
+    n = int(fx["n"])
+    case = _parity.Case(prob, n, (1, 1, 2, 10), 0, fns=M.problem(prob), phi=fx["phi"])
+    lvl = case.gpu_level()
+    rows = fx["rows"].astype(np.int64)
+    ijk = np.stack(np.unravel_index(rows, (n, n, n)), 1)
+    low = (ijk <= 1).any(1)
+    assert low.sum() >= 64 and (~low).sum() >= 64
+    for ukey, rkey in (("u_rand", "res_rand"), ("u_exact", "res_exact")):
+        got = krylov.fv_residual(lvl, (n, n, n), torch.as_tensor(fx[ukey], device="cuda")).cpu().numpy()[rows]
+        ref = fx[rkey]
+        scale = float(np.max(np.abs(ref)))
+        err = np.abs(got - ref)
+        assert float(err[~low].max()) <= 3e-5 * scale, (ukey, float(err[~low].max()), scale)
+        bad = err > 3e-5 * scale
+        assert not (bad & ~low).any()

@@ -29,6 +29,7 @@ KEYS = _parity.reference_fixtures()
 
 def test_reference_fixtures_present():
     assert len(KEYS) >= 8, KEYS
+    assert len(_parity.reference_fixtures("fvop")) >= 2
 
 
 @pytest.fixture(scope="module")
@@ -81,3 +82,44 @@ def test_oracle_gradient_matches_reference_directional_derivatives(cases, key):
     d = fx["dirs"].astype(np.float64) @ g64
     gn = float(np.linalg.norm(g64))
     np.testing.assert_allclose(d, fx["dloss64"], rtol=0, atol=1e-4 * gn)
+
+
+FV_KEYS = _parity.reference_fixtures("fvop")
+
+
+def _quadratic_lookup(phi_case, u):
+    """Network values replaced by the reference's non-oscillatory quadratic interpolant of the
+    nodal vector u (interpolate.py:572-759), as compute_Ax_and_b_discrete_fn reads u."""
+    g = phi_case.grid
+    T = _parity.O.Trilinear(u, g.x, g.y, g.z)
+
+    def values(net, x, phi_x):
+        q = x.detach().reshape(-1, 3).numpy().astype(np.float32)
+        return torch.as_tensor(T.quadratic(q)).to(x.dtype).reshape(x.shape[:-1])
+
+    return values
+
+
+@pytest.mark.parametrize("key", FV_KEYS)
+def test_oracle_discrete_operator_matches_reference(key):
+    """The reference's own residual_vector (trainer.py:883-890) of a random nodal vector and of
+    the exact solution against the oracle's residual with u read through the quadratic
+    interpolant, on every fixture row (the first-cell rows included)."""
+    from golden import make_reference_golden as M
+
+    fx = _parity.load_reference_fixture(key)
+    prob = str(fx["problem"])
+    n = int(fx["n"])
+    case = _parity.Case(prob, n, (1, 1, 2, 10), 0, fns=M.problem(prob), phi=fx["phi"], ids=fx["rows"])
+    rg = case.oracle_geometry()
+    L = _parity.L
+    orig = L.nn_eval
+    try:
+        for ukey, rkey in (("u_rand", "res_rand"), ("u_exact", "res_exact")):
+            L.nn_eval = _quadratic_lookup(case, fx[ukey])
+            got = L.residual(torch.zeros(L.n_params(case.arch)), case.arch, rg, torch.float32).numpy()
+            ref = fx[rkey]
+            scale = float(np.max(np.abs(ref)))
+            assert float(np.max(np.abs(got - ref))) <= 3e-5 * scale, (ukey, float(np.max(np.abs(got - ref))), scale)
+    finally:
+        L.nn_eval = orig
