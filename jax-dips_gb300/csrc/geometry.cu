@@ -382,68 +382,145 @@ __device__ void face_coefficients(const Cell& cell, const float p[3], const floa
 // ----------------------------------------------------------------------------------------
 // least-squares regression at a crossed stencil point (discretization.py:199-296)
 // ----------------------------------------------------------------------------------------
-// Eigen-decomposition of a symmetric 3x3 matrix by cyclic Jacobi rotations (double).
-__device__ void jacobi_eig3(double a[3][3], double v[3][3]) {
+// Eigen-decomposition of a symmetric 3x3 matrix by cyclic Jacobi rotations (float32; only for
+// cells whose stencil spacing differs between axes, see lsq_operator).
+__device__ void jacobi_eig3f(float a[3][3], float v[3][3]) {
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) v[i][j] = (i == j) ? 1.0 : 0.0;
-  for (int sweep = 0; sweep < 12; ++sweep) {
-    double off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
-    double scale = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]);
-    if (off == 0.0 || off <= 1e-16 * scale) break;
+    for (int j = 0; j < 3; ++j) v[i][j] = (i == j) ? 1.0f : 0.0f;
+  for (int sweep = 0; sweep < 10; ++sweep) {
+    const float off = fabsf(a[0][1]) + fabsf(a[0][2]) + fabsf(a[1][2]);
+    const float scale = fabsf(a[0][0]) + fabsf(a[1][1]) + fabsf(a[2][2]);
+    if (off == 0.0f || off <= 1e-9f * scale) break;
     for (int p = 0; p < 2; ++p)
       for (int q = p + 1; q < 3; ++q) {
-        double apq = a[p][q];
-        if (apq == 0.0) continue;
-        double theta = (a[q][q] - a[p][p]) / (2.0 * apq);
-        double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        const float apq = a[p][q];
+        if (apq == 0.0f) continue;
+        const float theta = (a[q][q] - a[p][p]) / (2.0f * apq);
+        const float t = (theta >= 0.0f ? 1.0f : -1.0f) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+        const float c = 1.0f / sqrtf(t * t + 1.0f), sn = t * c;
         for (int k = 0; k < 3; ++k) {
-          double akp = a[k][p], akq = a[k][q];
-          a[k][p] = c * akp - s * akq;
-          a[k][q] = s * akp + c * akq;
+          const float akp = a[k][p], akq = a[k][q];
+          a[k][p] = c * akp - sn * akq;
+          a[k][q] = sn * akp + c * akq;
         }
         for (int k = 0; k < 3; ++k) {
-          double apk = a[p][k], aqk = a[q][k];
-          a[p][k] = c * apk - s * aqk;
-          a[q][k] = s * apk + c * aqk;
+          const float apk = a[p][k], aqk = a[q][k];
+          a[p][k] = c * apk - sn * aqk;
+          a[q][k] = sn * apk + c * aqk;
         }
         for (int k = 0; k < 3; ++k) {
-          double vkp = v[k][p], vkq = v[k][q];
-          v[k][p] = c * vkp - s * vkq;
-          v[k][q] = s * vkp + c * vkq;
+          const float vkp = v[k][p], vkq = v[k][q];
+          v[k][p] = c * vkp - sn * vkq;
+          v[k][q] = sn * vkp + c * vkq;
         }
       }
   }
 }
 
-// D = pinv(X^T W X)(W X)^T (3 x 27), jax's pinv cutoff 10*3*eps_f32*sigma_max.
-__device__ void lsq_operator(const float X[27][3], const bool w[27], float D[3][27]) {
-  double M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+__device__ __forceinline__ int cube_o(int k, int a) { return (a == 0 ? k % 3 : (a == 1 ? (k / 3) % 3 : k / 9)) - 1; }
+
+// D = pinv(X^T W X)(W X)^T (3 x 27) under the reference's pinv rule: jnp.linalg.pinv drops the
+// singular values at or below 10 * 3 * eps_f32 * sigma_max (discretization.py:257-258).
+//
+// X's rows are the cube offsets o_k h (o_k in {-1, 0, 1}^3, x fastest; get_Xijk,
+// discretization.py:164-197), so X^T W X = S N S with S = diag(h) and N = sum_k w_k o_k o_k^T,
+// an integer matrix with diagonal entries <= 18.  Its rank follows exactly from integer
+// invariants: det N, s = the sum of its principal 2x2 minors and t = tr N (rank 3, 2 or 1 for the
+// first of them that is nonzero).  These are the ranks the cutoff keeps: for a positive
+// semidefinite integer N of rank 3, lambda_min >= det / lambda_max^2 >= 1 / lambda_max^2 and
+// lambda_max <= t <= 54, so lambda_min / lambda_max >= 1 / 54^3 = 6.4e-6 > 3.6e-6; for rank 2 the
+// smaller nonzero eigenvalue is >= s / lambda_max >= 1 / 54, a ratio >= 3.4e-4; and a zero
+// eigenvalue comes out of a float32 SVD at about eps * lambda_max, below the cutoff.
+//
+// With the same spacing on every axis (the reference's grids), pinv(X^T W X) = pinv(N) / h^2 and
+// pinv(N) is an integer matrix over an integer: adj(N) / det N (rank 3); by Cayley-Hamilton on
+// the range, ((t^2 - s) N - t N^2) / s^2 (rank 2); N / t^2 (rank 1).  D[i][k] = w_k (P o_k)_i /
+// (den h) is then one float32 division of exact integers followed by the division by h.  With
+// spacings that differ between axes, S N S is decomposed by float32 Jacobi rotations and its r
+// largest eigenpairs (r the exact rank) are inverted.  Float32 throughout.
+__device__ void lsq_operator(const float h[3], const bool w[27], float D[3][27]) {
+  int N[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   for (int k = 0; k < 27; ++k) {
     if (!w[k]) continue;
+    const int o[3] = {cube_o(k, 0), cube_o(k, 1), cube_o(k, 2)};
     for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) M[i][j] += (double)X[k][i] * (double)X[k][j];
+      for (int j = 0; j < 3; ++j) N[i][j] += o[i] * o[j];
   }
-  double V[3][3];
-  jacobi_eig3(M, V);
-  double lam[3] = {fabs(M[0][0]), fabs(M[1][1]), fabs(M[2][2])};
-  double lmax = fmax(lam[0], fmax(lam[1], lam[2]));
-  double cut = 10.0 * 3.0 * 1.1920928955078125e-07 * lmax;
-  double P[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  const int t = N[0][0] + N[1][1] + N[2][2];
+  const int m01 = N[0][0] * N[1][1] - N[0][1] * N[1][0];
+  const int m02 = N[0][0] * N[2][2] - N[0][2] * N[2][0];
+  const int m12 = N[1][1] * N[2][2] - N[1][2] * N[2][1];
+  const int sm = m01 + m02 + m12;
+  int adj[3][3];
+  adj[0][0] = m12;
+  adj[1][1] = m02;
+  adj[2][2] = m01;
+  adj[0][1] = adj[1][0] = N[0][2] * N[2][1] - N[0][1] * N[2][2];
+  adj[0][2] = adj[2][0] = N[0][1] * N[1][2] - N[0][2] * N[1][1];
+  adj[1][2] = adj[2][1] = N[0][2] * N[1][0] - N[0][0] * N[1][2];
+  const int det = N[0][0] * adj[0][0] + N[0][1] * adj[1][0] + N[0][2] * adj[2][0];
+  const int rank = det != 0 ? 3 : (sm != 0 ? 2 : (t != 0 ? 1 : 0));
+  if (rank == 0) {
+    for (int i = 0; i < 3; ++i)
+      for (int k = 0; k < 27; ++k) D[i][k] = 0.0f;
+    return;
+  }
+  if (h[0] == h[1] && h[1] == h[2]) {
+    int P[3][3];
+    int den;
+    if (rank == 3) {
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) P[i][j] = adj[i][j];
+      den = det;
+    } else if (rank == 2) {
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          const int n2 = N[i][0] * N[0][j] + N[i][1] * N[1][j] + N[i][2] * N[2][j];
+          P[i][j] = (t * t - sm) * N[i][j] - t * n2;
+        }
+      den = sm * sm;
+    } else {
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) P[i][j] = N[i][j];
+      den = t * t;
+    }
+    const float fden = (float)den;
+    for (int k = 0; k < 27; ++k) {
+      const int o[3] = {cube_o(k, 0), cube_o(k, 1), cube_o(k, 2)};
+      for (int i = 0; i < 3; ++i) {
+        const int num = w[k] ? P[i][0] * o[0] + P[i][1] * o[1] + P[i][2] * o[2] : 0;
+        D[i][k] = __fdiv_rn(__fdiv_rn((float)num, fden), h[0]);
+      }
+    }
+    return;
+  }
+  float A[3][3], V[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) A[i][j] = (float)N[i][j] * h[i] * h[j];
+  jacobi_eig3f(A, V);
+  // the `rank` largest eigenvalues
+  float lam[3] = {A[0][0], A[1][1], A[2][2]};
+  bool keep[3] = {false, false, false};
+  for (int r = 0; r < rank; ++r) {
+    int best = -1;
+    for (int e = 0; e < 3; ++e)
+      if (!keep[e] && (best < 0 || lam[e] > lam[best])) best = e;
+    keep[best] = true;
+  }
+  float P[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   for (int e = 0; e < 3; ++e) {
-    if (!(lam[e] > cut)) continue;
-    double inv = 1.0 / M[e][e];
+    if (!keep[e]) continue;
+    const float inv = 1.0f / lam[e];
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) P[i][j] += V[i][e] * V[j][e] * inv;
   }
-  for (int k = 0; k < 27; ++k) {
+  for (int k = 0; k < 27; ++k)
     for (int i = 0; i < 3; ++i) {
-      double s = 0.0;
+      float s = 0.0f;
       if (w[k])
-        for (int j = 0; j < 3; ++j) s += P[i][j] * (double)X[k][j];
-      D[i][k] = (float)s;
+        for (int j = 0; j < 3; ++j) s += P[i][j] * ((float)cube_o(k, j) * h[j]);
+      D[i][k] = s;
     }
-  }
 }
 
 struct StencilRegression {
@@ -794,10 +871,8 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
       stencil_point(p, h, j, s);
       StencilRegression R;
       regression_geometry(L, s, h, R);
-      float X[27][3];
       bool wpos[27], wneg[27];
       for (int k = 0; k < 27; ++k) {
-        for (int a = 0; a < 3; ++a) X[k][a] = cube_offset(k, a, h);
         wpos[k] = R.phi_v[k] > 0.0f;
         wneg[k] = R.phi_v[k] < 0.0f;
       }
@@ -814,7 +889,7 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
       // regression on the phase whose normal derivative enters the extrapolation:
       // mu- > mu+ uses Omega^- (C^-), otherwise Omega^+ (C^+)
       float D[3][27];
-      lsq_operator(X, mbig ? wneg : wpos, D);
+      lsq_operator(h, mbig ? wneg : wpos, D);
       float C[27];
       for (int k = 0; k < 27; ++k)
         C[k] = __fadd_rn(__fadd_rn(__fmul_rn(R.n[0], D[0][k]), __fmul_rn(R.n[1], D[1][k])), __fmul_rn(R.n[2], D[2][k]));
