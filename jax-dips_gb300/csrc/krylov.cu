@@ -8,9 +8,18 @@
 // as the NBM path with each job's network value replaced by u at the job's grid node:
 //     r_p(u) = nan_to_num((lhs0_p + sum_j A_j u[node_j]) / diag_p) - rod_p
 // which is affine in u: r(u) = K u - b.  BiCGSTAB solves K u = b with float32 vectors and
-// FP64 inner products; the scalar recurrences stay on the device.
+// FP64 inner products; the scalar recurrences stay on the device, and the iterations between
+// two host checks run in one cooperative launch (k_bicg_coop).
+//
+// At a node of the lowest layer of an axis the reference's operator does not read the nodal
+// value: its quadratic interpolant (interpolate.py:572-759) clamps the first cell and
+// extrapolates 2 u_1 - u_2 + min|second difference|, which is not linear in u.  Here every
+// job reads its node's value, so K is linear (as BiCGSTAB needs) and equals the reference's
+// operator on every row whose stencil and regression cube stay off those layers.
 
 #include <math.h>
+
+#include <cooperative_groups.h>
 
 #include "dips_common.cuh"
 
@@ -174,11 +183,13 @@ struct KState {
 
 struct KVecs {
   float *x, *r, *rhat, *p, *v, *s, *t;
-  double* part;     // [(kKGrid + kGenGrid) * 3]: bulk-row blocks, then general-row blocks
+  double* part;     // [(kKGrid + kGenGrid) * 3]: per-block partial inner products
   int32_t* glist;   // [n] the general rows (found once per solve)
   int32_t* gcount;  // their number
   KState* st;
   float* err_part;  // [kKGrid] max |x - u_exact|
+  float4* coef;     // [n][2] bulk rows: A_0..A_6 (stencil order) and diag, packed once per solve
+  uint8_t* gen;     // [n] 1 for a general row (warp path), 0 for a bulk row
 };
 
 
@@ -283,9 +294,48 @@ __global__ void k_bicg_init_scalars(KVecs V, int nblk) {
   }
 }
 
-// reduce the first `nv` partial columns into the given state slots
-__device__ void reduce_partials(const double* part, int nblk, int nv, double* out0, double* out1, double* out2) {
+// ---- persistent BiCGSTAB ------------------------------------------------------------------------
+// The whole iteration runs in one cooperative launch (check_every iterations per launch): its
+// phases are separated by grid-wide barriers (all blocks co-resident by the cooperative launch),
+// and every block reduces the per-block inner-product partials itself, in one fixed order, so
+// all blocks hold the same recurrence scalars without another barrier and the result does not
+// depend on timing.  Per iteration: 2 matrix-free products and 5 barriers, no host work.
+
+// packs each bulk row's 7 stencil coefficients and diag (32 bytes, from its packed record) and
+// flags the general rows, once per solve
+__global__ void k_krylov_pack(dips_records_t rec, float4* __restrict__ coef, uint8_t* __restrict__ gen) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rec.n_pts; i += (int64_t)gridDim.x * blockDim.x) {
+    const bool b = bulk_row(rec, i);
+    gen[i] = b ? 0 : 1;
+    if (b) {
+      const float4* r4 = reinterpret_cast<const float4*>(rec.bulk_rec + i * 16);
+      coef[2 * i] = r4[1];
+      coef[2 * i + 1] = r4[2];
+    }
+  }
+}
+
+// (K x)_i of a bulk row from its packed coefficients (the same operations as bulk_apply)
+__device__ __forceinline__ float coef_apply(const float4* __restrict__ coef, const Grid3& g, int64_t p,
+                                            const float* __restrict__ x) {
+  const float4 a = __ldg(coef + 2 * p), b = __ldg(coef + 2 * p + 1);
+  const int64_t sj = g.nz, si = (int64_t)g.ny * g.nz;
+  float acc = a.x * __ldg(x + p);
+  acc = fmaf(a.y, __ldg(x + p - si), acc);
+  acc = fmaf(a.z, __ldg(x + p + si), acc);
+  acc = fmaf(a.w, __ldg(x + p - sj), acc);
+  acc = fmaf(b.x, __ldg(x + p + sj), acc);
+  acc = fmaf(b.y, __ldg(x + p - 1), acc);
+  acc = fmaf(b.z, __ldg(x + p + 1), acc);
+  const float v = acc / b.w;
+  return isfinite(v) ? v : 0.0f;
+}
+
+// sum of the first `nv` columns of the grid's partials, in one fixed order; every thread of the
+// block gets the sums
+__device__ __forceinline__ void reduce_all(const double* part, int nblk, int nv, double out[3]) {
   __shared__ double s[3][32];
+  __shared__ double res[3];
   double a = 0, b = 0, c = 0;
   for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
     a += part[3 * i];
@@ -309,75 +359,107 @@ __device__ void reduce_partials(const double* part, int nblk, int nv, double* ou
       x1 += s[1][q];
       x2 += s[2][q];
     }
-    *out0 = x0;
-    if (nv > 1) *out1 = x1;
-    if (nv > 2) *out2 = x2;
+    res[0] = x0;
+    res[1] = x1;
+    res[2] = x2;
   }
+  __syncthreads();
+  out[0] = res[0];
+  out[1] = res[1];
+  out[2] = res[2];
+  __syncthreads();
 }
 
-// beta = (rho_new/rho)(alpha/omega); rho = rho_new;  p = r + beta (p - omega v)
-__global__ void k_bicg_p(int64_t n, KVecs V) {
-  const KState S = *V.st;
-  const double beta = (S.rho_new / S.rho) * (S.alpha / S.omega);
-  const float fb = (float)beta, fw = (float)S.omega;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    V.p[i] = V.r[i] + fb * (V.p[i] - fw * V.v[i]);
+// one product over all rows (bulk rows a thread each, listed general rows a warp each), with the
+// row's follow-up of MODE; per-block partials into part
+template <int MODE>
+__device__ __forceinline__ void coop_apply(const dips_records_t& rec, const Grid3& g, const float* __restrict__ x,
+                                           const KVecs& V, int64_t n, int64_t gcnt, double* part) {
+  double a0 = 0.0, a1 = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+    if (!V.gen[i]) row_done<MODE>(rec, V, i, coef_apply(V.coef, g, i, x), a0, a1);
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = stride >> 5;
+  for (int64_t k = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; k < gcnt; k += warps) {
+    const int64_t gp = V.glist[k];
+    const float kx = general_apply_warp(rec, g, gp, x);
+    if (lane == 0) row_done<MODE>(rec, V, gp, kx, a0, a1);
+  }
+  block_partials(a0, a1, 0.0, part, 2);
 }
 
-__global__ void k_bicg_rho_shift(KVecs V) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    KState& S = *V.st;
+// `iters` BiCGSTAB iterations (it0 = the global number of the first); the recurrence state is
+// read from and written back to V.st (block 0)
+__global__ void __launch_bounds__(kKThreads, 4) k_bicg_coop(dips_records_t rec, Grid3 g, KVecs V, int64_t n, int it0,
+                                                         int iters) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  const int nblk = gridDim.x;
+  const int64_t gcnt = *V.gcount;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  // two partial buffers: the x/r update writes its partials right after the blocks read the
+  // t-product's, with no barrier in between, so the two use different buffers
+  double* partA = V.part;                // products (v, then t)
+  double* partB = V.part + 3 * kKGrid;   // the x/r update
+  KState S = *V.st;
+  double red[3];
+  for (int q = 0; q < iters && !S.breakdown; ++q) {
+    // beta = (rho_new / rho)(alpha / omega); rho <- rho_new; p = r (first) or r + beta (p - omega v)
+    const bool first = it0 + q == 1;
     S.beta = (S.rho_new / S.rho) * (S.alpha / S.omega);
     S.rho = S.rho_new;
-    if (!isfinite(S.beta) || S.rho == 0.0) S.breakdown = 1;
-  }
-}
-
-
-__global__ void k_bicg_alpha(KVecs V, int nblk) {
-  reduce_partials(V.part, nblk, 1, &V.st->rhat_v, nullptr, nullptr);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    KState& S = *V.st;
+    if (!isfinite(S.beta) || S.rho == 0.0) {  // every block takes the same decision
+      S.breakdown = 1;
+      break;
+    }
+    const float fb = (float)S.beta, fw = (float)S.omega;
+    for (int64_t i = i0; i < n; i += stride) V.p[i] = first ? V.r[i] : V.r[i] + fb * (V.p[i] - fw * V.v[i]);
+    grid.sync();
+    // v = K p; alpha = rho / (rhat, v); s = r - alpha v
+    coop_apply<kApplyV>(rec, g, V.p, V, n, gcnt, partA);
+    grid.sync();
+    reduce_all(partA, nblk, 1, red);
+    S.rhat_v = red[0];
     S.alpha = S.rho / S.rhat_v;
-    if (!isfinite(S.alpha)) S.breakdown = 1;
-  }
-}
-
-// s = r - alpha v
-__global__ void k_bicg_s(int64_t n, KVecs V) {
-  const float a = (float)V.st->alpha;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    V.s[i] = V.r[i] - a * V.v[i];
-}
-
-
-__global__ void k_bicg_omega(KVecs V, int nblk) {
-  reduce_partials(V.part, nblk, 2, &V.st->ts, &V.st->tt, nullptr);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    KState& S = *V.st;
+    if (!isfinite(S.alpha)) {
+      S.breakdown = 1;
+      break;
+    }
+    const float fa = (float)S.alpha;
+    for (int64_t i = i0; i < n; i += stride) V.s[i] = V.r[i] - fa * V.v[i];
+    grid.sync();
+    // t = K s; omega = (t, s) / (t, t)
+    coop_apply<kApplyT>(rec, g, V.s, V, n, gcnt, partA);
+    grid.sync();
+    reduce_all(partA, nblk, 2, red);
+    S.ts = red[0];
+    S.tt = red[1];
     S.omega = S.tt > 0.0 ? S.ts / S.tt : 0.0;
-    if (S.omega == 0.0) S.breakdown = 1;
+    if (S.omega == 0.0) {
+      S.breakdown = 1;
+      break;
+    }
+    // x += alpha p + omega s; r = s - omega t; (rhat, r), (r, r)
+    const float w = (float)S.omega;
+    double rr = 0.0, rh = 0.0;
+    for (int64_t i = i0; i < n; i += stride) {
+      const float sv = V.s[i];
+      V.x[i] = V.x[i] + fa * V.p[i] + w * sv;
+      const float r = sv - w * V.t[i];
+      V.r[i] = r;
+      rh += (double)V.rhat[i] * r;
+      rr += (double)r * r;
+    }
+    block_partials(rh, rr, 0.0, partB, 2);
+    grid.sync();
+    reduce_all(partB, nblk, 2, red);
+    S.rho_new = red[0];
+    S.rr = red[1];
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *V.st = S;
 }
-
-// x += alpha p + omega s;  r = s - omega t;  partials (rhat, r), (r, r)
-__global__ void k_bicg_xr(int64_t n, KVecs V) {
-  const float a = (float)V.st->alpha, w = (float)V.st->omega;
-  double rr = 0.0, rh = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float s = V.s[i];
-    V.x[i] = V.x[i] + a * V.p[i] + w * s;
-    const float r = s - w * V.t[i];
-    V.r[i] = r;
-    rh += (double)V.rhat[i] * r;
-    rr += (double)r * r;
-  }
-  block_partials(rh, rr, 0.0, V.part, 2);
-}
-
-__global__ void k_bicg_rho(KVecs V, int nblk) { reduce_partials(V.part, nblk, 2, &V.st->rho_new, &V.st->rr, nullptr); }
 
 // max |x - u_exact| / max |u_exact| partials
 __global__ void k_err(int64_t n, const float* __restrict__ x, const float* __restrict__ ex, float* __restrict__ part) {
@@ -430,9 +512,34 @@ static size_t kcarve(KVecs* V, char* base, int64_t n) {
   v.gcount = (int32_t*)take(sizeof(int32_t));
   v.st = (KState*)take(sizeof(KState));
   v.err_part = (float*)take(sizeof(float) * 2 * kKGrid);
+  v.coef = (float4*)take(sizeof(float4) * 2 * n);
+  v.gen = (uint8_t*)take(n);
   v.x = nullptr;
   if (V) *V = v;
   return off;
+}
+
+// blocks of the cooperative BiCGSTAB launch on the current device (all co-resident), cached
+static int coop_grid_size(int* out) {
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "bicgstab: cudaGetDevice");
+  if (dev >= 0 && dev < 64 && cached[dev]) {
+    *out = cached[dev];
+    return DIPS_OK;
+  }
+  int coop = 0, sms = 0, per_sm = 0;
+  e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bicg_coop, kKThreads, 0);
+  if (e != cudaSuccess) return cuda_status(e, "bicgstab: cooperative launch attributes");
+  DIPS_REQUIRE(coop && per_sm > 0, DIPS_E_CUDA, "bicgstab: the device does not support the cooperative launch");
+  int grid = sms * per_sm;
+  if (grid > kKGrid) grid = kKGrid;
+  if (dev >= 0 && dev < 64) cached[dev] = grid;
+  *out = grid;
+  return DIPS_OK;
 }
 
 static int check_grid(const dips_records_t* rec, int nx, int ny, int nz) {
@@ -482,6 +589,12 @@ extern "C" int dips_bicgstab(const dips_records_t* rec, int32_t nx, int32_t ny, 
   cudaError_t ez = cudaMemsetAsync(V.gcount, 0, sizeof(int32_t), stream);
   if (ez != cudaSuccess) return cuda_status(ez, "bicgstab general-row count");
   k_general_rows<<<G, T, 0, stream>>>(*rec, V.glist, V.gcount);
+  if (rec->bulk_rec) {
+    k_krylov_pack<<<G, T, 0, stream>>>(*rec, V.coef, V.gen);
+  } else {  // no packed records: every row takes the warp path
+    cudaError_t eg = cudaMemsetAsync(V.gen, 1, n, stream);
+    if (eg != cudaSuccess) return cuda_status(eg, "bicgstab row kinds");
+  }
   k_apply_bulk<kInit><<<G, T, 0, stream>>>(*rec, g, V.x, V);
   k_apply_general<kInit><<<kGenGrid, T, 0, stream>>>(*rec, g, V.x, V);
   k_bicg_init_scalars<<<1, 1024, 0, stream>>>(V, GP);
@@ -521,28 +634,22 @@ extern "C" int dips_bicgstab(const dips_records_t* rec, int32_t nx, int32_t ny, 
   }
   // with an exact solution and a positive target the solve stops once the target is met
   const bool stop_at_target = u_exact != nullptr && target_rel_linf > 0.0f;
-  for (int it = 1; it <= max_iter && S.rel_residual > rtol && !(stop_at_target && S.target_iteration >= 0); ++it) {
-    if (it > 1) {
-      k_bicg_p<<<G, T, 0, stream>>>(n, V);
-      k_bicg_rho_shift<<<1, 32, 0, stream>>>(V);
-    } else {
-      // first iteration: p = r
-      k_bicg_rho_shift<<<1, 32, 0, stream>>>(V);
-      cudaError_t e = cudaMemcpyAsync(V.p, V.r, sizeof(float) * n, cudaMemcpyDeviceToDevice, stream);
-      if (e != cudaSuccess) return cuda_status(e, "bicgstab p = r");
-    }
-    k_apply_bulk<kApplyV><<<G, T, 0, stream>>>(*rec, g, V.p, V);
-    k_apply_general<kApplyV><<<kGenGrid, T, 0, stream>>>(*rec, g, V.p, V);
-    k_bicg_alpha<<<1, 1024, 0, stream>>>(V, GP);
-    k_bicg_s<<<G, T, 0, stream>>>(n, V);
-    k_apply_bulk<kApplyT><<<G, T, 0, stream>>>(*rec, g, V.s, V);
-    k_apply_general<kApplyT><<<kGenGrid, T, 0, stream>>>(*rec, g, V.s, V);
-    k_bicg_omega<<<1, 1024, 0, stream>>>(V, GP);
-    k_bicg_xr<<<G, T, 0, stream>>>(n, V);
-    k_bicg_rho<<<1, 1024, 0, stream>>>(V, G);
-    DIPS_CHECK_LAUNCH("bicgstab iteration");
-    S.iterations = it;
-    if (it % check_every == 0 || it == max_iter) {
+  // the iterations between two host checks run in one cooperative launch: as many blocks as
+  // fit on the device at once (so that the grid-wide barriers are legal), at most kKGrid
+  int coop_grid = 0;
+  if ((st = coop_grid_size(&coop_grid))) return st;
+  for (int it = 1; it <= max_iter && S.rel_residual > rtol && !(stop_at_target && S.target_iteration >= 0);) {
+    int chunk = check_every - (it - 1) % check_every;
+    if (chunk > max_iter - it + 1) chunk = max_iter - it + 1;
+    int64_t n_arg = n;
+    int it0 = it;
+    void* args[] = {(void*)rec, (void*)&g, (void*)&V, (void*)&n_arg, (void*)&it0, (void*)&chunk};
+    cudaError_t el = cudaLaunchCooperativeKernel((const void*)k_bicg_coop, dim3(coop_grid), dim3(kKThreads), args, 0,
+                                                 stream);
+    if (el != cudaSuccess) return cuda_status(el, "bicgstab cooperative launch");
+    it += chunk;
+    S.iterations = it - 1;
+    {
       if ((st = read_state())) return st;
       S.rel_residual = sqrt(hs.rr) / bnorm;
       if (hs.breakdown) {
@@ -551,7 +658,7 @@ extern "C" int dips_bicgstab(const dips_records_t* rec, int32_t nx, int32_t ny, 
       }
       if (u_exact && S.target_iteration < 0) {
         if ((st = read_err(&S.rel_linf))) return st;
-        if (S.rel_linf <= target_rel_linf) S.target_iteration = it;
+        if (S.rel_linf <= target_rel_linf) S.target_iteration = it - 1;
       }
     }
   }
