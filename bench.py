@@ -82,6 +82,10 @@ def parse():
     ap.add_argument("--arch", default="3x32", choices=["3x32", "4x64", "2x16"],
                     help="hidden layers x width of both networks (4x64 runs on the TF32 tensor cores)")
     ap.add_argument("--n-ls", type=int, default=0, help="level-set grid side (default: the training grid's)")
+    ap.add_argument("--krylov", action="store_true",
+                    help="the plain method alone: BiCGSTAB iterations on the --n^3 sphere's FV system, time per "
+                         "iteration against HBM (--steps iterations, host checks every --krylov-check)")
+    ap.add_argument("--krylov-check", type=int, default=10)
     return ap.parse_args()
 
 
@@ -722,6 +726,73 @@ TTA_SWEEP = tuple(("adam", b, lr) for b in (1 << 14, 1 << 15, 1 << 16, 1 << 17, 
                   for lr in (3e-3, 1e-2, 3e-2)) + (("lbfgs", None, None),)
 
 
+def run_krylov(args, rank, world):
+    """BiCGSTAB on the FV system of the --n^3 sphere: time per iteration (CUDA events around a
+    fixed number of iterations, host checks every --krylov-check) against HBM."""
+    import torch
+
+    from dips_gb300 import krylov, levelset, mesh, problems
+    from dips_gb300.records import FVLevel
+
+    dev = "cuda:0"
+    pr = getattr(problems, f"{args.problem}_problem")()
+    g = mesh.uniform_grid(args.n)
+    ls = levelset.LevelSetGrid.from_callable(g, lambda r: levelset.perturb(pr["phi"](r)), dev)
+    lvl = FVLevel(ls, pr, torch.as_tensor(g.R, device=dev), np.array([g.dx, g.dy, g.dz], np.float32))
+    shape = (args.n, args.n, args.n)
+    ex = torch.as_tensor(problems.exact_solution(pr, g.R), device=dev)
+    n = lvl.n
+    ws = torch.empty(int(__import__("dips_gb300")._lib.load().dips_bicgstab_workspace_bytes(n)), dtype=torch.uint8,
+                     device=dev)
+    for _ in range(max(args.warmup, 1)):
+        krylov.bicgstab(lvl, shape, max_iter=20, rtol=0.0, check_every=args.krylov_check, workspace=ws)
+    torch.cuda.synchronize()
+    iters = max(args.steps, args.krylov_check)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(0)
+    e0.record()
+    res = krylov.bicgstab(lvl, shape, max_iter=iters, rtol=0.0, check_every=args.krylov_check, workspace=ws)
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    t = e0.elapsed_time(e1) / 1e3
+    it = max(res.iterations, 1)
+    # to target, as in time_to_target: floor, then the timed solve
+    floor = krylov.bicgstab(lvl, shape, u_exact=ex, max_iter=3000, rtol=1e-6, check_every=25).rel_linf
+    target = max(1e-2, 1.1 * floor)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    kr = krylov.bicgstab(lvl, shape, u_exact=ex, max_iter=3000, rtol=1e-9, check_every=5, target_rel_linf=target)
+    torch.cuda.synchronize()
+    t_kr = time.perf_counter() - t0
+    # streaming model of one iteration (bytes per row): two products (packed coefficients 32 B,
+    # row kind 1 B, own x 4 B, product written 4 B, rhat or s read 4 B), s = r - alpha v (12 B),
+    # the x/r update with its dots (28 B), the p update (16 B); general rows add their job data
+    gen = int((lvl.cnt != 7).sum()) + int(((lvl.cnt == 7) & (lvl.cnt_m != 0) & (lvl.cnt_m != 7)).sum())
+    gen_jobs = int(lvl.n_jobs) - 7 * (n - gen)
+    bytes_it = 142 * n + 2 * 10 * gen_jobs
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = bytes_it / (t / it) / 1e9
+    line = {"metric": "BiCGSTAB iteration on the FV system (plain method)", "value": 1e3 * t / it, "unit": "ms/iteration",
+            "n_gpus": 1, "steps": it, "warmup": args.warmup, "higher_is_better": False, "dtype": "f32 (f64 dots)",
+            "data": "synthetic", "config": {"workload": f"{args.problem} {args.n}^3, rows {n}, general rows {gen}",
+                                            "check_every": args.krylov_check},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "algorithmic": f"{bytes_it / n:.1f} B per row per iteration (streaming model: 142 B per "
+                                        "row + 10 B per general-row job and product)",
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"},
+            "to_target": {"target_rel_linf": target, "floor_rel_linf": floor, "s": t_kr, "iterations": kr.iterations,
+                          "reached": kr.target_iteration >= 0},
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def time_to_target(args, lvl, g, pr, arch, dev):
     import torch
 
@@ -814,6 +885,8 @@ def main():
         run_reference(args, rank, world)
     elif args.c1:
         run_c1(args, rank, world)
+    elif args.krylov:
+        run_krylov(args, rank, world)
     elif args.problem == "lpbe":
         run_instances(args, rank, world)
     else:
