@@ -33,11 +33,10 @@ struct Grid3 {
   int nx, ny, nz;
 };
 
-// grid node of job code c of row p (stencil offset + cube offset, clamped to the grid)
-__device__ __forceinline__ int64_t job_node(int64_t p, uint16_t c, const Grid3& g) {
-  int k = (int)(p % g.nz);
-  int j = (int)((p / g.nz) % g.ny);
-  int i = (int)(p / ((int64_t)g.ny * g.nz));
+// grid node of job code c of the row at (i, j, k): stencil offset + cube offset, clamped to the
+// grid (the row's coordinates are computed once per row, so a job costs no integer division
+// beyond the constant ones that decode its code)
+__device__ __forceinline__ int64_t job_node(int i, int j, int k, uint16_t c, const Grid3& g) {
   const int st = job_stencil(c), v = job_vertex(c);
   if (st > 0) {
     const int a = (st - 1) >> 1, d = ((st - 1) & 1) ? 1 : -1;
@@ -85,10 +84,13 @@ __device__ __forceinline__ float general_apply_warp(const dips_records_t& rec, c
   const int lane = threadIdx.x & 31;
   const int64_t o0 = rec.job_off[gp], o1 = rec.job_off[gp + 1];
   const int cm = rec.cnt_m[gp], n = rec.cnt[gp];
+  const int k = (int)(gp % g.nz);
+  const int j = (int)((gp / g.nz) % g.ny);
+  const int i = (int)(gp / ((int64_t)g.ny * g.nz));
   float part = 0.0f;
   for (int q = lane; q < n; q += 32) {
     const int64_t o = q < cm ? o0 + q : o1 - n + q;  // u- jobs at the front, u+ jobs at the back
-    part = fmaf(rec.job_A[o], __ldg(x + job_node(gp, rec.job_code[o], g)), part);
+    part = fmaf(rec.job_A[o], __ldg(x + job_node(i, j, k, rec.job_code[o], g)), part);
   }
 #pragma unroll
   for (int s = 16; s > 0; s >>= 1) part += __shfl_xor_sync(0xffffffffu, part, s);

@@ -43,9 +43,13 @@ constexpr int kParams = 2 * kNetParams;
 constexpr int kOut = 4 * W + (L - 1) * (W * W + W);  // offset of the output weights in a network
 __host__ __device__ constexpr int layer_off(int l) { return l == 0 ? 0 : 4 * W + (l - 1) * (W * W + W); }
 
-constexpr int kThreads = 256;  // two threads per job: features [0, 32) and [32, 64)
+constexpr int kThreads = 256;  // forward kernel: two threads per job, features [0, 32) and [32, 64)
 constexpr int kTile = 128;
 constexpr int kHalf = 32;
+// adjoint kernel: four threads per job (warps w, w + 4, w + 8, w + 12), 16 features each, so that
+// 16 warps share the SM and hide each other's tcgen05.ld, mbarrier and MUFU latencies
+constexpr int kAdjThreads = 512;
+constexpr int kAQ = 16;
 constexpr int kGrid = kTileGrid;
 // polls of an mbarrier wait before the CTA gives up (kernel argument; dips_tc_set_wait_limit
 // changes it for tests of the timeout path); the wait for MMAs still in flight after a give-up
@@ -196,10 +200,11 @@ __device__ __forceinline__ void drain_after_abort(uint64_t* bar, uint32_t phase,
   __syncthreads();
 }
 
-// h1 = tanh(W1^T x + b1) for features [f0, f0 + 32), on the FP32 pipe
+// h1 = tanh(W1^T x + b1) for features [f0, f0 + NQ), on the FP32 pipe
+template <int NQ = kHalf>
 __device__ __forceinline__ void layer1(const float* small, const float x[3], float* h, int f0) {
 #pragma unroll
-  for (int o = 0; o < kHalf; ++o) {
+  for (int o = 0; o < NQ; ++o) {
     float z = small[3 * W + f0 + o];
     z = fmaf(x[0], small[f0 + o], z);
     z = fmaf(x[1], small[W + f0 + o], z);
@@ -208,24 +213,27 @@ __device__ __forceinline__ void layer1(const float* small, const float x[3], flo
   }
 }
 
-// this thread's 32 values into its TMEM lane, columns [col, col + 32), rounded to TF32
+// this thread's NQ values into its TMEM lane, columns [col, col + NQ), rounded to TF32
+template <int NQ = kHalf>
 __device__ __forceinline__ void to_tmem(uint32_t lane_base, uint32_t col, const float* v) {
 #pragma unroll
-  for (int c = 0; c < kHalf; c += 16) {
+  for (int c = 0; c < NQ; c += 16) {
     float t[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) t[q] = tf32(v[c + q]);
     tst16(lane_base + col + c, t);
   }
 }
+template <int NQ = kHalf>
 __device__ __forceinline__ void from_tmem(uint32_t lane_base, uint32_t col, float* v) {
 #pragma unroll
-  for (int c = 0; c < kHalf; c += 16) tld16(lane_base + col + c, v + c);
+  for (int c = 0; c < NQ; c += 16) tld16(lane_base + col + c, v + c);
 }
-// rows [f0, f0 + 32) of column t (this thread's job) of a feature-major matrix
+// rows [f0, f0 + NQ) of column t (this thread's job) of a feature-major matrix
+template <int NQ = kHalf>
 __device__ __forceinline__ void to_fm(unsigned char* m, int t, const float* v, int f0) {
 #pragma unroll
-  for (int r = 0; r < kHalf; ++r) *reinterpret_cast<float*>(m + foff(f0 + r, t)) = tf32(v[r]);
+  for (int r = 0; r < NQ; ++r) *reinterpret_cast<float*>(m + foff(f0 + r, t)) = tf32(v[r]);
 }
 __device__ __forceinline__ float fm_at(const unsigned char* m, int r, int t) {
   return *reinterpret_cast<const float*>(m + foff(r, t));
@@ -350,9 +358,10 @@ constexpr size_t kAdjSmem = kOffSmall + sizeof(float) * kSmallFloats + 64;
 // 128 with dL/du from the general residual.  BWD = false: bulk tiles only, forward, residual
 // and loss (the forward-only path); BWD = true: the backward of every tile as well.
 constexpr int kBulkPts = 18;
+static_assert(kBulkPts <= 32, "the bulk residuals of a tile are formed by warp 0");
 
 template <bool BWD>
-__global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restrict__ params, int off, Workspace w,
+__global__ void __launch_bounds__(kAdjThreads, 1) k_tc_adjoint(const float* __restrict__ params, int off, Workspace w,
                                                             int net_p, PtsH ph, float* __restrict__ residual_out,
                                                             uint32_t wait_limit) {
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -365,9 +374,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
   float* small = reinterpret_cast<float*>(sm + kOffSmall);
   uint64_t* bar = reinterpret_cast<uint64_t*>(small + kSmallFloats);
   uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
-  __shared__ int s_abort;
+  int& s_abort = *reinterpret_cast<int*>(slot + 1);  // in the dynamic block's slack (static shared memory is full)
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const int job = 32 * (warp & 3) + lane, f0 = kHalf * (warp >> 2);
+  const int job = 32 * (warp & 3) + lane, part = warp >> 2, f0 = kAQ * part;
   load_weights<true>(params + off, wf, wb, small);
   // constant rows: 64 = ones (the bias input) and 65..71 = 0 in the 72-row matrices; rows 1..7
   // of GX and rows 64..71 of the 72-row matrices are never rewritten
@@ -396,8 +405,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
   const float* recs = w.brec + (size_t)(net_p ? w.B : 0) * kRecFloats;
   const float hh[3] = {ph.h[0], ph.h[1], ph.h[2]};
   const float Bf = (float)w.B;
-  __shared__ float s_part[kTile], s_au[kTile], s_g[kTile];
-  __shared__ double s_loss[kThreads / 32];
+  __shared__ float s_part[2][kTile], s_au[kTile], s_g[kTile];
+  // the fourth quarter's partial output sums use s_g, which is written only after they are read
+  // (static + dynamic shared memory must stay within the 227 KB a CTA may have)
+  float* const s_part3 = s_g;
   double lsum = 0.0;
   uint32_t phase = 0;
   bool first = true;
@@ -452,9 +463,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
       }
     }
     // ---- forward, keeping h2^T and h3^T
-    float h[kHalf];
-    layer1(small, x, h, f0);
-    to_tmem(lb, cA + f0, h);
+    float h[kAQ];
+    layer1<kAQ>(small, x, h, f0);
+    to_tmem<kAQ>(lb, cA + f0, h);
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -462,11 +473,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
       commit(bar);
     }
     wait();
-    from_tmem(lb, cD + f0, h);
+    from_tmem<kAQ>(lb, cD + f0, h);
 #pragma unroll
-    for (int o = 0; o < kHalf; ++o) h[o] = tanh_f(h[o] + small[4 * W + f0 + o]);
-    to_tmem(lb, cA + f0, h);
-    to_fm(H2, job, h, f0);
+    for (int o = 0; o < kAQ; ++o) h[o] = tanh_f(h[o] + small[4 * W + f0 + o]);
+    to_tmem<kAQ>(lb, cA + f0, h);
+    to_fm<kAQ>(H2, job, h, f0);
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -474,11 +485,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
       commit(bar);
     }
     wait();
-    from_tmem(lb, cD + f0, h);
+    from_tmem<kAQ>(lb, cD + f0, h);
 #pragma unroll
-    for (int o = 0; o < kHalf; ++o) h[o] = tanh_f(h[o] + small[5 * W + f0 + o]);
-    to_tmem(lb, cA + f0, h);
-    to_fm(H3, job, h, f0);
+    for (int o = 0; o < kAQ; ++o) h[o] = tanh_f(h[o] + small[5 * W + f0 + o]);
+    to_tmem<kAQ>(lb, cA + f0, h);
+    to_fm<kAQ>(H3, job, h, f0);
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -486,17 +497,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
       commit(bar);
     }
     wait();
-    from_tmem(lb, cD + f0, h);
+    from_tmem<kAQ>(lb, cD + f0, h);
 #pragma unroll
-    for (int o = 0; o < kHalf; ++o) h[o] = tanh_f(h[o] + small[6 * W + f0 + o]);  // h4
+    for (int o = 0; o < kAQ; ++o) h[o] = tanh_f(h[o] + small[6 * W + f0 + o]);  // h4
     if (bulk) {
       // u of every job, A_j u_j, the residual of each of the tile's points, then dL/du
       float u = 0.0f;
 #pragma unroll
-      for (int o = 0; o < kHalf; ++o) u = fmaf(small[7 * W + f0 + o], h[o], u);
-      if (f0) s_part[job] = u;
+      for (int o = 0; o < kAQ; ++o) u = fmaf(small[7 * W + f0 + o], h[o], u);
+      if (part == 1) s_part[0][job] = u;
+      if (part == 2) s_part[1][job] = u;
+      if (part == 3) s_part3[job] = u;
       __syncthreads();
-      if (!f0) s_au[job] = A * (u + s_part[job] + small[8 * W]);
+      if (!part) s_au[job] = A * (((u + s_part[0][job]) + (s_part[1][job] + s_part3[job])) + small[8 * W]);
       __syncthreads();
       if (t < kBulkPts) {
         if (rvalid) {
@@ -522,7 +535,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     }
     if (!BWD) continue;
     // ---- output layer: dWo, dbo = sum_j g_j [h4, 1]  (A = [g] replicated, B = h4^T with its ones row)
-    to_fm(Z, job, h, f0);
+    to_fm<kAQ>(Z, job, h, f0);
     if (!f0) {
       *reinterpret_cast<float*>(GX + foff(0, job)) = tf32(g);
       *reinterpret_cast<float*>(GX + foff(1, job)) = 0.0f;
@@ -538,9 +551,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     wait();
     // delta4 = g wo (1 - h4^2)
 #pragma unroll
-    for (int o = 0; o < kHalf; ++o) h[o] = g * small[7 * W + f0 + o] * fmaf(-h[o], h[o], 1.0f);
-    to_tmem(lb, cA + f0, h);
-    to_fm(Z, job, h, f0);
+    for (int o = 0; o < kAQ; ++o) h[o] = g * small[7 * W + f0 + o] * fmaf(-h[o], h[o], 1.0f);
+    to_tmem<kAQ>(lb, cA + f0, h);
+    to_fm<kAQ>(Z, job, h, f0);
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -550,14 +563,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     }
     wait();
     // delta3 = (W4 delta4) (1 - h3^2)
-    from_tmem(lb, cD + f0, h);
+    from_tmem<kAQ>(lb, cD + f0, h);
 #pragma unroll
-    for (int o = 0; o < kHalf; ++o) {
+    for (int o = 0; o < kAQ; ++o) {
       const float a = fm_at(H3, f0 + o, job);
       h[o] *= fmaf(-a, a, 1.0f);
     }
-    to_tmem(lb, cA + f0, h);
-    to_fm(Z, job, h, f0);
+    to_tmem<kAQ>(lb, cA + f0, h);
+    to_fm<kAQ>(Z, job, h, f0);
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -567,17 +580,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     }
     wait();
     // delta2 = (W3 delta3) (1 - h2^2); h1 recomputed into H3
-    from_tmem(lb, cD + f0, h);
+    from_tmem<kAQ>(lb, cD + f0, h);
 #pragma unroll
-    for (int o = 0; o < kHalf; ++o) {
+    for (int o = 0; o < kAQ; ++o) {
       const float a = fm_at(H2, f0 + o, job);
       h[o] *= fmaf(-a, a, 1.0f);
     }
-    float h1[kHalf];
-    layer1(small, x, h1, f0);
-    to_fm(H3, job, h1, f0);
-    to_tmem(lb, cA + f0, h);
-    to_fm(Z, job, h, f0);
+    float h1[kAQ];
+    layer1<kAQ>(small, x, h1, f0);
+    to_fm<kAQ>(H3, job, h1, f0);
+    to_tmem<kAQ>(lb, cA + f0, h);
+    to_fm<kAQ>(Z, job, h, f0);
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -587,10 +600,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     }
     wait();
     // delta1 = (W2 delta2) (1 - h1^2); dW1^T | db1 = delta1^T [x, y, z, 1]
-    from_tmem(lb, cD + f0, h);
+    from_tmem<kAQ>(lb, cD + f0, h);
 #pragma unroll
-    for (int o = 0; o < kHalf; ++o) h[o] *= fmaf(-h1[o], h1[o], 1.0f);
-    to_fm(Z, job, h, f0);
+    for (int o = 0; o < kAQ; ++o) h[o] *= fmaf(-h1[o], h1[o], 1.0f);
+    to_fm<kAQ>(Z, job, h, f0);
     if (!f0) {
       *reinterpret_cast<float*>(GX + foff(0, job)) = tf32(x[0]);
       *reinterpret_cast<float*>(GX + foff(1, job)) = tf32(x[1]);
@@ -607,17 +620,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_adjoint(const float* __restr
     first = false;
   }
   drain_after_abort(bar, phase, s_abort);
-  // ---- loss partial of the bulk points of this CTA
+  // ---- loss partial of the bulk points of this CTA (only threads 0..17, in warp 0, hold any)
+  if (warp == 0) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
-  if (lane == 0) s_loss[warp] = lsum;
-  __syncthreads();
-  if (t == 0) {
-    double v = 0.0;
-    for (int k = 0; k < kThreads / 32; ++k) v += s_loss[k];
-    w.floss[net_p * kLossSlots + blockIdx.x] = v;
-    if (blockIdx.x == 0) w.ctl->floss_n[net_p] = gridDim.x;
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+    if (t == 0) {
+      w.floss[net_p * kLossSlots + blockIdx.x] = lsum;
+      if (blockIdx.x == 0) w.ctl->floss_n[net_p] = gridDim.x;
+    }
   }
+  __syncthreads();
   if (!BWD) {
     fence_before();
     __syncthreads();
@@ -762,9 +774,9 @@ static int adjoint_pair(const PtsH& ph, const Workspace& w, float* residual_out,
   int st = set_smem((const void*)k_tc_adjoint<BWD>, kAdjSmem, &attr);
   if (st) return st;
   const uint32_t lim = g_wait_limit.load();
-  k_tc_adjoint<BWD><<<kGrid, kThreads, kAdjSmem, s>>>(t_params, 0, w, 0, ph, residual_out, lim);
+  k_tc_adjoint<BWD><<<kGrid, kAdjThreads, kAdjSmem, s>>>(t_params, 0, w, 0, ph, residual_out, lim);
   mark(mk, kMarkFusedM, s);
-  k_tc_adjoint<BWD><<<kGrid, kThreads, kAdjSmem, s>>>(t_params, kNetParams, w, 1, ph, residual_out, lim);
+  k_tc_adjoint<BWD><<<kGrid, kAdjThreads, kAdjSmem, s>>>(t_params, kNetParams, w, 1, ph, residual_out, lim);
   mark(mk, kMarkFusedP, s);
   DIPS_CHECK_LAUNCH("tcgen05 bulk / adjoint");
   return DIPS_OK;
