@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=1 << 18)
     ap.add_argument("--tta-seconds", type=float, default=15.0,
                     help="NBM time budget of each configuration of the time-to-target run")
+    ap.add_argument("--tta-sweep-decay", action="store_true",
+                    help="time to target at batch 2^17 over learning rates 1e-2, 2e-2 and decay rates 0.9, 0.5, 0.25")
     ap.add_argument("--tta-sweep", action="store_true",
                     help="time to target over minibatch sizes 2^14..2^18 x learning rates 3e-3, 1e-2, 3e-2 and "
                          "L-BFGS, instead of the default three configurations")
@@ -631,7 +633,7 @@ def run_c1(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def _nbm_adam_run(lvl, arch, dev, B, lr, budget, target, rel_err):
+def _nbm_adam_run(lvl, arch, dev, B, lr, budget, target, rel_err, decay=0.9):
     """Chained-Adam NBM training (graph-captured steps, uniform minibatches of B points) until
     the relative L-inf error reaches the target or the training time reaches the budget.  The
     error checks run between replays and are not counted in the time."""
@@ -644,7 +646,7 @@ def _nbm_adam_run(lvl, arch, dev, B, lr, budget, target, rel_err):
     nb = lvl.n // B
     P = nn.n_params(arch)
     params = torch.as_tensor(nn.init_params(arch, 42), device=dev)
-    opt = ops.AdamState(P, lr=lr, decay_rate=0.9)
+    opt = ops.AdamState(P, lr=lr, decay_rate=decay)
     ws = ops.StepWorkspace(arch, B, lvl.max_jobs(B), dev)
     ids = torch.empty(B, dtype=torch.int32, device=dev)
     loss = torch.zeros((), dtype=torch.float64, device=dev)
@@ -680,7 +682,7 @@ def _nbm_adam_run(lvl, arch, dev, B, lr, budget, target, rel_err):
         if err <= target:
             reached = t_train
             break
-    return {"optimizer": "adam", "batch": B, "lr": lr, "reached": reached is not None, "s": reached,
+    return {"optimizer": "adam", "batch": B, "lr": lr, "decay_rate": decay, "reached": reached is not None, "s": reached,
             "steps": steps, "best_rel_linf": best, "train_s": t_train, "ms_per_step": 1e3 * t_train / max(steps, 1),
             "params": params}
 
@@ -721,9 +723,13 @@ def _nbm_lbfgs_run(lvl, arch, dev, budget, target, rel_err):
 # NBM configurations of the time-to-target run: chained Adam at the headline batch, the two
 # fastest configurations of a sweep over minibatch sizes 2^14..2^18 and learning rates
 # 3e-3/1e-2/3e-2 (--tta-sweep), and the reference's full-batch L-BFGS
-TTA_RUNS = (("adam", 1 << 18, 1e-2), ("adam", 1 << 17, 1e-2), ("adam", 1 << 15, 3e-3), ("lbfgs", None, None))
-TTA_SWEEP = tuple(("adam", b, lr) for b in (1 << 14, 1 << 15, 1 << 16, 1 << 17, 1 << 18)
-                  for lr in (3e-3, 1e-2, 3e-2)) + (("lbfgs", None, None),)
+TTA_RUNS = (("adam", 1 << 18, 1e-2, 0.9), ("adam", 1 << 17, 1e-2, 0.9), ("adam", 1 << 15, 3e-3, 0.9),
+            ("lbfgs", None, None, None))
+TTA_SWEEP = tuple(("adam", b, lr, 0.9) for b in (1 << 14, 1 << 15, 1 << 16, 1 << 17, 1 << 18)
+                  for lr in (3e-3, 1e-2, 3e-2)) + (("lbfgs", None, None, None),)
+# the exponential decay of the chained Adam's rate (optimizer_dict["sched"]["decay_rate"], per
+# 1000 steps) around the fastest configuration
+TTA_SWEEP_DECAY = tuple(("adam", 1 << 17, lr, d) for lr in (1e-2, 2e-2) for d in (0.9, 0.5, 0.25))
 
 
 def run_krylov(args, rank, world):
@@ -818,9 +824,10 @@ def time_to_target(args, lvl, g, pr, arch, dev):
         return float((u - ex).abs().max()) / exmax
 
     runs = []
-    for opt, B, lr in (TTA_SWEEP if args.tta_sweep else TTA_RUNS):
+    plan = TTA_SWEEP if args.tta_sweep else (TTA_SWEEP_DECAY if args.tta_sweep_decay else TTA_RUNS)
+    for opt, B, lr, decay in plan:
         if opt == "adam":
-            runs.append(_nbm_adam_run(lvl, arch, dev, B, lr, args.tta_seconds, target, rel_err))
+            runs.append(_nbm_adam_run(lvl, arch, dev, B, lr, args.tta_seconds, target, rel_err, decay))
         else:
             runs.append(_nbm_lbfgs_run(lvl, arch, dev, args.tta_seconds, target, rel_err))
     done = [r for r in runs if r["reached"]]
@@ -863,6 +870,7 @@ def time_to_target(args, lvl, g, pr, arch, dev):
             "krylov_reached": kr.target_iteration >= 0,
             "nbm_s": best["s"] if best["reached"] else None, "nbm_reached": best["reached"],
             "nbm_optimizer": best["optimizer"], "nbm_batch": best["batch"], "nbm_lr": best["lr"],
+            "nbm_decay_rate": best.get("decay_rate"),
             "nbm_steps": best["steps"], "nbm_best_rel_linf": best["best_rel_linf"],
             "nbm_budget_s": args.tta_seconds,
             "nbm_over_krylov": (best["s"] / t_kr) if best["reached"] else None,
