@@ -62,7 +62,8 @@ def parse():
     ap.add_argument("--tta-seconds", type=float, default=15.0,
                     help="NBM time budget of each configuration of the time-to-target run")
     ap.add_argument("--tta-sweep-decay", action="store_true",
-                    help="time to target at batch 2^17 over learning rates 1e-2, 2e-2 and decay rates 0.9, 0.5, 0.25")
+                    help="time to target at batches 2^16 and 2^17 over learning rates 1e-2, 2e-2, 3e-2 and decay "
+                         "rates 0.9, 0.7, 0.5, 0.25")
     ap.add_argument("--tta-sweep", action="store_true",
                     help="time to target over minibatch sizes 2^14..2^18 x learning rates 3e-3, 1e-2, 3e-2 and "
                          "L-BFGS, instead of the default three configurations")
@@ -720,16 +721,18 @@ def _nbm_lbfgs_run(lvl, arch, dev, budget, target, rel_err):
             "ms_per_step": 1e3 * train_s / max(state["iters"], 1), "params": params}
 
 
-# NBM configurations of the time-to-target run: chained Adam at the headline batch, the two
-# fastest configurations of a sweep over minibatch sizes 2^14..2^18 and learning rates
-# 3e-3/1e-2/3e-2 (--tta-sweep), and the reference's full-batch L-BFGS
-TTA_RUNS = (("adam", 1 << 18, 1e-2, 0.9), ("adam", 1 << 17, 1e-2, 0.9), ("adam", 1 << 15, 3e-3, 0.9),
-            ("lbfgs", None, None, None))
+# NBM configurations of the time-to-target run: chained Adam at the headline batch, the fastest
+# configurations of sweeps over minibatch sizes 2^14..2^18 x learning rates 3e-3/1e-2/3e-2
+# (--tta-sweep) and over learning rates x decay rates (--tta-sweep-decay), and the reference's
+# full-batch L-BFGS
+TTA_RUNS = (("adam", 1 << 18, 1e-2, 0.9), ("adam", 1 << 17, 1e-2, 0.9), ("adam", 1 << 17, 2e-2, 0.5),
+            ("adam", 1 << 15, 3e-3, 0.9), ("lbfgs", None, None, None))
 TTA_SWEEP = tuple(("adam", b, lr, 0.9) for b in (1 << 14, 1 << 15, 1 << 16, 1 << 17, 1 << 18)
                   for lr in (3e-3, 1e-2, 3e-2)) + (("lbfgs", None, None, None),)
 # the exponential decay of the chained Adam's rate (optimizer_dict["sched"]["decay_rate"], per
 # 1000 steps) around the fastest configuration
-TTA_SWEEP_DECAY = tuple(("adam", 1 << 17, lr, d) for lr in (1e-2, 2e-2) for d in (0.9, 0.5, 0.25))
+TTA_SWEEP_DECAY = tuple(("adam", b, lr, d) for b in (1 << 16, 1 << 17) for lr in (1e-2, 2e-2, 3e-2)
+                        for d in (0.9, 0.7, 0.5, 0.25))
 
 
 def run_krylov(args, rank, world):

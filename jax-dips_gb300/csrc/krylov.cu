@@ -98,6 +98,23 @@ __device__ __forceinline__ float general_apply_warp(const dips_records_t& rec, c
   return isfinite(v) ? v : 0.0f;
 }
 
+// (K x)_gp of any row by one thread, its jobs in order (u- jobs at the front, u+ at the back)
+__device__ __forceinline__ float general_apply_thread(const dips_records_t& rec, const Grid3& g, int64_t gp,
+                                                      const float* __restrict__ x) {
+  const int64_t o0 = rec.job_off[gp], o1 = rec.job_off[gp + 1];
+  const int cm = rec.cnt_m[gp], n = rec.cnt[gp];
+  const int k = (int)(gp % g.nz);
+  const int j = (int)((gp / g.nz) % g.ny);
+  const int i = (int)(gp / ((int64_t)g.ny * g.nz));
+  float acc = 0.0f;
+  for (int q = 0; q < n; ++q) {
+    const int64_t o = q < cm ? o0 + q : o1 - n + q;
+    acc = fmaf(rec.job_A[o], __ldg(x + job_node(i, j, k, rec.job_code[o], g)), acc);
+  }
+  const float v = acc / rec.diag[gp];
+  return isfinite(v) ? v : 0.0f;
+}
+
 // (K x)_p of the rows p of one warp (valid lanes): bulk rows inline, the others one at a time
 // by the whole warp.  All 32 lanes call it.
 __device__ __forceinline__ float warp_apply(const dips_records_t& rec, const Grid3& g, int64_t p, bool valid,
@@ -381,12 +398,11 @@ __device__ __forceinline__ void coop_apply(const dips_records_t& rec, const Grid
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
     if (!V.gen[i]) row_done<MODE>(rec, V, i, coef_apply(V.coef, g, i, x), a0, a1);
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = stride >> 5;
-  for (int64_t k = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; k < gcnt; k += warps) {
+  // general rows a thread each: about one row per thread at 128^3 (136,680 rows, 15 jobs on
+  // average), so their dependent loads overlap across the grid instead of queueing per warp
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < gcnt; k += stride) {
     const int64_t gp = V.glist[k];
-    const float kx = general_apply_warp(rec, g, gp, x);
-    if (lane == 0) row_done<MODE>(rec, V, gp, kx, a0, a1);
+    row_done<MODE>(rec, V, gp, general_apply_thread(rec, g, gp, x), a0, a1);
   }
   block_partials(a0, a1, 0.0, part, 2);
 }
