@@ -725,8 +725,8 @@ def _nbm_lbfgs_run(lvl, arch, dev, budget, target, rel_err):
 # configurations of sweeps over minibatch sizes 2^14..2^18 x learning rates 3e-3/1e-2/3e-2
 # (--tta-sweep) and over learning rates x decay rates (--tta-sweep-decay), and the reference's
 # full-batch L-BFGS
-TTA_RUNS = (("adam", 1 << 18, 1e-2, 0.9), ("adam", 1 << 17, 1e-2, 0.9), ("adam", 1 << 17, 2e-2, 0.5),
-            ("adam", 1 << 15, 3e-3, 0.9), ("lbfgs", None, None, None))
+TTA_RUNS = (("adam", 1 << 18, 1e-2, 0.9), ("adam", 1 << 17, 3e-2, 0.5), ("adam", 1 << 16, 3e-2, 0.7),
+            ("adam", 1 << 16, 2e-2, 0.7), ("lbfgs", None, None, None))
 TTA_SWEEP = tuple(("adam", b, lr, 0.9) for b in (1 << 14, 1 << 15, 1 << 16, 1 << 17, 1 << 18)
                   for lr in (3e-3, 1e-2, 3e-2)) + (("lbfgs", None, None, None),)
 # the exponential decay of the chained Adam's rate (optimizer_dict["sched"]["decay_rate"], per
