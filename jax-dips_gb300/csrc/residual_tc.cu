@@ -111,6 +111,7 @@ __device__ __forceinline__ bool wait_phase(uint64_t* bar, uint32_t phase, uint32
                  : "r"(saddr(bar)), "r"(phase));
   return done != 0;
 }
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
@@ -544,16 +545,20 @@ __global__ void __launch_bounds__(kAdjThreads, 1) k_tc_adjoint(const float* __re
     }
     sync_for_mma();
     if (s_abort) break;
+    // Work that does not depend on an MMA in flight runs while it runs (between the issue and
+    // the wait): the next delta where it needs no product, the factors read from H2/H3 (which
+    // the MMA may read at the same time), and the rewrite of a buffer that the MMAs completed
+    // at an earlier wait (GX after dWo, H3 after dW4).
     if (t == 0) {
       issue_dw(tb + cWO, GX, 0, Z, 72, !first);
       commit(bar);
     }
-    wait();
-    // delta4 = g wo (1 - h4^2)
+    // delta4 = g wo (1 - h4^2) into TMEM A (the dWo MMA reads only shared memory)
 #pragma unroll
     for (int o = 0; o < kAQ; ++o) h[o] = g * small[7 * W + f0 + o] * fmaf(-h[o], h[o], 1.0f);
     to_tmem<kAQ>(lb, cA + f0, h);
-    to_fm<kAQ>(Z, job, h, f0);
+    wait();
+    to_fm<kAQ>(Z, job, h, f0);  // Z held h4^T for dWo until the wait
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
@@ -561,14 +566,23 @@ __global__ void __launch_bounds__(kAdjThreads, 1) k_tc_adjoint(const float* __re
       issue_delta(tb, wb + 2 * kWBytes);             // W4 delta4
       commit(bar);
     }
+    float fac[kAQ];
+#pragma unroll
+    for (int o = 0; o < kAQ; ++o) {
+      const float a = fm_at(H3, f0 + o, job);
+      fac[o] = fmaf(-a, a, 1.0f);
+    }
+    if (!f0) {  // [x, y, z, 1] for dW1 (GX's last reader, dWo, completed at the previous wait)
+      *reinterpret_cast<float*>(GX + foff(0, job)) = tf32(x[0]);
+      *reinterpret_cast<float*>(GX + foff(1, job)) = tf32(x[1]);
+      *reinterpret_cast<float*>(GX + foff(2, job)) = tf32(x[2]);
+      *reinterpret_cast<float*>(GX + foff(3, job)) = 1.0f;
+    }
     wait();
     // delta3 = (W4 delta4) (1 - h3^2)
     from_tmem<kAQ>(lb, cD + f0, h);
 #pragma unroll
-    for (int o = 0; o < kAQ; ++o) {
-      const float a = fm_at(H3, f0 + o, job);
-      h[o] *= fmaf(-a, a, 1.0f);
-    }
+    for (int o = 0; o < kAQ; ++o) h[o] *= fac[o];
     to_tmem<kAQ>(lb, cA + f0, h);
     to_fm<kAQ>(Z, job, h, f0);
     sync_for_mma();
@@ -578,17 +592,20 @@ __global__ void __launch_bounds__(kAdjThreads, 1) k_tc_adjoint(const float* __re
       issue_delta(tb, wb + kWBytes);                 // W3 delta3
       commit(bar);
     }
-    wait();
-    // delta2 = (W3 delta3) (1 - h2^2); h1 recomputed into H3
-    from_tmem<kAQ>(lb, cD + f0, h);
 #pragma unroll
     for (int o = 0; o < kAQ; ++o) {
       const float a = fm_at(H2, f0 + o, job);
-      h[o] *= fmaf(-a, a, 1.0f);
+      fac[o] = fmaf(-a, a, 1.0f);
     }
+    // h1 recomputed into H3 (its last reader, dW4, completed at the previous wait)
     float h1[kAQ];
     layer1<kAQ>(small, x, h1, f0);
     to_fm<kAQ>(H3, job, h1, f0);
+    wait();
+    // delta2 = (W3 delta3) (1 - h2^2)
+    from_tmem<kAQ>(lb, cD + f0, h);
+#pragma unroll
+    for (int o = 0; o < kAQ; ++o) h[o] *= fac[o];
     to_tmem<kAQ>(lb, cA + f0, h);
     to_fm<kAQ>(Z, job, h, f0);
     sync_for_mma();
@@ -598,18 +615,27 @@ __global__ void __launch_bounds__(kAdjThreads, 1) k_tc_adjoint(const float* __re
       issue_delta(tb, wb);                           // W2 delta2
       commit(bar);
     }
+#pragma unroll
+    for (int o = 0; o < kAQ; ++o) fac[o] = fmaf(-h1[o], h1[o], 1.0f);
+    {  // the next tile's inputs into L2 (its first loads then wait on L2, not DRAM)
+      const int64_t nt = tile + gridDim.x;
+      if (nt < nbt) {
+        const int64_t q = nt * kBulkPts + t;
+        if (t < kBulkPts && q < nb) prefetch_l2(recs + q * kRecFloats);
+      } else if (nt < ntiles) {
+        const int64_t j = jbeg + (nt - nbt) * kTile + (t & (kTile - 1));
+        if (j < jend) {
+          if (t < kTile) prefetch_l2(w.jx + j);
+          else if (t < 2 * kTile) prefetch_l2(w.jg + j);
+        }
+      }
+    }
     wait();
     // delta1 = (W2 delta2) (1 - h1^2); dW1^T | db1 = delta1^T [x, y, z, 1]
     from_tmem<kAQ>(lb, cD + f0, h);
 #pragma unroll
-    for (int o = 0; o < kAQ; ++o) h[o] *= fmaf(-h1[o], h1[o], 1.0f);
+    for (int o = 0; o < kAQ; ++o) h[o] *= fac[o];
     to_fm<kAQ>(Z, job, h, f0);
-    if (!f0) {
-      *reinterpret_cast<float*>(GX + foff(0, job)) = tf32(x[0]);
-      *reinterpret_cast<float*>(GX + foff(1, job)) = tf32(x[1]);
-      *reinterpret_cast<float*>(GX + foff(2, job)) = tf32(x[2]);
-      *reinterpret_cast<float*>(GX + foff(3, job)) = 1.0f;
-    }
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
