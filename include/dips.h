@@ -91,7 +91,19 @@ typedef struct {
   const float* bulk_rec;    /* [n][16] optional: each bulk point's packed record
                                (dips_pack_bulk_records), one 64-byte read per point per step;
                                NULL: gathered from the arrays above every step */
+  /* Optional nonlinear operators (trainer.py:992-1017; the residual adds
+     N-(u-) V- + N+(u+) V+ at an interior point, discretization.py:369).  NULL nl_pt: none.
+     With them every point takes the general path (no bulk points), and the plain method and the
+     coefficient derivative refuse the records (DIPS_E_ARG). */
+  const float* nl_pt;       /* [n][4] K-, K+, V-, V+ (dips_geometry_assemble_nl): u-/+ at the point
+                               = K-/+ + sum over its jobs of the job's weight times its value */
+  const float* nl_w;        /* [jobs][2] the job's weights in u- and u+ at the point */
+  int32_t nl_kind[2];       /* per network (u-, u+): DIPS_NL_ZERO or DIPS_NL_SINH */
+  float nl_c[2];            /* DIPS_NL_SINH: N(u) = c sinh(u) */
 } dips_records_t;
+
+#define DIPS_NL_ZERO 0
+#define DIPS_NL_SINH 1
 
 typedef struct {
   int32_t m_layers, m_width, p_layers, p_width; /* DoubleMLP hidden layers and widths, tanh */
@@ -158,6 +170,14 @@ int dips_geometry_assemble(const dips_levelset_t* ls, const float* pts, int64_t 
                            const int64_t* job_off, const dips_coeffs_t* co, float* lhs0, float* diag,
                            float* rod, int32_t* cnt, int32_t* cnt_m, uint16_t* job_code, float* job_A,
                            float* coeff26, float* beta_int, cudaStream_t stream);
+/* dips_geometry_assemble that also writes the nonlinear operators' arguments: nl_pt ([n][4]:
+   K-, K+, V-, V+) and nl_w ([jobs][2], job order of job_code) as dips_records_t describes them
+   (u_mp_at_point at the point, discretization.py:426-519).  Both NULL: dips_geometry_assemble. */
+int dips_geometry_assemble_nl(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
+                              const uint32_t* flags, const int64_t* tri_off, const int64_t* xs_off,
+                              const int64_t* job_off, const dips_coeffs_t* co, float* lhs0, float* diag,
+                              float* rod, int32_t* cnt, int32_t* cnt_m, uint16_t* job_code, float* job_A,
+                              float* coeff26, float* beta_int, float* nl_pt, float* nl_w, cudaStream_t stream);
 
 /* Derivative of the records along a direction in coefficient space (no counterpart in the
    reference, which would take jax.jvp of its assembly): dco holds the derivative of every

@@ -732,7 +732,8 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
                            const int64_t* __restrict__ job_off, dips_coeffs_t co, dips_coeffs_t dco,
                            float* __restrict__ lhs0_out, float* __restrict__ diag_out, float* __restrict__ rod_out,
                            int32_t* __restrict__ cnt_out, int32_t* __restrict__ cntm_out, uint16_t* __restrict__ code_out,
-                           float* __restrict__ A_out, float* __restrict__ coeff26_out, float* __restrict__ beta_int_out) {
+                           float* __restrict__ A_out, float* __restrict__ coeff26_out, float* __restrict__ beta_int_out,
+                           float* __restrict__ nl_pt_out, float* __restrict__ nl_w_out) {
   LevelSet L = L0;
   levelset_init(L);
   const float* h = hh.v;
@@ -744,11 +745,17 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
     int64_t wm = job_off[i];          // u- jobs from the front
     int64_t wp = job_off[i + 1] - 1;  // u+ jobs from the back
     int nm = 0, np = 0;
-    // A: the job's coefficient, or its tangent
-    auto emit = [&](int j, int k, bool netp, float A) {
+    // A: the job's coefficient, or its tangent; xm, xp: the job's weights in u- and u+ at the
+    // point itself (the nonlinear operator's arguments; only the centre stencil point's jobs
+    // have any)
+    auto emit = [&](int j, int k, bool netp, float A, float xm = 0.0f, float xp = 0.0f) {
       const int64_t o = netp ? wp : wm;
       if (!TAN) code_out[o] = job_code(j, k, netp);
       A_out[o] = A;
+      if (!TAN && nl_w_out) {
+        nl_w_out[2 * o] = xm;
+        nl_w_out[2 * o + 1] = xp;
+      }
       if (netp) {
         --wp;
         ++np;
@@ -810,6 +817,8 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
       const bool net = (f >> kFlagNetS) & 1u;
       emit(0, kCubeCentre, net, TAN ? 0.0f : V);
       lhs0_out[i] = 0.0f;
+      if (!TAN && nl_pt_out)  // no nonlinear term on the box boundary (discretization.py:389-393)
+        reinterpret_cast<float4*>(nl_pt_out)[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       if (TAN) {
         diag_out[i] = 0.0f;
         rod_out[i] = isfinite(__fdiv_rn(__fmul_rn(co.g[i], V), V)) ? tsample(dco.g, i) : 0.0f;
@@ -854,16 +863,20 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
       tAp[j] = -t26[2 * (j - 1) + 1];
     }
     float lhs0 = 0.0f, tlhs0 = 0.0f;
+    // the nonlinear operator's arguments at the point (discretization.py:369 with u_mp_at_point,
+    // :426-519): u- = Km + sum of the jobs' xm weights times their values, u+ likewise.  A point
+    // off the interface has u- = u (in Omega-) and u+ = 0, or the reverse.
+    float nlK[2] = {0.0f, 0.0f};
     int64_t ox = xs_off[i];
     for (int j = 0; j < kStencil; ++j) {
       const int cj = dec_crossed(f, kFlagCrossedS + 2 * j);
       const bool netj = (f >> (kFlagNetS + j)) & 1u;
       if (cj == -1) {
-        emit(j, kCubeCentre, netj, TAN ? tAm[j] : Am[j]);
+        emit(j, kCubeCentre, netj, TAN ? tAm[j] : Am[j], j == 0 ? 1.0f : 0.0f, 0.0f);
         continue;
       }
       if (cj == 1) {
-        emit(j, kCubeCentre, netj, TAN ? tAp[j] : Ap[j]);
+        emit(j, kCubeCentre, netj, TAN ? tAp[j] : Ap[j], 0.0f, j == 0 ? 1.0f : 0.0f);
         continue;
       }
       // interface stencil point: extrapolate the other phase (discretization.py:464-513)
@@ -949,12 +962,21 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
       const float wc = __fadd_rn(__fsub_rn(__fmul_rn(Ax, __fadd_rn(__fsub_rn(1.0f, g), G[kCubeCentre])),
                                            __fmul_rn(Ax, G[kCubeCentre])),
                                  Ao);
+      // at the centre stencil point: the extrapolated component (u- if pos, else u+) weighs the
+      // point's own value by (1 - g + G[centre]) - G[centre] and vertex k by -G[k], plus K; the
+      // other component is the point's own value
+      const bool c0 = j == 0;
+      const float xself = c0 ? __fsub_rn(__fadd_rn(__fsub_rn(1.0f, g), G[kCubeCentre]), G[kCubeCentre]) : 0.0f;
       // d wc: Ax (1 - g) + Ao as a function (the G[centre] terms cancel)
-      emit(j, kCubeCentre, netj, TAN ? tAx * (1.0f - g) - Ax * tg + tAo : wc);
+      emit(j, kCubeCentre, netj, TAN ? tAx * (1.0f - g) - Ax * tg + tAo : wc, c0 ? (pos ? xself : 1.0f) : 0.0f,
+           c0 ? (pos ? 1.0f : xself) : 0.0f);
       for (int k = 0; k < 27; ++k) {
         if (k == kCubeCentre || G[k] == 0.0f) continue;
-        emit(j, k, R.phi_v[k] >= 0.0f, TAN ? -(tAx * G[k] + Ax * tG(k)) : -__fmul_rn(Ax, G[k]));
+        const float xk = c0 ? -G[k] : 0.0f;
+        emit(j, k, R.phi_v[k] >= 0.0f, TAN ? -(tAx * G[k] + Ax * tG(k)) : -__fmul_rn(Ax, G[k]), pos ? xk : 0.0f,
+             pos ? 0.0f : xk);
       }
+      if (c0) nlK[pos ? 0 : 1] = K;
       lhs0 = __fadd_rn(lhs0, __fmul_rn(Ax, K));
       if (TAN) tlhs0 += tAx * K + Ax * tK;
     }
@@ -969,6 +991,7 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
       rod_out[i] = nan_to_num(__fdiv_rn(rhs, diag));
       cnt_out[i] = nm + np;
       cntm_out[i] = nm;
+      if (nl_pt_out) reinterpret_cast<float4*>(nl_pt_out)[i] = make_float4(nlK[0], nlK[1], Vm, Vp);
     }
   }
 }
@@ -1070,7 +1093,19 @@ extern "C" int dips_geometry_assemble(const dips_levelset_t* ls, const float* pt
                                       const int64_t* job_off, const dips_coeffs_t* co, float* lhs0, float* diag,
                                       float* rod, int32_t* cnt, int32_t* cnt_m, uint16_t* job_code, float* job_A,
                                       float* coeff26, float* beta_int, cudaStream_t stream) {
+  return dips_geometry_assemble_nl(ls, pts, n, h, flags, tri_off, xs_off, job_off, co, lhs0, diag, rod, cnt, cnt_m,
+                                   job_code, job_A, coeff26, beta_int, nullptr, nullptr, stream);
+}
+
+extern "C" int dips_geometry_assemble_nl(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
+                                         const uint32_t* flags, const int64_t* tri_off, const int64_t* xs_off,
+                                         const int64_t* job_off, const dips_coeffs_t* co, float* lhs0, float* diag,
+                                         float* rod, int32_t* cnt, int32_t* cnt_m, uint16_t* job_code, float* job_A,
+                                         float* coeff26, float* beta_int, float* nl_pt, float* nl_w,
+                                         cudaStream_t stream) {
   DIPS_REQUIRE(n >= 0 && h && co, DIPS_E_ARG, "dips_geometry_assemble: bad n, h or coeffs");
+  DIPS_REQUIRE((nl_pt == nullptr) == (nl_w == nullptr), DIPS_E_ARG,
+               "dips_geometry_assemble_nl: nl_pt and nl_w are given together");
   if (n == 0) return DIPS_OK;
   DIPS_REQUIRE(pts && flags && tri_off && xs_off && job_off && lhs0 && diag && rod && cnt && cnt_m && job_code && job_A,
                DIPS_E_ARG, "dips_geometry_assemble: null pointer");
@@ -1082,7 +1117,7 @@ extern "C" int dips_geometry_assemble(const dips_levelset_t* ls, const float* pt
   dips_coeffs_t none{};
   k_assemble<false><<<grid_for(n, 64), 64, 0, stream>>>(L, pts, n, make_h(h), flags, tri_off, xs_off, job_off, *co,
                                                         none, lhs0, diag, rod, cnt, cnt_m, job_code, job_A, coeff26,
-                                                        beta_int);
+                                                        beta_int, nl_pt, nl_w);
   DIPS_CHECK_LAUNCH("dips_geometry_assemble");
   return DIPS_OK;
 }
@@ -1103,7 +1138,7 @@ extern "C" int dips_geometry_assemble_tangent(const dips_levelset_t* ls, const f
   if (st) return st;
   k_assemble<true><<<grid_for(n, 64), 64, 0, stream>>>(L, pts, n, make_h(h), flags, tri_off, xs_off, job_off, *co,
                                                        *dco, d_lhs0, d_diag, d_rod, nullptr, nullptr, nullptr, d_job_A,
-                                                       nullptr, nullptr);
+                                                       nullptr, nullptr, nullptr, nullptr);
   DIPS_CHECK_LAUNCH("dips_geometry_assemble_tangent");
   return DIPS_OK;
 }

@@ -871,6 +871,7 @@ static int check_grid(const dips_records_t* rec, int nx, int ny, int nz) {
   DIPS_REQUIRE(rec && rec->job_off && rec->job_code && rec->job_A && rec->cnt && rec->cnt_m && rec->diag && rec->rod &&
                    rec->lhs0,
                DIPS_E_ARG, "krylov: null record pointer");
+  DIPS_REQUIRE(!rec->nl_pt, DIPS_E_ARG, "krylov: the operator with nonlinear terms is not linear (no BiCGSTAB)");
   DIPS_REQUIRE(nx > 0 && ny > 0 && nz > 0 && (int64_t)nx * ny * nz == rec->n_pts, DIPS_E_ARG,
                "krylov: records must be the %d x %d x %d grid nodes in C order (n_pts = %lld)", nx, ny, nz,
                (long long)rec->n_pts);

@@ -156,7 +156,7 @@ __global__ void k_count(const int32_t* __restrict__ ids, int64_t B, int64_t n_pt
 __global__ void k_count_multi(const Inst* __restrict__ T, int bulk_ok) {
   const Inst& I = T[blockIdx.y];
   if ((int64_t)blockIdx.x >= I.w.nblk) return;
-  count_body(I.ids, I.B, I.rec.n_pts, I.rec.cnt, I.rec.cnt_m, bulk_ok, I.w, blockIdx.x);
+  count_body(I.ids, I.B, I.rec.n_pts, I.rec.cnt, I.rec.cnt_m, bulk_ok && !I.rec.nl_pt, I.w, blockIdx.x);
 }
 
 __device__ __forceinline__ void scan_body(const Workspace& w) {
@@ -384,6 +384,21 @@ __device__ __forceinline__ double block_sum_d(double v) {
 // (up to 7 x 27): lhs = lhs0 + sum_j A_j u_j, r = P (lhs/diag - rhs/diag), dL/du_j = dL/dlhs A_j.
 // Each lane first loads its own point's records, so that a point's turn costs one round trip
 // for its jobs.
+//
+// With nonlinear operators (rec.nl_pt set) lhs also gets N-(u-) V- + N+(u+) V+ with u-/+ at the
+// point = K-/+ + sum_j x-/+_j u_j (discretization.py:369), and dL/du_j gets
+// dL/dlhs (N-'(u-) V- x-_j + N+'(u+) V+ x+_j).
+
+// N(u) and N'(u) of a nonlinear operator kind
+__device__ __forceinline__ void nl_eval(int kind, float c, float u, float& f, float& df) {
+  if (kind == DIPS_NL_SINH) {
+    f = c * sinhf(u);
+    df = c * coshf(u);
+  } else {
+    f = 0.0f;
+    df = 0.0f;
+  }
+}
 
 __device__ __forceinline__ void residual_body(const int32_t* __restrict__ ids, int64_t B, const dips_records_t& rec,
                                               const Workspace& w, float* __restrict__ residual_out, int bx) {
@@ -399,6 +414,9 @@ __device__ __forceinline__ void residual_body(const int32_t* __restrict__ ids, i
   int64_t om = 0, op = 0;
   int cm = 0, n = 0;
   float lhs0 = 0.0f, diag = 1.0f, rod = 0.0f, Pv = 1.0f;
+  const bool nl = rec.nl_pt != nullptr;
+  float4 nlp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  int64_t ro0 = 0, rop = 0;  // the point's jobs in the records (for their nonlinear weights)
   if (kind == 0) {
     const int64_t pid = batch_pid(ids, b);
     om = w.om[b];
@@ -410,6 +428,11 @@ __device__ __forceinline__ void residual_body(const int32_t* __restrict__ ids, i
     rod = rec.rod[pid];
     // the learned preconditioner scales both lhs/diag and rhs/diag (discretization.py:419-420)
     if (w.pre_P) Pv = w.pre_P[b];
+    if (nl) {
+      nlp = reinterpret_cast<const float4*>(rec.nl_pt)[pid];
+      ro0 = rec.job_off[pid];
+      rop = rec.job_off[pid + 1] - n;
+    }
   }
   unsigned todo = __ballot_sync(0xffffffffu, kind == 0);
   while (todo) {
@@ -417,38 +440,80 @@ __device__ __forceinline__ void residual_body(const int32_t* __restrict__ ids, i
     todo &= todo - 1;
     const int64_t g_om = __shfl_sync(0xffffffffu, om, owner), g_op = __shfl_sync(0xffffffffu, op, owner);
     const int g_cm = __shfl_sync(0xffffffffu, cm, owner), g_n = __shfl_sync(0xffffffffu, n, owner);
-    float av[kMaxJobRounds];
-    float part = 0.0f;
+    float av[kMaxJobRounds], xm[kMaxJobRounds], xp[kMaxJobRounds];
+    float part = 0.0f, pm = 0.0f, pp = 0.0f;
+    if (nl) {
+      const int64_t g_ro0 = __shfl_sync(0xffffffffu, ro0, owner), g_rop = __shfl_sync(0xffffffffu, rop, owner);
 #pragma unroll
-    for (int k = 0; k < kMaxJobRounds; ++k) {
-      const int q = lane + 32 * k;
-      av[k] = 0.0f;
-      if (q < g_n) {
-        const int64_t j = q < g_cm ? g_om + q : g_op + (q - g_cm);
-        av[k] = w.jA[j];
-        part = fmaf(av[k], w.ju[j], part);
+      for (int k = 0; k < kMaxJobRounds; ++k) {
+        const int q = lane + 32 * k;
+        av[k] = xm[k] = xp[k] = 0.0f;
+        if (q < g_n) {
+          const int64_t j = q < g_cm ? g_om + q : g_op + (q - g_cm);
+          const int64_t r = q < g_cm ? g_ro0 + q : g_rop + q;
+          av[k] = w.jA[j];
+          const float u = w.ju[j];
+          const float2 x = reinterpret_cast<const float2*>(rec.nl_w)[r];
+          xm[k] = x.x;
+          xp[k] = x.y;
+          part = fmaf(av[k], u, part);
+          pm = fmaf(x.x, u, pm);
+          pp = fmaf(x.y, u, pp);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < kMaxJobRounds; ++k) {
+        const int q = lane + 32 * k;
+        av[k] = xm[k] = xp[k] = 0.0f;
+        if (q < g_n) {
+          const int64_t j = q < g_cm ? g_om + q : g_op + (q - g_cm);
+          av[k] = w.jA[j];
+          part = fmaf(av[k], w.ju[j], part);
+        }
       }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    float gs = 0.0f;
+    if (nl) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        pm += __shfl_xor_sync(0xffffffffu, pm, o);
+        pp += __shfl_xor_sync(0xffffffffu, pp, o);
+      }
+    }
+    float gs = 0.0f, gm = 0.0f, gp = 0.0f;
     if (lane == owner) {
-      const float lhs = lhs0 + part;
+      float lhs = lhs0 + part;
+      float dm = 0.0f, dp = 0.0f;
+      if (nl) {
+        float fm, fp;
+        nl_eval(rec.nl_kind[0], rec.nl_c[0], nlp.x + pm, fm, dm);
+        nl_eval(rec.nl_kind[1], rec.nl_c[1], nlp.y + pp, fp, dp);
+        lhs += fm * nlp.z + fp * nlp.w;
+        dm *= nlp.z;
+        dp *= nlp.w;
+      }
       const float qv = lhs / diag;
       const float r0 = nan_to_num(qv) - rod;
       const float r = Pv * r0;
       // d(mean 0.5 r^2)/d lhs; nan_to_num has zero derivative where lhs/diag is not finite
       gs = isfinite(qv) ? (r / (float)B) * Pv / diag : 0.0f;
+      gm = gs * dm;
+      gp = gs * dp;
       w.gs[b] = gs;
       if (w.pre_P) w.pre_r0[b] = r0;
       if (residual_out) residual_out[b] = r;
       l = 0.5 * (double)r * (double)r;
     }
     gs = __shfl_sync(0xffffffffu, gs, owner);
+    gm = __shfl_sync(0xffffffffu, gm, owner);
+    gp = __shfl_sync(0xffffffffu, gp, owner);
 #pragma unroll
     for (int k = 0; k < kMaxJobRounds; ++k) {
       const int q = lane + 32 * k;
-      if (q < g_n) w.jg[q < g_cm ? g_om + q : g_op + (q - g_cm)] = gs * av[k];
+      if (q < g_n) w.jg[q < g_cm ? g_om + q : g_op + (q - g_cm)] = nl ? fmaf(gp, xp[k], fmaf(gm, xm[k], gs * av[k]))
+                                                                        : gs * av[k];
     }
   }
   const double t = block_sum_d(l);
@@ -795,6 +860,12 @@ static int check_rec(const dips_records_t* rec, int64_t B) {
                    rec->job_code && rec->job_A,
                DIPS_E_ARG, "records: null pointer");
   DIPS_REQUIRE(B > 0 && B <= 0x7fffffff, DIPS_E_ARG, "batch size must be in [1, 2^31)");
+  DIPS_REQUIRE((rec->nl_pt == nullptr) == (rec->nl_w == nullptr), DIPS_E_ARG,
+               "records: nl_pt and nl_w are given together");
+  if (rec->nl_pt)
+    for (int k = 0; k < 2; ++k)
+      DIPS_REQUIRE(rec->nl_kind[k] == DIPS_NL_ZERO || rec->nl_kind[k] == DIPS_NL_SINH, DIPS_E_ARG,
+                   "records: unknown nonlinear operator kind %d", rec->nl_kind[k]);
   return DIPS_OK;
 }
 
@@ -834,7 +905,8 @@ static int expand(const dips_records_t* rec, const int32_t* ids, int64_t B, Work
                   const Marks* mk, cudaStream_t s) {
   const int nblk = (int)W.nblk;
   mark(mk, kMarkStart, s);
-  k_count<<<nblk, kScanBlock, 0, s>>>(ids, B, rec->n_pts, rec->cnt, rec->cnt_m, bulk_ok, W);
+  // with nonlinear operators every point takes the general path
+  k_count<<<nblk, kScanBlock, 0, s>>>(ids, B, rec->n_pts, rec->cnt, rec->cnt_m, bulk_ok && !rec->nl_pt, W);
   k_scan_blocks<<<1, kScanBlock, 0, s>>>(W);
   k_emit<<<nblk, kScanBlock, 0, s>>>(ids, B, *rec, W);
   DIPS_CHECK_LAUNCH("batch expansion");
@@ -963,6 +1035,8 @@ extern "C" int dips_loss_coeff_tangent(const dips_arch_t* arch, const float* par
   DIPS_REQUIRE(arch->pre_layers == 0, DIPS_E_UNSUPPORTED,
                "dips_loss_coeff_tangent: the learned preconditioner's dependence on the coefficients is not "
                "differentiated");
+  DIPS_REQUIRE(!rec->nl_pt, DIPS_E_UNSUPPORTED,
+               "dips_loss_coeff_tangent: the nonlinear operators' terms are not differentiated along a coefficient");
   const ArchOps* ops = find_arch(arch);
   if (!ops) return DIPS_E_UNSUPPORTED;
   Workspace W;

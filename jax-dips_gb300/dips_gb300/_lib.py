@@ -171,6 +171,10 @@ class RecordsT(ctypes.Structure):
         ("job_A", c_void_p),
         ("coeff26", c_void_p),
         ("bulk_rec", c_void_p),
+        ("nl_pt", c_void_p),
+        ("nl_w", c_void_p),
+        ("nl_kind", c_i32 * 2),
+        ("nl_c", c_f32 * 2),
     ]
 
 
@@ -236,6 +240,12 @@ _SIGS = {
         c_i32,
         [P(LevelSetT), c_void_p, c_i64, P(c_f32), c_void_p, c_void_p, c_void_p, c_void_p, P(CoeffsT)]
         + [c_void_p] * 9
+        + [c_void_p],
+    ),
+    "dips_geometry_assemble_nl": (
+        c_i32,
+        [P(LevelSetT), c_void_p, c_i64, P(c_f32), c_void_p, c_void_p, c_void_p, c_void_p, P(CoeffsT)]
+        + [c_void_p] * 11
         + [c_void_p],
     ),
     "dips_geometry_assemble_tangent": (

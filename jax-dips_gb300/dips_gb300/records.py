@@ -20,7 +20,7 @@ import time
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, nonlinear
 from .levelset import LevelSetGrid
 
 F32 = np.float32
@@ -139,11 +139,17 @@ class FVLevel:
         self.job_A = torch.zeros(max(self.n_jobs_cap, 1), **f32)
         self.coeff26 = torch.empty(n, 26, **f32) if keep_geometry else None
         self.beta_int = torch.empty(n, **f32) if keep_geometry else None
+        # nonlinear operators (``nl_m``/``nl_p`` in the coefficient dict): their arguments' records
+        self.nl = (nonlinear.resolve(coeff_fns.get("nl_m")), nonlinear.resolve(coeff_fns.get("nl_p")))
+        has_nl = not (nonlinear.is_zero(self.nl[0]) and nonlinear.is_zero(self.nl[1]))
+        self.nl_pt = torch.empty(max(n, 1), 4, **f32) if has_nl else None
+        self.nl_w = torch.zeros(max(self.n_jobs_cap, 1), 2, **f32) if has_nl else None
         _lib.check(
-            lib.dips_geometry_assemble(ls.desc, P(self.pts), n, hc, P(flags), P(tri_off), P(xs_off), P(self.job_off),
-                                       co, P(self.lhs0), P(self.diag), P(self.rod), P(self.cnt), P(self.cnt_m),
-                                       P(self.job_code), P(self.job_A), P(self.coeff26), P(self.beta_int), st),
-            "dips_geometry_assemble",
+            lib.dips_geometry_assemble_nl(ls.desc, P(self.pts), n, hc, P(flags), P(tri_off), P(xs_off),
+                                          P(self.job_off), co, P(self.lhs0), P(self.diag), P(self.rod), P(self.cnt),
+                                          P(self.cnt_m), P(self.job_code), P(self.job_A), P(self.coeff26),
+                                          P(self.beta_int), P(self.nl_pt), P(self.nl_w), st),
+            "dips_geometry_assemble_nl",
         )
         mark("assemble")
         self.flags = flags if keep_geometry else None
@@ -157,6 +163,11 @@ class FVLevel:
             P(self.pts), n, (_lib.c_f32 * 3)(*[float(v) for v in self.h]), P(self.lhs0), P(self.diag), P(self.rod),
             P(self.cnt), P(self.cnt_m), P(self.job_off), P(self.job_code), P(self.job_A), P(self.coeff26), None,
         )
+        if has_nl:
+            self.desc.nl_pt = P(self.nl_pt)
+            self.desc.nl_w = P(self.nl_w)
+            self.desc.nl_kind = (_lib.c_i32 * 2)(self.nl[0].kind, self.nl[1].kind)
+            self.desc.nl_c = (_lib.c_f32 * 2)(self.nl[0].c, self.nl[1].c)
         # each bulk point's 64-byte record, packed once so that a step reads it in one piece
         self.bulk_rec = torch.empty(max(n, 1), 16, **f32)
         if n:

@@ -26,7 +26,7 @@ from typing import Callable
 import numpy as np
 import torch
 
-from . import _lib, dp, levelset, nn, ops
+from . import _lib, dp, levelset, nn, nonlinear, ops
 from .mesh import GridState
 from .records import FVLevel, eval_callable
 
@@ -199,7 +199,7 @@ class Trainer:
             h = self.h0 * F32(0.5**k)
             fns = {"mu_m": self.fn.mu_m_fn, "mu_p": self.fn.mu_p_fn, "k_m": self.fn.k_m_fn, "k_p": self.fn.k_p_fn,
                    "f_m": self.fn.f_m_fn, "f_p": self.fn.f_p_fn, "alpha": self.fn.alpha_fn, "beta": self.fn.beta_fn,
-                   "g": self.fn.dir_bc_fn}
+                   "g": self.fn.dir_bc_fn, "nl_m": self.fn.nonlinear_op_m, "nl_p": self.fn.nonlinear_op_p}
             # the learned preconditioner reads the 26 cell coefficients of each point
             self._level_cache[k] = FVLevel(self.ls, fns, self.points, h, keep_geometry=self.arch.pre_layers > 0)
         return self._level_cache[k]
@@ -377,12 +377,14 @@ class Trainer:
 
 def setup(initial_value_fn, dirichlet_bc_fn, lvl_set_fn, mu_m_fn_, mu_p_fn_, k_m_fn_, k_p_fn_, f_m_fn_, f_p_fn_,
           alpha_fn_, beta_fn_, nonlinear_op_m=None, nonlinear_op_p=None):
-    """``trainer.setup`` (trainer.py:980-1137)."""
-    if nonlinear_op_m is not None or nonlinear_op_p is not None:
-        raise NotImplementedError("nonlinear operators are not on the GB300 path (the reference's default is 0)")
-    zero = lambda u: 0.0  # noqa: E731
+    """``trainer.setup`` (trainer.py:980-1137).
+
+    ``nonlinear_op_m/p``: None (zero, the reference's default) or an operator of
+    ``dips_gb300.nonlinear`` (``Sinh(c)``: N(u) = c sinh(u)); any other callable raises
+    NotImplementedError, since the residual kernel evaluates the operator on the GPU."""
     fn = PoissonSimStateFn(initial_value_fn, dirichlet_bc_fn, lvl_set_fn, mu_m_fn_, mu_p_fn_, k_m_fn_, k_p_fn_,
-                           f_m_fn_, f_p_fn_, alpha_fn_, beta_fn_, zero, zero)
+                           f_m_fn_, f_p_fn_, alpha_fn_, beta_fn_, nonlinear.resolve(nonlinear_op_m),
+                           nonlinear.resolve(nonlinear_op_p))
 
     def init_fn(lvl_gstate: GridState = None, tr_gstate: GridState = None, eval_gstate: GridState = None,
                 num_epochs: int = 1000, batch_size: int = 131072, algorithm: int = 0,

@@ -4,8 +4,10 @@ TEST INFRASTRUCTURE ONLY (see ``nbm_oracle.py`` for the scope and the parity
 status).  The forward restates, literally, ``compute_Ax_and_b_preconditioned_fn``
 and ``get_u_mp_by_regression_at_point_fn`` (solvers/poisson/discretization.py:299-519)
 and ``Trainer.loss`` (solvers/poisson/trainer.py:892-912) with the preconditioner
-disabled (``precond = 1.0``, trainer.py:245-253) and no nonlinear operator
-(trainer.py:1007-1017).  The u^-/u^+ networks restate ``DoubleMLP``
+disabled (``precond = 1.0``, trainer.py:245-253).  The nonlinear operators N-(u-) V- +
+N+(u+) V+ (discretization.py:369) come from the problem's ``nl_m``/``nl_p`` callables
+(torch-callable; absent: zero, the reference's default, trainer.py:1007-1017).  The
+u^-/u^+ networks restate ``DoubleMLP``
 (nn/mlp/MLP.py:93-139): ``hk.Linear`` + tanh per hidden layer, ``Linear(1)`` out,
 u = MLP_p(x) where phi(x) >= 0 else MLP_m(x).
 
@@ -159,6 +161,7 @@ class ResidualGeometry:
         self.k_m, self.k_p = prob.co("k_m", p), prob.co("k_p", p)
         self.f_m, self.f_p = prob.co("f_m", p), prob.co("f_p", p)
         self.g = prob.co("g", p)
+        self.nl_m, self.nl_p = prob.fns.get("nl_m"), prob.fns.get("nl_p")
         self.stencil = O.stencil_points(p, h)  # (N,7,3)
         st = self.stencil.reshape(-1, 3)
         self.crossed_s = O.is_crossed(phi, st, h).reshape(N, 7)
@@ -234,6 +237,10 @@ def residual(flat_params, arch: Arch, rg: ResidualGeometry, dtype=torch.float32)
     so = ((((c[:, 1] + c[:, 3]) + c[:, 5]) + c[:, 7]) + c[:, 9]) + c[:, 11]
     lhs = km * Vm * u_m[:, 0]
     lhs = lhs + kp * Vp * u_p[:, 0]
+    if rg.nl_m is not None or rg.nl_p is not None:  # discretization.py:369
+        nm = rg.nl_m(u_m[:, 0]) if rg.nl_m is not None else torch.zeros_like(Vm)
+        npl = rg.nl_p(u_p[:, 0]) if rg.nl_p is not None else torch.zeros_like(Vp)
+        lhs = lhs + nm * Vm + npl * Vp
     lhs = lhs + se * u_m[:, 0] + so * u_p[:, 0]
     for j in range(1, 7):
         lhs = lhs + (-1.0 * c[:, 2 * (j - 1)] * u_m[:, j] - c[:, 2 * (j - 1) + 1] * u_p[:, j])

@@ -224,7 +224,8 @@ def make_harness(mods):
 
 def sim_state_fn_from(mods, fns, phi_fn):
     """``PoissonSimStateFn`` as ``trainer.setup`` builds it (trainer.py:995-1031): every
-    per-point callable vmapped, nonlinear operators zero."""
+    per-point callable vmapped; the nonlinear operators ``fns["nl_m"]``/``fns["nl_p"]`` passed
+    as they are (called on the scalar u at a point, discretization.py:369), zero when absent."""
     jax = sys.modules["jax"]
     SS = mods["simulation_states"].PoissonSimStateFn
     v = jax.vmap
@@ -232,8 +233,10 @@ def sim_state_fn_from(mods, fns, phi_fn):
     def zero(x):
         return 0.0
 
+    nl_m = fns.get("nl_m") or zero
+    nl_p = fns.get("nl_p") or zero
     return SS(v(fns["u0"]), v(fns["g"]), phi_fn, v(fns["mu_m"]), v(fns["mu_p"]), v(fns["k_m"]),
-              v(fns["k_p"]), v(fns["f_m"]), v(fns["f_p"]), v(fns["alpha"]), v(fns["beta"]), zero, zero)
+              v(fns["k_p"]), v(fns["f_m"]), v(fns["f_p"]), v(fns["alpha"]), v(fns["beta"]), nl_m, nl_p)
 
 
 def per_point(fn, dtype):

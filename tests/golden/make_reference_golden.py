@@ -62,6 +62,7 @@ CASES = {
     "sphere_mu10_1_16_3x32_l0": ("sphere_mu10_1", 16, (3, 32, 3, 32), 0, 160, 96),
     "blob16_4x64_l0": ("blob", 16, (4, 64, 4, 64), 0, 160, 96),
     "lpbe16_2x16_l0": ("lpbe", 16, (2, 16, 2, 16), 0, 160, 96),
+    "sphere16_sinh_3x32_l0": ("sphere_sinh", 16, (3, 32, 3, 32), 0, 160, 96),
 }
 
 
@@ -92,6 +93,10 @@ def problem(name):
         return problems.blob_problem()
     if name == "lpbe":
         return problems.lpbe_problem(*lpbe_spheres())
+    if name == "sphere_sinh":  # the sphere with nonlinear operators N-(u) = 300 sinh(u), N+(u) = 100 sinh(u)
+        from dips_gb300 import nonlinear
+
+        return dict(problems.sphere_problem(), nl_m=nonlinear.Sinh(300.0), nl_p=nonlinear.Sinh(100.0))
     raise KeyError(name)
 
 
@@ -137,6 +142,14 @@ def run_case(args):
     pts = R[ids]
     a = L.Arch(*arch)
     flat = case_params(arch)
+    if prob_name == "sphere_sinh":
+        # output biases +0.8 (u-) and -0.6 (u+): u of order one, where sinh is far from linear
+        sizes_m = L.net_sizes(*a.net("m"))
+        n_m = sum(i * o + o for i, o in sizes_m)
+        n_p = sum(i * o + o for i, o in L.net_sizes(*a.net("p")))
+        flat = flat.copy()
+        flat[n_m - 1] += F32(0.8)
+        flat[n_m + n_p - 1] -= F32(0.6)
     out = dict(name=np.array(name), problem=np.array(prob_name), n=np.int32(n), level=np.int32(level),
                arch=np.array(arch, np.int32), phi=phi, ids=ids, params=flat, h=h)
 
@@ -145,6 +158,9 @@ def run_case(args):
         fns = {k: H.per_point(prob[k], dtype) for k in ("mu_m", "mu_p", "k_m", "k_p", "f_m", "f_p", "alpha",
                                                          "beta", "g")}
         fns["u0"] = lambda r: 0.0
+        for k in ("nl_m", "nl_p"):
+            if k in prob:
+                fns[k] = prob[k]
         ssf = H.sim_state_fn_from(mods, fns, phi_fn)
         return H.make_harness(mods)(gs, ssf, a)
 

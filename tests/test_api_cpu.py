@@ -52,3 +52,24 @@ def test_sphere_beta_is_the_reference_flux_jump_convention():
     dn_up = 2 * 0.5
     dn_um = np.cos(0.5) * np.cos(0.0) * np.exp(0.0)
     assert np.isclose(pr["beta"](x)[0], -(10.0 * dn_up - 1.0 * dn_um), rtol=1e-6)
+
+
+def test_nonlinear_operators_are_callables_and_setup_refuses_others():
+    torch = pytest.importorskip("torch")
+    from dips_gb300 import nonlinear, trainer
+
+    s = nonlinear.Sinh(2.5)
+    u = np.linspace(-2, 2, 9).astype(np.float32)
+    v = s(u)
+    assert v.dtype == np.float32
+    np.testing.assert_allclose(v, 2.5 * np.sinh(u), rtol=1e-6)
+    np.testing.assert_allclose(s(torch.as_tensor(u)).numpy(), v, rtol=1e-6)
+    assert nonlinear.resolve(None).kind == nonlinear.ZERO_KIND and nonlinear.is_zero(None)
+    assert nonlinear.resolve(s) is s and not nonlinear.is_zero(s)
+    with pytest.raises(NotImplementedError):
+        nonlinear.resolve(lambda x: x**3)
+    one = lambda r: 1.0  # noqa: E731
+    init_fn = trainer.setup(one, one, one, one, one, one, one, one, one, one, one, nonlinear_op_m=s)
+    assert callable(init_fn)
+    with pytest.raises(NotImplementedError):
+        trainer.setup(one, one, one, one, one, one, one, one, one, one, one, nonlinear_op_p=np.cbrt)
