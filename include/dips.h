@@ -95,7 +95,7 @@ typedef struct {
      N-(u-) V- + N+(u+) V+ at an interior point, discretization.py:369).  NULL nl_pt: none.
      With them every point takes the general path (no bulk points), and the plain method and the
      coefficient derivative refuse the records (DIPS_E_ARG). */
-  const float* nl_pt;       /* [n][4] K-, K+, V-, V+ (dips_geometry_assemble_nl): u-/+ at the point
+  const float* nl_pt;       /* [n][4] K-, K+, V-, V+ (dips_geometry_assemble_ex): u-/+ at the point
                                = K-/+ + sum over its jobs of the job's weight times its value */
   const float* nl_w;        /* [jobs][2] the job's weights in u- and u+ at the point */
   int32_t nl_kind[2];       /* per network (u-, u+): DIPS_NL_ZERO or DIPS_NL_SINH */
@@ -170,14 +170,21 @@ int dips_geometry_assemble(const dips_levelset_t* ls, const float* pts, int64_t 
                            const int64_t* job_off, const dips_coeffs_t* co, float* lhs0, float* diag,
                            float* rod, int32_t* cnt, int32_t* cnt_m, uint16_t* job_code, float* job_A,
                            float* coeff26, float* beta_int, cudaStream_t stream);
-/* dips_geometry_assemble that also writes the nonlinear operators' arguments: nl_pt ([n][4]:
-   K-, K+, V-, V+) and nl_w ([jobs][2], job order of job_code) as dips_records_t describes them
-   (u_mp_at_point at the point, discretization.py:426-519).  Both NULL: dips_geometry_assemble. */
-int dips_geometry_assemble_nl(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
+/* dips_geometry_assemble with two optional parts:
+   - nl_pt ([n][4]: K-, K+, V-, V+) and nl_w ([jobs][2], job order of job_code): the nonlinear
+     operators' arguments as dips_records_t describes them (u_mp_at_point at the point,
+     discretization.py:426-519); both NULL: none;
+   - scratch (dips_geometry_assemble_scratch_bytes(n) bytes, 4-byte aligned, device memory):
+     the points with an interface stencil point are listed there and assembled by a second
+     launch, 32 to a warp, instead of a few per warp among bulk points; NULL: one launch.
+   The records are the same either way. */
+size_t dips_geometry_assemble_scratch_bytes(int64_t n);
+int dips_geometry_assemble_ex(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
                               const uint32_t* flags, const int64_t* tri_off, const int64_t* xs_off,
                               const int64_t* job_off, const dips_coeffs_t* co, float* lhs0, float* diag,
                               float* rod, int32_t* cnt, int32_t* cnt_m, uint16_t* job_code, float* job_A,
-                              float* coeff26, float* beta_int, float* nl_pt, float* nl_w, cudaStream_t stream);
+                              float* coeff26, float* beta_int, float* nl_pt, float* nl_w, void* scratch,
+                              size_t scratch_bytes, cudaStream_t stream);
 
 /* Derivative of the records along a direction in coefficient space (no counterpart in the
    reference, which would take jax.jvp of its assembly): dco holds the derivative of every

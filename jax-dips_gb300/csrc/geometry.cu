@@ -322,6 +322,28 @@ __device__ __forceinline__ float face_area_m(const Cell& cell, int ta, int tb, i
 
 __device__ __forceinline__ float pos_or_zero(float v) { return v < 0.0f ? 0.0f : v; }
 
+// The 26 cell coefficients of a cell that the interface does not cross (crossed = -1 or +1):
+// full faces and volume on its side
+__device__ __forceinline__ void face_coefficients_uncrossed(int crossed, const float h[3], const float mm[6],
+                                                            const float mp[6], float out[26]) {
+  const float dx = h[0], dy = h[1], dz = h[2];
+  const float vol = __fmul_rn(__fmul_rn(dx, dy), dz);
+  const float ax = __fmul_rn(dy, dz), ay = __fmul_rn(dx, dz), az = __fmul_rn(dx, dy);
+  const float sm = crossed < 0 ? 1.0f : 0.0f;
+  const float sp = crossed > 0 ? 1.0f : 0.0f;
+  const float nom[6] = {ax, ax, ay, ay, az, az};
+  const float hh[6] = {dx, dx, dy, dy, dz, dz};
+#pragma unroll
+  for (int f = 0; f < 6; ++f) {
+    out[2 * f] = __fdiv_rn(__fmul_rn(nom[f], __fmul_rn(mm[f], sm)), hh[f]);
+    out[2 * f + 1] = __fdiv_rn(__fmul_rn(nom[f], __fmul_rn(mp[f], sp)), hh[f]);
+    out[14 + 2 * f] = __fmul_rn(nom[f], sm);
+    out[14 + 2 * f + 1] = __fmul_rn(nom[f], sp);
+  }
+  out[12] = __fmul_rn(vol, sm);
+  out[13] = __fmul_rn(vol, sp);
+}
+
 // The 26 cell coefficients of compute_face_centroids_values_plus_minus_at_point
 // (geom_pp.py:514-1007); mu at the 6 face centres are caller-supplied samples.
 __device__ void face_coefficients(const Cell& cell, const float p[3], const float h[3], const float mm[6],
@@ -363,19 +385,7 @@ __device__ void face_coefficients(const Cell& cell, const float p[3], const floa
     out[12] = vol_m;
     out[13] = vol_p;
   } else {
-    const float sm = cell.crossed < 0 ? 1.0f : 0.0f;
-    const float sp = cell.crossed > 0 ? 1.0f : 0.0f;
-    const float nom[6] = {ax, ax, ay, ay, az, az};
-    const float hh[6] = {dx, dx, dy, dy, dz, dz};
-#pragma unroll
-    for (int f = 0; f < 6; ++f) {
-      out[2 * f] = __fdiv_rn(__fmul_rn(nom[f], __fmul_rn(mm[f], sm)), hh[f]);
-      out[2 * f + 1] = __fdiv_rn(__fmul_rn(nom[f], __fmul_rn(mp[f], sp)), hh[f]);
-      out[14 + 2 * f] = __fmul_rn(nom[f], sm);
-      out[14 + 2 * f + 1] = __fmul_rn(nom[f], sp);
-    }
-    out[12] = __fmul_rn(vol, sm);
-    out[13] = __fmul_rn(vol, sp);
+    face_coefficients_uncrossed(cell.crossed, h, mm, mp, out);
   }
 }
 
@@ -726,19 +736,50 @@ __device__ __forceinline__ float tsample(const float* a, int64_t i) { return a ?
 // geometry is the same in both modes and the branches (which phase is extrapolated, which cube
 // vertices have a weight) are the records' own, so the tangent is the exact derivative of the
 // records as a function of the coefficients.
-template <bool TAN>
+// Passes of k_assemble: every point in one pass (kAllPoints), or two passes that keep the heavy
+// points together: kDeferHeavy does the points without an interface stencil point and lists
+// the others; kListed does the listed points.  A point with interface stencil points costs
+// about a hundred times a bulk point (regression, five-tetrahedron clipping) and such points come
+// a few to a warp of 32 consecutive points, so in one pass most of a warp idles while its heavy
+// lanes run; listed, 32 heavy points share a warp.
+enum AssemblePass { kAllPoints = 0, kDeferHeavy = 1, kListed = 2 };
+
+__device__ __forceinline__ bool heavy_point(uint32_t f) {
+  bool x = false;
+#pragma unroll
+  for (int j = 0; j < kStencil; ++j) x |= dec_crossed(f, kFlagCrossedS + 2 * j) == 0;
+  return x;
+}
+
+template <bool TAN, int PASS = kAllPoints>
 __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n, H3 hh, const uint32_t* __restrict__ flags,
                            const int64_t* __restrict__ tri_off, const int64_t* __restrict__ xs_off,
                            const int64_t* __restrict__ job_off, dips_coeffs_t co, dips_coeffs_t dco,
                            float* __restrict__ lhs0_out, float* __restrict__ diag_out, float* __restrict__ rod_out,
                            int32_t* __restrict__ cnt_out, int32_t* __restrict__ cntm_out, uint16_t* __restrict__ code_out,
                            float* __restrict__ A_out, float* __restrict__ coeff26_out, float* __restrict__ beta_int_out,
-                           float* __restrict__ nl_pt_out, float* __restrict__ nl_w_out) {
+                           float* __restrict__ nl_pt_out, float* __restrict__ nl_w_out,
+                           int32_t* __restrict__ heavy_list = nullptr, int32_t* __restrict__ heavy_count = nullptr) {
   LevelSet L = L0;
   levelset_init(L);
   const float* h = hh.v;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t end = PASS == kListed ? (int64_t)*heavy_count : n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < end; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = PASS == kListed ? (int64_t)heavy_list[t] : t;
     const uint32_t f = flags[i];
+    if (PASS == kDeferHeavy) {
+      const bool heavy = heavy_point(f);
+      const unsigned act = __activemask();
+      const unsigned m = __ballot_sync(act, heavy);
+      if (m) {
+        const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(heavy_count, __popc(m));
+        base = __shfl_sync(act, base, leader);
+        if (heavy) heavy_list[base + __popc(m & ((1u << lane) - 1))] = (int32_t)i;
+      }
+      if (heavy) continue;
+    }
     float p[3];
     load_point(pts, i, p);
     const float V = __fmul_rn(__fmul_rn(h[0], h[1]), h[2]);
@@ -765,7 +806,16 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
       }
     };
     Cell cell;
-    cell_eval(L, p, h, cell);
+    // The centre cell's crossing is in the flags (k_classify evaluates the same corners with the
+    // same arithmetic).  Off the interface nothing below reads the corners, so they are sampled
+    // only for a crossed cell: 8 trilinear phi samples saved at 98 % of the points.
+    // (the kDeferHeavy pass sees no crossed cell or stencil point: its instance leaves out that
+    // code, so it needs fewer registers)
+    const int cpc = dec_crossed(f, kFlagCrossedP);
+    if (PASS != kDeferHeavy && cpc == 0)
+      cell_eval(L, p, h, cell);
+    else
+      cell.crossed = cpc;
     float mm[6], mp[6], tmm[6], tmp[6];
     for (int q = 0; q < 6; ++q) {
       mm[q] = co.mu_m_face[6 * i + q];
@@ -774,7 +824,10 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
       tmp[q] = TAN ? tsample(dco.mu_p_face, 6 * i + q) : 0.0f;
     }
     float c26[26], t26[26];
-    face_coefficients(cell, p, h, mm, mp, c26);
+    if (PASS == kDeferHeavy)
+      face_coefficients_uncrossed(cell.crossed, h, mm, mp, c26);
+    else
+      face_coefficients(cell, p, h, mm, mp, c26);
     if (TAN) {
       // the face fluxes (entries 0..11) are linear in the face mu's; the rest is geometry
       face_coefficients(cell, p, h, tmm, tmp, t26);
@@ -782,7 +835,7 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
     }
     // interface integral of beta (integrate_over_interface_at_point, geom_pp.py:383-420)
     float bint = 0.0f, tbint = 0.0f;
-    if (cell.crossed == 0) {
+    if (PASS != kDeferHeavy && cell.crossed == 0) {
       const float b0 = co.beta_origin;
       const float pad_mean = __fdiv_rn(__fadd_rn(__fadd_rn(b0, b0), b0), 3.0f);
       const float pad_term = __fmul_rn(0.0f, pad_mean);
@@ -879,6 +932,7 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
         emit(j, kCubeCentre, netj, TAN ? tAp[j] : Ap[j], 0.0f, j == 0 ? 1.0f : 0.0f);
         continue;
       }
+      if (PASS == kDeferHeavy) continue;  // not reached: such points are listed
       // interface stencil point: extrapolate the other phase (discretization.py:464-513)
       float s[3];
       stencil_point(p, h, j, s);
@@ -1093,19 +1147,23 @@ extern "C" int dips_geometry_assemble(const dips_levelset_t* ls, const float* pt
                                       const int64_t* job_off, const dips_coeffs_t* co, float* lhs0, float* diag,
                                       float* rod, int32_t* cnt, int32_t* cnt_m, uint16_t* job_code, float* job_A,
                                       float* coeff26, float* beta_int, cudaStream_t stream) {
-  return dips_geometry_assemble_nl(ls, pts, n, h, flags, tri_off, xs_off, job_off, co, lhs0, diag, rod, cnt, cnt_m,
-                                   job_code, job_A, coeff26, beta_int, nullptr, nullptr, stream);
+  return dips_geometry_assemble_ex(ls, pts, n, h, flags, tri_off, xs_off, job_off, co, lhs0, diag, rod, cnt, cnt_m,
+                                   job_code, job_A, coeff26, beta_int, nullptr, nullptr, nullptr, 0, stream);
 }
 
-extern "C" int dips_geometry_assemble_nl(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
+extern "C" size_t dips_geometry_assemble_scratch_bytes(int64_t n) {
+  return n <= 0 ? 0 : (size_t)(n + 1) * sizeof(int32_t);
+}
+
+extern "C" int dips_geometry_assemble_ex(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
                                          const uint32_t* flags, const int64_t* tri_off, const int64_t* xs_off,
                                          const int64_t* job_off, const dips_coeffs_t* co, float* lhs0, float* diag,
                                          float* rod, int32_t* cnt, int32_t* cnt_m, uint16_t* job_code, float* job_A,
-                                         float* coeff26, float* beta_int, float* nl_pt, float* nl_w,
-                                         cudaStream_t stream) {
+                                         float* coeff26, float* beta_int, float* nl_pt, float* nl_w, void* scratch,
+                                         size_t scratch_bytes, cudaStream_t stream) {
   DIPS_REQUIRE(n >= 0 && h && co, DIPS_E_ARG, "dips_geometry_assemble: bad n, h or coeffs");
   DIPS_REQUIRE((nl_pt == nullptr) == (nl_w == nullptr), DIPS_E_ARG,
-               "dips_geometry_assemble_nl: nl_pt and nl_w are given together");
+               "dips_geometry_assemble_ex: nl_pt and nl_w are given together");
   if (n == 0) return DIPS_OK;
   DIPS_REQUIRE(pts && flags && tri_off && xs_off && job_off && lhs0 && diag && rod && cnt && cnt_m && job_code && job_A,
                DIPS_E_ARG, "dips_geometry_assemble: null pointer");
@@ -1115,10 +1173,26 @@ extern "C" int dips_geometry_assemble_nl(const dips_levelset_t* ls, const float*
   int st = make_ls(ls, &L, stream);
   if (st) return st;
   dips_coeffs_t none{};
-  k_assemble<false><<<grid_for(n, 64), 64, 0, stream>>>(L, pts, n, make_h(h), flags, tri_off, xs_off, job_off, *co,
-                                                        none, lhs0, diag, rod, cnt, cnt_m, job_code, job_A, coeff26,
-                                                        beta_int, nl_pt, nl_w);
-  DIPS_CHECK_LAUNCH("dips_geometry_assemble");
+  if (!scratch) {
+    k_assemble<false><<<grid_for(n, 64), 64, 0, stream>>>(L, pts, n, make_h(h), flags, tri_off, xs_off, job_off, *co,
+                                                          none, lhs0, diag, rod, cnt, cnt_m, job_code, job_A, coeff26,
+                                                          beta_int, nl_pt, nl_w);
+    DIPS_CHECK_LAUNCH("dips_geometry_assemble");
+    return DIPS_OK;
+  }
+  DIPS_REQUIRE(scratch_bytes >= dips_geometry_assemble_scratch_bytes(n) && ((uintptr_t)scratch & 3) == 0,
+               DIPS_E_WORKSPACE, "dips_geometry_assemble_ex: scratch too small or misaligned");
+  int32_t* count = static_cast<int32_t*>(scratch);
+  int32_t* list = count + 1;
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int32_t), stream);
+  if (e != cudaSuccess) return cuda_status(e, "dips_geometry_assemble_ex: scratch counter");
+  k_assemble<false, kDeferHeavy><<<grid_for(n, 64), 64, 0, stream>>>(
+      L, pts, n, make_h(h), flags, tri_off, xs_off, job_off, *co, none, lhs0, diag, rod, cnt, cnt_m, job_code, job_A,
+      coeff26, beta_int, nl_pt, nl_w, list, count);
+  k_assemble<false, kListed><<<grid_for(n, 64), 64, 0, stream>>>(
+      L, pts, n, make_h(h), flags, tri_off, xs_off, job_off, *co, none, lhs0, diag, rod, cnt, cnt_m, job_code, job_A,
+      coeff26, beta_int, nl_pt, nl_w, list, count);
+  DIPS_CHECK_LAUNCH("dips_geometry_assemble_ex");
   return DIPS_OK;
 }
 

@@ -242,11 +242,12 @@ _SIGS = {
         + [c_void_p] * 9
         + [c_void_p],
     ),
-    "dips_geometry_assemble_nl": (
+    "dips_geometry_assemble_scratch_bytes": (ctypes.c_size_t, [c_i64]),
+    "dips_geometry_assemble_ex": (
         c_i32,
         [P(LevelSetT), c_void_p, c_i64, P(c_f32), c_void_p, c_void_p, c_void_p, c_void_p, P(CoeffsT)]
-        + [c_void_p] * 11
-        + [c_void_p],
+        + [c_void_p] * 12
+        + [ctypes.c_size_t, c_void_p],
     ),
     "dips_geometry_assemble_tangent": (
         c_i32,

@@ -144,12 +144,15 @@ class FVLevel:
         has_nl = not (nonlinear.is_zero(self.nl[0]) and nonlinear.is_zero(self.nl[1]))
         self.nl_pt = torch.empty(max(n, 1), 4, **f32) if has_nl else None
         self.nl_w = torch.zeros(max(self.n_jobs_cap, 1), 2, **f32) if has_nl else None
+        # the points next to the interface are listed and assembled together (second launch)
+        scratch = torch.empty(max(int(lib.dips_geometry_assemble_scratch_bytes(n)), 4), dtype=torch.uint8, device=dev)
         _lib.check(
-            lib.dips_geometry_assemble_nl(ls.desc, P(self.pts), n, hc, P(flags), P(tri_off), P(xs_off),
+            lib.dips_geometry_assemble_ex(ls.desc, P(self.pts), n, hc, P(flags), P(tri_off), P(xs_off),
                                           P(self.job_off), co, P(self.lhs0), P(self.diag), P(self.rod), P(self.cnt),
                                           P(self.cnt_m), P(self.job_code), P(self.job_A), P(self.coeff26),
-                                          P(self.beta_int), P(self.nl_pt), P(self.nl_w), st),
-            "dips_geometry_assemble_nl",
+                                          P(self.beta_int), P(self.nl_pt), P(self.nl_w), P(scratch), scratch.numel(),
+                                          st),
+            "dips_geometry_assemble_ex",
         )
         mark("assemble")
         self.flags = flags if keep_geometry else None
