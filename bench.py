@@ -67,6 +67,9 @@ def parse():
     ap.add_argument("--tta-sweep", action="store_true",
                     help="time to target over minibatch sizes 2^14..2^18 x learning rates 3e-3, 1e-2, 3e-2 and "
                          "L-BFGS, instead of the default three configurations")
+    ap.add_argument("--tta-sweep-fast", action="store_true",
+                    help="time to target at the small batches 2^14, 2^15 and 2^16 over learning rates 3e-2, 5e-2 "
+                         "and 8e-2 and decay rates 0.7, 0.5, 0.3")
     ap.add_argument("--no-tta", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--problem", default="sphere", choices=["sphere", "star", "blob", "lpbe"],
@@ -733,6 +736,9 @@ TTA_SWEEP = tuple(("adam", b, lr, 0.9) for b in (1 << 14, 1 << 15, 1 << 16, 1 <<
 # 1000 steps) around the fastest configuration
 TTA_SWEEP_DECAY = tuple(("adam", b, lr, d) for b in (1 << 16, 1 << 17) for lr in (1e-2, 2e-2, 3e-2)
                         for d in (0.9, 0.7, 0.5, 0.25))
+# smaller batches (cheaper steps) at larger learning rates
+TTA_SWEEP_FAST = tuple(("adam", b, lr, d) for b in (1 << 14, 1 << 15, 1 << 16) for lr in (3e-2, 5e-2, 8e-2)
+                       for d in (0.7, 0.5, 0.3))
 
 
 def run_krylov(args, rank, world):
@@ -827,7 +833,8 @@ def time_to_target(args, lvl, g, pr, arch, dev):
         return float((u - ex).abs().max()) / exmax
 
     runs = []
-    plan = TTA_SWEEP if args.tta_sweep else (TTA_SWEEP_DECAY if args.tta_sweep_decay else TTA_RUNS)
+    plan = (TTA_SWEEP if args.tta_sweep else TTA_SWEEP_DECAY if args.tta_sweep_decay
+            else TTA_SWEEP_FAST if args.tta_sweep_fast else TTA_RUNS)
     for opt, B, lr, decay in plan:
         if opt == "adam":
             runs.append(_nbm_adam_run(lvl, arch, dev, B, lr, args.tta_seconds, target, rel_err, decay))
