@@ -160,6 +160,13 @@ int dips_geometry_classify(const dips_levelset_t* ls, const float* pts, int64_t 
 int dips_geometry_queries(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
                           const uint32_t* flags, const int64_t* tri_off, const int64_t* xs_off,
                           float* tri_pts, float* xs_pts, float* xr_pts, cudaStream_t stream);
+/* dips_geometry_queries that lists the points with queries (those with an interface stencil
+   point) in scratch (dips_geometry_assemble_scratch_bytes(n) bytes, 4-byte aligned, device
+   memory) and runs them 32 to a warp; NULL scratch: one pass over every point.  Same outputs. */
+int dips_geometry_queries_ex(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
+                             const uint32_t* flags, const int64_t* tri_off, const int64_t* xs_off,
+                             float* tri_pts, float* xs_pts, float* xr_pts, void* scratch, size_t scratch_bytes,
+                             cudaStream_t stream);
 /* Pass 3: the per-point residual records.  job_off ([n+1]) is the exclusive prefix sum of
    job_cap; cnt[i] <= job_cap[i] jobs are written (u- jobs from the front of the point's
    range, u+ jobs from its back).  coeff26

@@ -686,13 +686,50 @@ __global__ void k_classify(LevelSet L0, const float* __restrict__ pts, int64_t n
   }
 }
 
+// Passes of k_assemble: every point in one pass (kAllPoints), or two passes that keep the heavy
+// points together: kDeferHeavy does the points without an interface stencil point and lists
+// the others; kListed does the listed points.  A point with interface stencil points costs
+// about a hundred times a bulk point (regression, five-tetrahedron clipping) and such points come
+// a few to a warp of 32 consecutive points, so in one pass most of a warp idles while its heavy
+// lanes run; listed, 32 heavy points share a warp.
+enum AssemblePass { kAllPoints = 0, kDeferHeavy = 1, kListed = 2 };
+
+__device__ __forceinline__ bool heavy_point(uint32_t f) {
+  bool x = false;
+#pragma unroll
+  for (int j = 0; j < kStencil; ++j) x |= dec_crossed(f, kFlagCrossedS + 2 * j) == 0;
+  return x;
+}
+
+// The points with an interface stencil point (the only ones with queries or regression work),
+// listed so that a pass over them runs 32 of them to a warp
+__global__ void k_heavy_list(const uint32_t* __restrict__ flags, int64_t n, int32_t* __restrict__ list,
+                             int32_t* __restrict__ count) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const bool heavy = heavy_point(flags[i]);
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, heavy);
+    if (!m) continue;
+    const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(act, base, leader);
+    if (heavy) list[base + __popc(m & ((1u << lane) - 1))] = (int32_t)i;
+  }
+}
+
+// the queries of every point (LISTED = false) or of the listed points (the others have none)
+template <bool LISTED>
 __global__ void k_queries(LevelSet L0, const float* __restrict__ pts, int64_t n, H3 hh, const uint32_t* __restrict__ flags,
                           const int64_t* __restrict__ tri_off, const int64_t* __restrict__ xs_off, float* __restrict__ tri_pts,
-                          float* __restrict__ xs_pts, float* __restrict__ xr_pts) {
+                          float* __restrict__ xs_pts, float* __restrict__ xr_pts, const int32_t* __restrict__ list,
+                          const int32_t* __restrict__ count) {
   LevelSet L = L0;
   levelset_init(L);
   const float* h = hh.v;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t end = LISTED ? (int64_t)*count : n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < end; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = LISTED ? (int64_t)list[t] : t;
     const uint32_t f = flags[i];
     float p[3];
     load_point(pts, i, p);
@@ -736,21 +773,6 @@ __device__ __forceinline__ float tsample(const float* a, int64_t i) { return a ?
 // geometry is the same in both modes and the branches (which phase is extrapolated, which cube
 // vertices have a weight) are the records' own, so the tangent is the exact derivative of the
 // records as a function of the coefficients.
-// Passes of k_assemble: every point in one pass (kAllPoints), or two passes that keep the heavy
-// points together: kDeferHeavy does the points without an interface stencil point and lists
-// the others; kListed does the listed points.  A point with interface stencil points costs
-// about a hundred times a bulk point (regression, five-tetrahedron clipping) and such points come
-// a few to a warp of 32 consecutive points, so in one pass most of a warp idles while its heavy
-// lanes run; listed, 32 heavy points share a warp.
-enum AssemblePass { kAllPoints = 0, kDeferHeavy = 1, kListed = 2 };
-
-__device__ __forceinline__ bool heavy_point(uint32_t f) {
-  bool x = false;
-#pragma unroll
-  for (int j = 0; j < kStencil; ++j) x |= dec_crossed(f, kFlagCrossedS + 2 * j) == 0;
-  return x;
-}
-
 template <bool TAN, int PASS = kAllPoints>
 __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n, H3 hh, const uint32_t* __restrict__ flags,
                            const int64_t* __restrict__ tri_off, const int64_t* __restrict__ xs_off,
@@ -1131,14 +1153,35 @@ extern "C" int dips_geometry_classify(const dips_levelset_t* ls, const float* pt
 extern "C" int dips_geometry_queries(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
                                      const uint32_t* flags, const int64_t* tri_off, const int64_t* xs_off,
                                      float* tri_pts, float* xs_pts, float* xr_pts, cudaStream_t stream) {
+  return dips_geometry_queries_ex(ls, pts, n, h, flags, tri_off, xs_off, tri_pts, xs_pts, xr_pts, nullptr, 0, stream);
+}
+
+extern "C" int dips_geometry_queries_ex(const dips_levelset_t* ls, const float* pts, int64_t n, const float h[3],
+                                        const uint32_t* flags, const int64_t* tri_off, const int64_t* xs_off,
+                                        float* tri_pts, float* xs_pts, float* xr_pts, void* scratch,
+                                        size_t scratch_bytes, cudaStream_t stream) {
   DIPS_REQUIRE(n >= 0 && h, DIPS_E_ARG, "dips_geometry_queries: bad n or h");
   if (n == 0) return DIPS_OK;
   DIPS_REQUIRE(pts && flags && tri_off && xs_off, DIPS_E_ARG, "dips_geometry_queries: null pointer");
   LevelSet L;
   int st = make_ls(ls, &L, stream);
   if (st) return st;
-  k_queries<<<grid_for(n, 128), 128, 0, stream>>>(L, pts, n, make_h(h), flags, tri_off, xs_off, tri_pts, xs_pts, xr_pts);
-  DIPS_CHECK_LAUNCH("dips_geometry_queries");
+  if (!scratch) {
+    k_queries<false><<<grid_for(n, 128), 128, 0, stream>>>(L, pts, n, make_h(h), flags, tri_off, xs_off, tri_pts,
+                                                           xs_pts, xr_pts, nullptr, nullptr);
+    DIPS_CHECK_LAUNCH("dips_geometry_queries");
+    return DIPS_OK;
+  }
+  DIPS_REQUIRE(scratch_bytes >= dips_geometry_assemble_scratch_bytes(n) && ((uintptr_t)scratch & 3) == 0,
+               DIPS_E_WORKSPACE, "dips_geometry_queries_ex: scratch too small or misaligned");
+  int32_t* count = static_cast<int32_t*>(scratch);
+  int32_t* list = count + 1;
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int32_t), stream);
+  if (e != cudaSuccess) return cuda_status(e, "dips_geometry_queries_ex: scratch counter");
+  k_heavy_list<<<grid_for(n, 256), 256, 0, stream>>>(flags, n, list, count);
+  k_queries<true><<<grid_for(n, 128), 128, 0, stream>>>(L, pts, n, make_h(h), flags, tri_off, xs_off, tri_pts, xs_pts,
+                                                        xr_pts, list, count);
+  DIPS_CHECK_LAUNCH("dips_geometry_queries_ex");
   return DIPS_OK;
 }
 

@@ -236,6 +236,11 @@ _SIGS = {
         [P(LevelSetT), c_void_p, c_i64, P(c_f32), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
          c_void_p],
     ),
+    "dips_geometry_queries_ex": (
+        c_i32,
+        [P(LevelSetT), c_void_p, c_i64, P(c_f32), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+         c_void_p, ctypes.c_size_t, c_void_p],
+    ),
     "dips_geometry_assemble": (
         c_i32,
         [P(LevelSetT), c_void_p, c_i64, P(c_f32), c_void_p, c_void_p, c_void_p, c_void_p, P(CoeffsT)]

@@ -6,10 +6,10 @@ for every point at every step (solvers/poisson/discretization.py:299-519).  Here
 is computed once per (point, h) by the geometry kernels:
 
 1. ``dips_geometry_classify``  flags and counts per point
-2. ``dips_geometry_queries``   the points where coefficient callables are needed
+2. ``dips_geometry_queries_ex``   the points where coefficient callables are needed
    (interface-triangle vertices, crossed stencil points, their projections r = s - phi n)
 3. the host evaluates the user's coefficient callables at those points (torch, on the GPU)
-4. ``dips_geometry_assemble``  the residual of each point as an affine function of the
+4. ``dips_geometry_assemble_ex``  the residual of each point as an affine function of the
    network values at its jobs: r = nan_to_num((lhs0 + sum_j A_j u(x_j)) / diag) - rod
 """
 
@@ -89,10 +89,13 @@ class FVLevel:
         tri_pts = torch.empty(max(3 * n_tri_tot, 1), 3, **f32)
         xs_pts = torch.empty(max(n_xs_tot, 1), 3, **f32)
         xr_pts = torch.empty(max(n_xs_tot, 1), 3, **f32)
+        # the points next to the interface are listed in scratch and run together (queries, and the
+        # second launch of the assembly)
+        scratch = torch.empty(max(int(lib.dips_geometry_assemble_scratch_bytes(n)), 4), dtype=torch.uint8, device=dev)
         _lib.check(
-            lib.dips_geometry_queries(ls.desc, P(self.pts), n, hc, P(flags), P(tri_off), P(xs_off), P(tri_pts),
-                                      P(xs_pts), P(xr_pts), st),
-            "dips_geometry_queries",
+            lib.dips_geometry_queries_ex(ls.desc, P(self.pts), n, hc, P(flags), P(tri_off), P(xs_off), P(tri_pts),
+                                         P(xs_pts), P(xr_pts), P(scratch), scratch.numel(), st),
+            "dips_geometry_queries_ex",
         )
         tri_pts = tri_pts[: 3 * n_tri_tot]
         xs_pts = xs_pts[:n_xs_tot]
@@ -144,8 +147,6 @@ class FVLevel:
         has_nl = not (nonlinear.is_zero(self.nl[0]) and nonlinear.is_zero(self.nl[1]))
         self.nl_pt = torch.empty(max(n, 1), 4, **f32) if has_nl else None
         self.nl_w = torch.zeros(max(self.n_jobs_cap, 1), 2, **f32) if has_nl else None
-        # the points next to the interface are listed and assembled together (second launch)
-        scratch = torch.empty(max(int(lib.dips_geometry_assemble_scratch_bytes(n)), 4), dtype=torch.uint8, device=dev)
         _lib.check(
             lib.dips_geometry_assemble_ex(ls.desc, P(self.pts), n, hc, P(flags), P(tri_off), P(xs_off),
                                           P(self.job_off), co, P(self.lhs0), P(self.diag), P(self.rod), P(self.cnt),

@@ -64,3 +64,24 @@ def test_two_pass_assembly_matches_one_pass(name, level, nl):
     for j in range(7):
         heavy |= ((f >> (4 + 2 * j)) & 3) == 1
     assert 0 < heavy.sum() < n // 2
+
+
+@pytest.mark.parametrize("name,level", [("sphere", 0), ("star", 1)])
+def test_listed_queries_match_one_pass(name, level):
+    from dips_gb300 import _lib
+
+    case = _parity.Case(name, 24, (1, 1, 2, 10), level=level, fns=_parity.make_problem(name))
+    lvl = case.gpu_level()  # queries of the listed points (scratch given)
+    lib = _lib.load()
+    P = _lib.ptr
+    tri_off, xs_off, tri_pts, xs_pts, xr_pts, _, _ = lvl._geo
+    a = [torch.full((max(t.shape[0], 1), 3), float("nan"), dtype=torch.float32, device="cuda")
+         for t in (tri_pts, xs_pts, xr_pts)]
+    st = lib.dips_geometry_queries(lvl.ls.desc, P(lvl.pts), lvl.n, lvl._hc(), P(lvl.flags), P(tri_off), P(xs_off),
+                                   P(a[0]), P(a[1]), P(a[2]), _lib.stream_handle())
+    assert st == 0, lib.dips_last_error()
+    torch.cuda.synchronize()
+    for got, ref in zip((tri_pts, xs_pts, xr_pts), a):
+        k = got.shape[0]
+        assert k > 0
+        np.testing.assert_array_equal(got.cpu().numpy().view(np.uint32), ref[:k].cpu().numpy().view(np.uint32))
