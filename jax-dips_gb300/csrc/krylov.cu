@@ -27,7 +27,7 @@ namespace dips {
 
 constexpr int kKThreads = 256;
 constexpr int kKGrid = 152 * 8;
-constexpr int kGenGrid = 152 * 8;  // blocks of the general-row kernels (8 warps each, a warp per row)
+constexpr int kGenGrid = 152 * 8;  // blocks of the initial residual's general rows (8 warps each, a warp per row)
 
 struct Grid3 {
   int nx, ny, nz;
@@ -340,15 +340,16 @@ struct KVecs {
   double* sums;      // [3][3] the grid's sums of those reductions
   float* err_part;  // [kKGrid] max |x - u_exact|
   float4* coef;     // [n][2] bulk rows: A_0..A_6 (stencil order) and diag, packed once per solve
-  uint8_t* gen;     // [n] 1 for a general row (warp path), 0 for a bulk row
+  uint8_t* gen;     // [n] 1 for a general row (listed in grows), 0 for a bulk row
 };
 
 
 // The general rows (those without a packed bulk record) are listed once per solve, in bins:
 // bin 0 holds the rows of at most kLightJobs jobs (a thread each in the cooperative product),
-// bin b >= 1 the rows that take b rounds of 32 jobs (a warp each).  The list holds bin 0, then
-// the bins of the most rounds first, so that warps striding over the heavy rows get similar
-// mixes.  counts[0, kRowBins) are the bins' sizes, counts[kRowBins, 2 kRowBins) scatter cursors.
+// bin b >= 1 the rows that take b rounds of 32 jobs (a group of kGroup lanes each).  The list
+// holds bin 0, then the bins of the most rounds first, so that the groups striding over the heavy
+// rows get similar mixes.  counts[0, kRowBins) are the bins' sizes, counts[kRowBins, 2 kRowBins)
+// scatter cursors.
 // The order within a bin depends on the warps' arrival; each row's value does not.
 constexpr int kRowBins = 16;  // rows of up to 15 x 32 jobs
 
@@ -920,7 +921,7 @@ extern "C" int dips_bicgstab(const dips_records_t* rec, int32_t nx, int32_t ny, 
   k_general_rows<<<G, T, 0, stream>>>(*rec, g, V.grows, V.gcount);
   if (rec->bulk_rec) {
     k_krylov_pack<<<G, T, 0, stream>>>(*rec, V.coef, V.gen);
-  } else {  // no packed records: every row takes the warp path
+  } else {  // no packed records: every row is a general row
     cudaError_t eg = cudaMemsetAsync(V.gen, 1, n, stream);
     if (eg != cudaSuccess) return cuda_status(eg, "bicgstab row kinds");
   }
