@@ -251,24 +251,29 @@ __device__ __forceinline__ void sync_for_mma() {
 }
 
 // one hidden-hidden forward layer: D = A(TMEM) x WF[l]
+// The descriptors of consecutive K steps differ only in the start-address field (bits 0-13,
+// the byte address >> 4).  Shared-memory addresses stay below 2^18 bytes, so adding the step
+// there cannot carry into the other fields: each group builds one descriptor per operand and
+// adds, and the issuing thread (alone while the CTA waits) runs a few instructions per MMA.
 __device__ __forceinline__ void issue_fwd(uint32_t tb, const unsigned char* wf_l) {
+  const uint64_t b0 = sdesc(saddr(wf_l), 128, 2048);
 #pragma unroll
-  for (int s = 0; s < W / 8; ++s)
-    mma_ts(tb + cD, tb + cA + 8 * s, sdesc(saddr(wf_l) + s * 256, 128, 2048), idesc(128, W), s > 0);
+  for (int s = 0; s < W / 8; ++s) mma_ts(tb + cD, tb + cA + 8 * s, b0 + (uint64_t)(16 * s), idesc(128, W), s > 0);
 }
 // delta GEMM: D = A(TMEM, delta_l job-major) x WB[l]   (W_l delta_l per job)
 __device__ __forceinline__ void issue_delta(uint32_t tb, const unsigned char* wb_l) {
+  const uint64_t b0 = sdesc(saddr(wb_l), 128, 2048);
 #pragma unroll
-  for (int s = 0; s < W / 8; ++s)
-    mma_ts(tb + cD, tb + cA + 8 * s, sdesc(saddr(wb_l) + s * 256, 128, 2048), idesc(128, W), s > 0);
+  for (int s = 0; s < W / 8; ++s) mma_ts(tb + cD, tb + cA + 8 * s, b0 + (uint64_t)(16 * s), idesc(128, W), s > 0);
 }
 // weight gradient: acc (M = 64 out features, N) += A (feature-major, a_rows rows) x B^T (feature-major, N rows)
 __device__ __forceinline__ void issue_dw(uint32_t d, const unsigned char* a, uint32_t a_sbo, const unsigned char* b, int N,
                                          bool accumulate) {
+  const uint64_t a0 = sdesc(saddr(a), kLboJ, a_sbo), b0 = sdesc(saddr(b), kLboJ, kSboJ);
+  constexpr uint64_t kStep = (2 * kLboJ) >> 4;  // two K-chunks of the 144-byte stride per K = 8 step
 #pragma unroll
   for (int s = 0; s < kTile / 8; ++s)
-    mma_ss(d, sdesc(saddr(a) + s * 2 * kLboJ, kLboJ, a_sbo), sdesc(saddr(b) + s * 2 * kLboJ, kLboJ, kSboJ), idesc(64, N),
-           (accumulate || s > 0) ? 1u : 0u);
+    mma_ss(d, a0 + kStep * s, b0 + kStep * s, idesc(64, N), (accumulate || s > 0) ? 1u : 0u);
 }
 
 // ---- forward kernel -------------------------------------------------------------------------
