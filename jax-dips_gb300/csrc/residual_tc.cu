@@ -483,25 +483,26 @@ __global__ void __launch_bounds__(kAdjThreads, 1) k_tc_adjoint(const float* __re
 #pragma unroll
     for (int o = 0; o < kAQ; ++o) h[o] = tanh_f(h[o] + small[4 * W + f0 + o]);
     to_tmem<kAQ>(lb, cA + f0, h);
-    to_fm<kAQ>(H2, job, h, f0);
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
       issue_fwd(tb, wf + kWBytes);
       commit(bar);
     }
+    // h2^T for dW3 while the layer-3 MMA runs (its last reader, the previous tile's dW3, is done)
+    to_fm<kAQ>(H2, job, h, f0);
     wait();
     from_tmem<kAQ>(lb, cD + f0, h);
 #pragma unroll
     for (int o = 0; o < kAQ; ++o) h[o] = tanh_f(h[o] + small[5 * W + f0 + o]);
     to_tmem<kAQ>(lb, cA + f0, h);
-    to_fm<kAQ>(H3, job, h, f0);
     sync_for_mma();
     if (s_abort) break;
     if (t == 0) {
       issue_fwd(tb, wf + 2 * kWBytes);
       commit(bar);
     }
+    to_fm<kAQ>(H3, job, h, f0);  // h3^T for dW4, likewise under the layer-4 MMA
     wait();
     from_tmem<kAQ>(lb, cD + f0, h);
 #pragma unroll
