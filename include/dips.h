@@ -93,8 +93,9 @@ typedef struct {
                                NULL: gathered from the arrays above every step */
   /* Optional nonlinear operators (trainer.py:992-1017; the residual adds
      N-(u-) V- + N+(u+) V+ at an interior point, discretization.py:369).  NULL nl_pt: none.
-     With them every point takes the general path (no bulk points), and the plain method and the
-     coefficient derivative refuse the records (DIPS_E_ARG). */
+     With them every point takes the general path (no bulk points); the plain method refuses the
+     records (DIPS_E_ARG), the coefficient derivative and the batched instance step
+     (dips_instances_prepare) too (DIPS_E_UNSUPPORTED). */
   const float* nl_pt;       /* [n][4] K-, K+, V-, V+ (dips_geometry_assemble_ex): u-/+ at the point
                                = K-/+ + sum over its jobs of the job's weight times its value */
   const float* nl_w;        /* [jobs][2] the job's weights in u- and u+ at the point */

@@ -400,6 +400,7 @@ __device__ __forceinline__ void nl_eval(int kind, float c, float u, float& f, fl
   }
 }
 
+template <bool NL>
 __device__ __forceinline__ void residual_body(const int32_t* __restrict__ ids, int64_t B, const dips_records_t& rec,
                                               const Workspace& w, float* __restrict__ residual_out, int bx) {
   const int64_t b = bx * (int64_t)blockDim.x + threadIdx.x;
@@ -414,7 +415,7 @@ __device__ __forceinline__ void residual_body(const int32_t* __restrict__ ids, i
   int64_t om = 0, op = 0;
   int cm = 0, n = 0;
   float lhs0 = 0.0f, diag = 1.0f, rod = 0.0f, Pv = 1.0f;
-  const bool nl = rec.nl_pt != nullptr;
+  constexpr bool nl = NL;  // (the records then carry nl_pt and nl_w; the launch checks it)
   float4 nlp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   int64_t ro0 = 0, rop = 0;  // the point's jobs in the records (for their nonlinear weights)
   if (kind == 0) {
@@ -520,15 +521,16 @@ __device__ __forceinline__ void residual_body(const int32_t* __restrict__ ids, i
   if (threadIdx.x == 0) w.lossp[bx] = t;
 }
 
+template <bool NL>
 __global__ void k_residual(const int32_t* __restrict__ ids, int64_t B, const __grid_constant__ dips_records_t rec,
                            const __grid_constant__ Workspace w, float* __restrict__ residual_out) {
-  residual_body(ids, B, rec, w, residual_out, blockIdx.x);
+  residual_body<NL>(ids, B, rec, w, residual_out, blockIdx.x);
 }
 
 __global__ void k_residual_multi(const Inst* __restrict__ T) {
   const Inst& I = T[blockIdx.y];
   if ((int64_t)blockIdx.x >= I.w.nres) return;
-  residual_body(I.ids, I.B, I.rec, I.w, nullptr, blockIdx.x);
+  residual_body<false>(I.ids, I.B, I.rec, I.w, nullptr, blockIdx.x);  // instances have no nonlinear operators
 }
 
 __global__ void k_loss_final(Workspace w, int64_t B, double* __restrict__ loss_out) {
@@ -926,7 +928,10 @@ static int run_forward(const ArchOps* ops, const dips_arch_t* arch, const float*
   }
   st = ops->job_forward(make_ph(rec), ids, W, mk, s);
   if (st) return st;
-  k_residual<<<(int)W.nres, 256, 0, s>>>(ids, B, *rec, W, residual_out);
+  if (rec->nl_pt)  // the nonlinear operators' variant (more registers) only where they are given
+    k_residual<true><<<(int)W.nres, 256, 0, s>>>(ids, B, *rec, W, residual_out);
+  else
+    k_residual<false><<<(int)W.nres, 256, 0, s>>>(ids, B, *rec, W, residual_out);
   DIPS_CHECK_LAUNCH("residual");
   mark(mk, kMarkResidual, s);
   st = ops->bulk_fused(make_ph(rec), ids, W, *rec, residual_out, fused_bwd, mk, s);
@@ -1158,6 +1163,8 @@ extern "C" int dips_instances_prepare(const dips_arch_t* arch, const dips_instan
     if (st) return st;
     DIPS_REQUIRE(d.params && d.mu && d.nu && d.count && d.batch_ids, DIPS_E_ARG,
                  "dips_instances_prepare: instance %d: null pointer", i);
+    DIPS_REQUIRE(!d.rec->nl_pt, DIPS_E_UNSUPPORTED,
+                 "dips_instances_prepare: instance %d: nonlinear operators take the single-instance step", i);
     DIPS_REQUIRE(d.ids_mode >= -1 && d.ids_mode <= 1, DIPS_E_ARG, "dips_instances_prepare: instance %d: ids_mode", i);
     if (d.ids_mode >= 0)
       DIPS_REQUIRE(d.n_batches > 0 && d.n_batches * d.batch <= d.rec->n_pts && d.rec->n_pts <= 0x7fffffff, DIPS_E_ARG,

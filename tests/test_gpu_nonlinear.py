@@ -15,6 +15,8 @@ through four layers), which the large operator (300 sinh u) amplifies: 1e-3 and 
 the term out moves the gradient by 0.3-6 % of its norm.
 """
 
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -78,3 +80,27 @@ def test_nonlinear_records_refuse_the_linear_only_entry_points():
     # the library is still usable
     lg, _ = case.gpu_loss_grad()
     assert np.isfinite(lg)
+
+
+def test_batched_instance_step_refuses_nonlinear_records():
+    from dips_gb300 import _lib, ops
+
+    case = _sinh_case((2, 16, 2, 16))
+    lvl = case.gpu_level()
+    arch = case.gpu_arch()
+    params = torch.as_tensor(case.params, device="cuda")
+    B = 256
+    opt = ops.AdamState(params.numel(), lr=1e-3)
+    ws = ops.StepWorkspace(arch, B, lvl.max_jobs(B), torch.device("cuda"))
+    ids = torch.arange(B, dtype=torch.int32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    arr = (_lib.InstanceT * 1)()
+    arr[0] = _lib.InstanceT(ctypes.addressof(lvl.desc), _lib.ptr(ids), B, 0, 0, -1, _lib.ptr(params),
+                            _lib.ptr(opt.mu), _lib.ptr(opt.nu), _lib.ptr(opt.count), _lib.ptr(ws.buf), ws.nbytes,
+                            _lib.ptr(loss), None)
+    lib = _lib.load()
+    nbytes = int(lib.dips_instances_table_bytes(1))
+    table = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    st = lib.dips_instances_prepare(arch.ctype(), arr, 1, _lib.ptr(table), nbytes, _lib.stream_handle())
+    assert st != 0
+    assert "nonlinear" in lib.dips_last_error().decode()
