@@ -117,3 +117,27 @@ def test_fv_residual_against_the_references_residual_vector(key):
         assert float(err[~low].max()) <= 3e-5 * scale, (ukey, float(err[~low].max()), scale)
         bad = err > 3e-5 * scale
         assert not (bad & ~low).any()
+
+
+def test_bicgstab_without_packed_records_and_on_a_larger_grid():
+    """Every row through the general-row path (no packed bulk records: the bulk rows become light
+    rows of 7 jobs) gives the solution of the packed solve, on a 40^3 grid whose general rows fill
+    several job-count bins."""
+    from dips_gb300 import krylov, problems
+
+    n = 40
+    case = _parity.build_case("sphere", n=n)
+    lvl = case.gpu_level()
+    ex = torch.as_tensor(problems.exact_solution(case.fns, case.grid.R), device="cuda")
+    a = krylov.bicgstab(lvl, (n, n, n), u_exact=ex, max_iter=3000, rtol=1e-6, check_every=10)
+    saved = lvl.desc.bulk_rec
+    try:
+        lvl.desc.bulk_rec = None
+        b = krylov.bicgstab(lvl, (n, n, n), u_exact=ex, max_iter=3000, rtol=1e-6, check_every=10)
+    finally:
+        lvl.desc.bulk_rec = saved
+    for r in (a, b):
+        assert not r.breakdown and r.rel_residual <= 1e-6
+    xa, xb = a.x.cpu().numpy(), b.x.cpu().numpy()
+    assert np.abs(xa - xb).max() <= 1e-4 * np.abs(xa).max()
+    assert abs(a.rel_linf - b.rel_linf) <= 1e-3
