@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(kAdjThreads, 1) k_tc_adjoint(const float* __re
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const bool bulk = tile < nbt;
     float x[3] = {0.0f, 0.0f, 0.0f};
-    float g = 0.0f, A = 0.0f;
+    float g = 0.0f;
     const int pl = job / kStencil, sj = job - kStencil * pl;  // bulk tile: point and stencil point
     const int64_t pidx = tile * kBulkPts + pl;
     const bool bvalid = bulk && job < kBulkPts * kStencil && pidx < nb;
@@ -456,7 +456,6 @@ __global__ void __launch_bounds__(kAdjThreads, 1) k_tc_adjoint(const float* __re
         const float* r = recs + pidx * kRecFloats;
         const float p[3] = {r[kRecP], r[kRecP + 1], r[kRecP + 2]};
         stencil_point(p, hh, sj, x);
-        A = r[kRecA + sj];
       }
     } else {
       const int64_t j = jbeg + (tile - nbt) * kTile + job;
@@ -512,17 +511,22 @@ __global__ void __launch_bounds__(kAdjThreads, 1) k_tc_adjoint(const float* __re
       float u = 0.0f;
 #pragma unroll
       for (int o = 0; o < kAQ; ++o) u = fmaf(small[7 * W + f0 + o], h[o], u);
+      if (part == 0) s_au[job] = u;
       if (part == 1) s_part[0][job] = u;
       if (part == 2) s_part[1][job] = u;
       if (part == 3) s_part3[job] = u;
       __syncthreads();
-      if (!part) s_au[job] = A * (((u + s_part[0][job]) + (s_part[1][job] + s_part3[job])) + small[8 * W]);
-      __syncthreads();
       if (t < kBulkPts) {
         if (rvalid) {
+          // u of the point's 7 jobs from the four partial sums, then lhs0 + sum A_j u_j (each
+          // product rounded before it is added)
           float lhs = r_lhs0;
 #pragma unroll
-          for (int k = 0; k < kStencil; ++k) lhs += s_au[kStencil * t + k];
+          for (int k = 0; k < kStencil; ++k) {
+            const int jj = kStencil * t + k;
+            const float uj = ((s_au[jj] + s_part[0][jj]) + (s_part[1][jj] + s_part3[jj])) + small[8 * W];
+            lhs += __fmul_rn(r_A[k], uj);
+          }
           const float qv = lhs / r_diag;
           const float r0 = nan_to_num(qv) - r_rod;
           const float rr = r_P * r0;  // learned preconditioner (1 without it)
