@@ -541,12 +541,15 @@ __global__ void __launch_bounds__(kAdjThreads, 1) k_tc_adjoint(const float* __re
           for (int k = 0; k < kStencil; ++k) s_g[kStencil * t + k] = 0.0f;
         }
       }
+      // h4^T for dWo while warp 0 forms the residuals (Z's last reader, the previous tile's dW1,
+      // is done)
+      if (BWD) to_fm<kAQ>(Z, job, h, f0);
       __syncthreads();
       g = bvalid ? s_g[job] : 0.0f;
     }
     if (!BWD) continue;
     // ---- output layer: dWo, dbo = sum_j g_j [h4, 1]  (A = [g] replicated, B = h4^T with its ones row)
-    to_fm<kAQ>(Z, job, h, f0);
+    if (!bulk) to_fm<kAQ>(Z, job, h, f0);
     if (!f0) {
       *reinterpret_cast<float*>(GX + foff(0, job)) = tf32(g);
       *reinterpret_cast<float*>(GX + foff(1, job)) = 0.0f;
