@@ -656,7 +656,7 @@ __global__ void k_classify(LevelSet L0, const float* __restrict__ pts, int64_t n
     float p[3];
     load_point(pts, i, p);
     const bool bnd = is_box_boundary(L, p, h);
-    uint32_t f = bnd ? 1u : 0u;
+    uint32_t f = (bnd ? 1u : 0u) << kFlagBnd;
     int nx = 0;
     for (int j = 0; j < kStencil; ++j) {
       float s[3];
@@ -745,7 +745,7 @@ __global__ void k_queries(LevelSet L0, const float* __restrict__ pts, int64_t n,
             for (int a = 0; a < 3; ++a) tri_pts[3 * o + a] = tri[q][v][a];
       }
     }
-    if (f & 1u) continue;  // box-boundary points have no stencil queries
+    if ((f >> kFlagBnd) & 1u) continue;  // box-boundary points have no stencil queries
     int64_t ox = xs_off[i];
     for (int j = 0; j < kStencil; ++j) {
       if (dec_crossed(f, kFlagCrossedS + 2 * j) != 0) continue;
@@ -888,7 +888,7 @@ __global__ void k_assemble(LevelSet L0, const float* __restrict__ pts, int64_t n
       for (int q = 0; q < 26; ++q) coeff26_out[26 * i + q] = c26[q];
     if (!TAN && beta_int_out) beta_int_out[i] = bint;
 
-    if (f & 1u) {  // box boundary: lhs = u*V, rhs = g*V (discretization.py:389-393, :410-411)
+    if ((f >> kFlagBnd) & 1u) {  // box boundary: lhs = u*V, rhs = g*V (discretization.py:389-393, :410-411)
       const bool net = (f >> kFlagNetS) & 1u;
       emit(0, kCubeCentre, net, TAN ? 0.0f : V);
       lhs0_out[i] = 0.0f;
