@@ -644,7 +644,8 @@ __device__ __forceinline__ void coop_apply(const dips_records_t& rec, const Grid
   const int64_t rounds = (gheavy + gstride - 1) / gstride;  // the same for every lane of the grid
   // A group past the last row computes row 0 again and drops it.  The next row's header and the
   // row's own follow-up operand ((rhat)_i or s_i) load while its jobs are read.
-  GenRow r = load_row(V.grows, glight + (w0 < gheavy ? w0 : 0));
+  GenRow r = {};
+  if (rounds > 0) r = load_row(V.grows, glight + (w0 < gheavy ? w0 : 0));  // (no heavy rows: nothing listed)
   for (int64_t t = 0; t < rounds; ++t) {
     const int64_t w = w0 + t * gstride, wn = w + gstride;
     const GenRow rn = load_row(V.grows, glight + (wn < gheavy ? wn : 0));
