@@ -117,11 +117,25 @@ typedef struct {
   float pre_scaling;
 } dips_arch_t;
 
-/* optax chain: clip_by_global_norm -> scale_by_adam -> scale_by_schedule(exponential_decay)
-   -> scale(-1) (solvers/optimizers.py:33-54). */
+/* The optimizers of get_optimizer (solvers/optimizers.py:13-97).
+   kind DIPS_OPT_ADAM: clip_by_global_norm(max_norm) -> scale_by_adam(b1, b2, eps) ->
+     scale_by_schedule -> scale(-1) (chained_adam, :33-54; optax.adam is max_norm = inf and a
+     constant rate, decay_rate = 1);
+   kind DIPS_OPT_RMSPROP: optax.rmsprop (:82-87): nu = (1 - b2) g^2 + b2 nu (b2 = the rms decay,
+     0.9), update -rate g / sqrt(nu + eps), with max_norm clipping if finite; mu is not used.
+   schedule DIPS_SCHED_EXPONENTIAL: rate = lr decay_rate^(count / transition_steps);
+   DIPS_SCHED_POLYNOMIAL: rate = lr (1 - min(count, transition_steps) / transition_steps)
+     (optax.polynomial_schedule with end value 0 and power 1, :25-28).
+   A struct with kind and schedule zero is the chained Adam with the exponential schedule. */
 typedef struct {
   float lr, decay_rate, transition_steps, max_norm, b1, b2, eps;
+  int32_t kind, schedule;
 } dips_adam_t;
+
+#define DIPS_OPT_ADAM 0
+#define DIPS_OPT_RMSPROP 1
+#define DIPS_SCHED_EXPONENTIAL 0
+#define DIPS_SCHED_POLYNOMIAL 1
 
 /* ---- errors ------------------------------------------------------------------------- */
 /* Text of the last failure on this thread (static storage; never NULL). */

@@ -618,7 +618,8 @@ __global__ void k_coeff_final(Workspace w, double* __restrict__ out) {
 
 // The optax chain (clip_by_global_norm, scale_by_adam, exponential-decay schedule, scale by
 // -1; solvers/optimizers.py:33-54) over P parameters by one block, given the squared gradient
-// norm.  Thread 0 increments the step counter.
+// norm; or optax.rmsprop, or the polynomial schedule (dips_adam_t).  Thread 0 increments the
+// step counter.
 __device__ void adam_update(const dips_adam_t& hp, int P, float gsq, float* __restrict__ params,
                             const float* __restrict__ grad, float* __restrict__ mu, float* __restrict__ nu,
                             int64_t* __restrict__ count) {
@@ -632,7 +633,23 @@ __device__ void adam_update(const dips_adam_t& hp, int P, float gsq, float* __re
   const float cnt1 = (float)(cnt0 + 1);
   const float bc1 = 1.0f - powf(hp.b1, cnt1);
   const float bc2 = 1.0f - powf(hp.b2, cnt1);
-  const float step = hp.lr * powf(hp.decay_rate, (float)cnt0 / hp.transition_steps);
+  float step;
+  if (hp.schedule == DIPS_SCHED_POLYNOMIAL)
+    step = hp.lr * (1.0f - fminf((float)cnt0, hp.transition_steps) / hp.transition_steps);
+  else
+    step = hp.lr * powf(hp.decay_rate, (float)cnt0 / hp.transition_steps);
+  if (hp.kind == DIPS_OPT_RMSPROP) {
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+      float g = __ldcg(grad + i);
+      if (gnorm >= 0.0f) g = (g / gnorm) * hp.max_norm;
+      const float v = (1.0f - hp.b2) * (g * g) + hp.b2 * nu[i];
+      nu[i] = v;
+      const float upd = g / sqrtf(v + hp.eps);
+      params[i] = params[i] + (upd * step) * -1.0f;
+    }
+    if (threadIdx.x == 0) *count = cnt0 + 1;
+    return;
+  }
   for (int i = threadIdx.x; i < P; i += blockDim.x) {
     float g = __ldcg(grad + i);  // L2: other blocks of k_reduce_adam wrote it in this launch
     if (gnorm >= 0.0f) g = (g / gnorm) * hp.max_norm;
@@ -1059,10 +1076,22 @@ extern "C" int dips_loss_coeff_tangent(const dips_arch_t* arch, const float* par
   return DIPS_OK;
 }
 
+static int check_hp(const dips_adam_t* hp) {
+  DIPS_REQUIRE(hp, DIPS_E_ARG, "null optimizer hyperparameters");
+  DIPS_REQUIRE(hp->kind == DIPS_OPT_ADAM || hp->kind == DIPS_OPT_RMSPROP, DIPS_E_ARG, "unknown optimizer kind %d",
+               hp->kind);
+  DIPS_REQUIRE(hp->schedule == DIPS_SCHED_EXPONENTIAL || hp->schedule == DIPS_SCHED_POLYNOMIAL, DIPS_E_ARG,
+               "unknown schedule %d", hp->schedule);
+  DIPS_REQUIRE(hp->transition_steps > 0.0f, DIPS_E_ARG, "transition_steps must be positive");
+  return DIPS_OK;
+}
+
 extern "C" int dips_adam_step(const dips_arch_t* arch, const dips_adam_t* hp, float* params, const float* grad,
                               float* mu, float* nu, int64_t* count, cudaStream_t stream) {
   const int P = arch_params(arch);
   DIPS_REQUIRE(P > 0 && hp && params && grad && mu && nu && count, DIPS_E_ARG, "dips_adam_step: bad argument");
+  int sth = check_hp(hp);
+  if (sth) return sth;
   k_adam<<<1, 1024, 0, stream>>>(*hp, P, params, grad, mu, nu, count);
   DIPS_CHECK_LAUNCH("dips_adam_step");
   return DIPS_OK;
@@ -1075,6 +1104,8 @@ static int train_step(const dips_arch_t* arch, const dips_adam_t* hp, float* par
   int st = check_rec(rec, batch);
   if (st) return st;
   DIPS_REQUIRE(hp && params && mu && nu && count, DIPS_E_ARG, "dips_train_step: null pointer");
+  st = check_hp(hp);
+  if (st) return st;
   const ArchOps* ops = find_arch(arch);
   if (!ops) return DIPS_E_UNSUPPORTED;
   Workspace W;
@@ -1194,6 +1225,10 @@ extern "C" int dips_instances_prepare(const dips_arch_t* arch, const dips_instan
 
 extern "C" int dips_train_step_instances(const dips_arch_t* arch, const dips_adam_t* hp, const void* table, int32_t n,
                                          int64_t max_batch, cudaStream_t stream) {
+  if (hp) {
+    const int sth = check_hp(hp);
+    if (sth) return sth;
+  }
   DIPS_REQUIRE(arch && hp && table && n > 0 && n <= 256 && max_batch > 0 && max_batch <= 0x7fffffff, DIPS_E_ARG,
                "dips_train_step_instances: bad argument");
   const ArchOps* ops = find_arch(arch);

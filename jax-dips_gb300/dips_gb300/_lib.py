@@ -184,7 +184,12 @@ class ArchT(ctypes.Structure):
 
 
 class AdamT(ctypes.Structure):
-    _fields_ = [(n, c_f32) for n in ("lr", "decay_rate", "transition_steps", "max_norm", "b1", "b2", "eps")]
+    _fields_ = [(n, c_f32) for n in ("lr", "decay_rate", "transition_steps", "max_norm", "b1", "b2", "eps")] + [
+        ("kind", c_i32), ("schedule", c_i32)]
+
+
+OPT_ADAM, OPT_RMSPROP = 0, 1
+SCHED_EXPONENTIAL, SCHED_POLYNOMIAL = 0, 1
 
 
 class InstanceT(ctypes.Structure):

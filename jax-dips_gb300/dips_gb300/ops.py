@@ -97,14 +97,19 @@ def residual_loss(params, arch: Arch, level: FVLevel, batch_ids=None):
 
 class AdamState:
     """clip_by_global_norm -> scale_by_adam -> scale_by_schedule(exponential_decay) -> scale(-1)
-    (solvers/optimizers.py:33-54); moments and step count live on the device."""
+    (solvers/optimizers.py:33-54); moments and step count live on the device.
+
+    ``kind="rmsprop"`` is optax.rmsprop (b2 is then its decay; mu unused) and
+    ``schedule="polynomial"`` optax.polynomial_schedule to 0 over transition_steps (dips_adam_t)."""
 
     def __init__(self, n: int, lr=1e-3, decay_rate=0.9, transition_steps=1000, max_norm=1.0,
-                 b1=0.9, b2=0.999, eps=1e-8, device="cuda"):
+                 b1=0.9, b2=0.999, eps=1e-8, device="cuda", kind="adam", schedule="exponential"):
         self.mu = torch.zeros(n, dtype=torch.float32, device=device)
         self.nu = torch.zeros(n, dtype=torch.float32, device=device)
         self.count = torch.zeros(1, dtype=torch.int64, device=device)
-        self.hp = _lib.AdamT(lr, decay_rate, float(transition_steps), max_norm, b1, b2, eps)
+        k = {"adam": _lib.OPT_ADAM, "rmsprop": _lib.OPT_RMSPROP}[kind]
+        sc = {"exponential": _lib.SCHED_EXPONENTIAL, "polynomial": _lib.SCHED_POLYNOMIAL}[schedule]
+        self.hp = _lib.AdamT(lr, decay_rate, float(transition_steps), max_norm, b1, b2, eps, k, sc)
 
     def step(self, arch: Arch, params: torch.Tensor, grad: torch.Tensor):
         lib = _lib.load()

@@ -85,17 +85,19 @@ def adam_state_from_dict(n_params, optimizer_dict, device):
     lr = float(optimizer_dict.get("learning_rate", 1e-3))
     sched = optimizer_dict.get("sched", {}) or {}
     if name == "custom":
-        if sched.get("scheduler_name", "exponential") != "exponential":
-            raise NotImplementedError("only the exponential schedule is on the GB300 path")
+        sname = sched.get("scheduler_name", "exponential")
+        if sname not in ("exponential", "polynomial"):  # get_scheduler (optimizers.py:13-30)
+            raise ValueError(f"Unknown scheduler: {sname}")
         return ops.AdamState(n_params, lr=lr, decay_rate=float(sched.get("decay_rate", 0.96)), transition_steps=1000,
-                             max_norm=1.0, device=device)
+                             max_norm=1.0, device=device, schedule=sname)
     if name == "adam":  # optax.adam: no clipping, constant rate
         return ops.AdamState(n_params, lr=lr, decay_rate=1.0, transition_steps=1000, max_norm=float("inf"),
                              device=device)
+    if name == "rmsprop":  # optax.rmsprop(lr): decay 0.9, eps 1e-8, no clipping, constant rate
+        return ops.AdamState(n_params, lr=lr, decay_rate=1.0, transition_steps=1000, max_norm=float("inf"), b2=0.9,
+                             eps=1e-8, device=device, kind="rmsprop")
     if name == "lbfgs":  # Trainer.solve runs scipy's L-BFGS-B instead (solve_jaxopt, trainer.py:354-420)
         return None
-    if name == "rmsprop":
-        raise NotImplementedError(f"optimizer {name!r} is outside the GB300 path")
     raise ValueError(f"Unknown optimizer: {name}")
 
 

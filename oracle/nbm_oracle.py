@@ -705,15 +705,26 @@ def sequential_batches(n_points, batch_size):
 # optimizer: clip_by_global_norm(1) -> scale_by_adam -> scale_by_schedule(exp decay) -> scale(-1)
 # ----------------------------------------------------------------------------------------
 class ChainedAdam:
-    """``chained_adam`` (optimizers.py:33-54) with optax 0.1.5 semantics, float32, flat params."""
+    """``chained_adam`` (optimizers.py:33-54) with optax 0.1.5 semantics, float32, flat params.
+
+    ``schedule``: "exponential" (``optax.exponential_decay``, non-staircase) or "polynomial"
+    (``optax.polynomial_schedule`` with end value 0 and power 1, optimizers.py:25-28: the rate
+    falls linearly to 0 over ``transition_steps`` steps and stays there)."""
 
     def __init__(self, n, lr=1e-3, decay_rate=0.9, transition_steps=1000, max_norm=1.0,
-                 b1=0.9, b2=0.999, eps=1e-8):
+                 b1=0.9, b2=0.999, eps=1e-8, schedule="exponential"):
         self.mu = np.zeros(n, F32)
         self.nu = np.zeros(n, F32)
         self.count = 0
         self.lr, self.rate, self.ts, self.max_norm = F32(lr), F32(decay_rate), transition_steps, F32(max_norm)
         self.b1, self.b2, self.eps = F32(b1), F32(b2), F32(eps)
+        self.schedule = schedule
+
+    def step_size(self):
+        if self.schedule == "polynomial":
+            c = F32(min(max(self.count, 0), self.ts))
+            return F32(self.lr * (F32(1) - c / F32(self.ts)))
+        return F32(self.lr * self.rate ** F32(self.count / self.ts))
 
     def update(self, params, grads):
         g = np.asarray(grads, F32)
@@ -726,7 +737,25 @@ class ChainedAdam:
         mu_hat = self.mu / (F32(1) - self.b1 ** F32(cnt))
         nu_hat = self.nu / (F32(1) - self.b2 ** F32(cnt))
         upd = mu_hat / (np.sqrt(nu_hat) + self.eps)
-        step = self.lr * self.rate ** F32(self.count / self.ts)
+        step = self.step_size()
         upd = (upd * F32(step)) * F32(-1.0)
         self.count = cnt
         return (np.asarray(params, F32) + upd).astype(F32)
+
+
+class RMSprop:
+    """``optax.rmsprop(learning_rate)`` (optimizers.py:82-87; optax 0.1.5: ``scale_by_rms`` with
+    decay 0.9, eps 1e-8 and initial scale 0, then ``scale(-learning_rate)``), float32, flat params:
+    nu = (1 - decay) g^2 + decay nu; params += -lr g / sqrt(nu + eps)."""
+
+    def __init__(self, n, lr=1e-3, decay=0.9, eps=1e-8):
+        self.nu = np.zeros(n, F32)
+        self.count = 0
+        self.lr, self.decay, self.eps = F32(lr), F32(decay), F32(eps)
+
+    def update(self, params, grads):
+        g = np.asarray(grads, F32)
+        self.nu = ((F32(1) - self.decay) * (g * g) + self.decay * self.nu).astype(F32)
+        upd = (g / np.sqrt(self.nu + self.eps)).astype(F32)
+        self.count += 1
+        return (np.asarray(params, F32) + (upd * self.lr) * F32(-1.0)).astype(F32)

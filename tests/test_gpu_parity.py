@@ -141,6 +141,63 @@ def test_adam_step_matches_optax_chain():
     assert int(opt.count.item()) == 6
 
 
+@pytest.mark.parametrize("variant", ["polynomial", "rmsprop"])
+def test_optimizer_variants_match_optax(variant):
+    """get_optimizer's other options (solvers/optimizers.py:13-97): the chained Adam with the
+    polynomial schedule (rate to 0 over transition_steps, here 3 of the 6 steps) and optax.rmsprop,
+    through dips_adam_step and through the fused training step's tail."""
+    from dips_gb300 import ops
+    from dips_gb300.nn import n_params
+
+    case = _parity.build_case("sphere", n=16, arch=(2, 16, 2, 16))
+    P = n_params(case.gpu_arch())
+    rng = np.random.default_rng(2)
+    if variant == "polynomial":
+        ref = O.ChainedAdam(P, lr=1e-3, transition_steps=3, schedule="polynomial")
+        opt = ops.AdamState(P, lr=1e-3, transition_steps=3, schedule="polynomial")
+    else:
+        ref = O.RMSprop(P, lr=1e-3)
+        opt = ops.AdamState(P, lr=1e-3, decay_rate=1.0, max_norm=float("inf"), b2=0.9, eps=1e-8, kind="rmsprop")
+    p_ref = case.params.copy()
+    p_gpu = torch.as_tensor(case.params.copy(), device="cuda")
+    for it in range(6):
+        scale = 0.3 if it % 2 == 0 else 5.0
+        g = (rng.standard_normal(P) * scale / np.sqrt(P)).astype(F32)
+        p_ref = ref.update(p_ref, g)
+        opt.step(case.gpu_arch(), p_gpu, torch.as_tensor(g, device="cuda"))
+    np.testing.assert_allclose(p_gpu.cpu().numpy(), p_ref, rtol=1e-5, atol=1e-7)
+    if variant == "polynomial":  # the last three steps had rate 0
+        assert float(ref.step_size()) == 0.0
+
+
+@pytest.mark.parametrize("variant", ["polynomial", "rmsprop"])
+def test_train_steps_with_optimizer_variants_track_oracle(variant):
+    from dips_gb300 import ops
+
+    case = _parity.build_case("sphere", n=16, arch=(1, 1, 2, 10))
+    lvl = case.gpu_level()
+    arch = case.gpu_arch()
+    P = case.params.size
+    params = torch.as_tensor(case.params.copy(), device="cuda")
+    if variant == "polynomial":
+        opt = ops.AdamState(P, lr=1e-3, transition_steps=4, schedule="polynomial")
+        ref = O.ChainedAdam(P, lr=1e-3, transition_steps=4, schedule="polynomial")
+    else:
+        opt = ops.AdamState(P, lr=1e-3, decay_rate=1.0, max_norm=float("inf"), b2=0.9, eps=1e-8, kind="rmsprop")
+        ref = O.RMSprop(P, lr=1e-3)
+    ws = ops.StepWorkspace(arch, lvl.n, lvl.max_jobs(lvl.n))
+    loss = torch.empty((), dtype=torch.float64, device="cuda")
+    p_ref = case.params.copy()
+    rg = case.oracle_geometry()
+    for _ in range(5):
+        ops.train_step(arch, params, opt, lvl, None, ws, loss)
+        l_ref, g_ref = L.loss_and_grad(p_ref, case.arch, rg)
+        p_ref = ref.update(p_ref, g_ref)
+        torch.cuda.synchronize()
+        assert abs(float(loss) - l_ref) <= 1e-4 * abs(l_ref)
+    np.testing.assert_allclose(params.cpu().numpy(), p_ref, rtol=1e-4, atol=1e-6)
+
+
 def test_train_steps_track_oracle():
     from dips_gb300 import ops
 

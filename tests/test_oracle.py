@@ -131,3 +131,17 @@ def test_quadratic_interpolation_reproduces_a_convex_quadratic():
     t = T(p)
     assert np.max(np.abs(q - exact)) < 2e-5
     assert np.max(np.abs(t - exact)) > 100 * np.max(np.abs(q - exact))
+
+
+def test_polynomial_schedule_and_rmsprop_semantics():
+    # polynomial_schedule(lr, end 0, power 1, transition_steps 4): lr (1 - min(count, 4) / 4)
+    opt = O.ChainedAdam(1, lr=1e-2, transition_steps=4, schedule="polynomial")
+    steps = []
+    for _ in range(6):
+        steps.append(float(opt.step_size()))
+        opt.update(np.zeros(1, F32), np.ones(1, F32))
+    np.testing.assert_allclose(steps, [1e-2, 7.5e-3, 5e-3, 2.5e-3, 0.0, 0.0], rtol=1e-6, atol=1e-12)
+    # rmsprop: first step -lr g / sqrt((1 - decay) g^2 + eps)
+    r = O.RMSprop(2, lr=1e-2)
+    p1 = r.update(np.zeros(2, F32), np.array([2.0, -0.5], F32))
+    np.testing.assert_allclose(p1, [-1e-2 * 2 / np.sqrt(0.1 * 4), 1e-2 * 0.5 / np.sqrt(0.1 * 0.25)], rtol=1e-5)
