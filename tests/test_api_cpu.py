@@ -73,3 +73,23 @@ def test_nonlinear_operators_are_callables_and_setup_refuses_others():
     assert callable(init_fn)
     with pytest.raises(NotImplementedError):
         trainer.setup(one, one, one, one, one, one, one, one, one, one, one, nonlinear_op_p=np.cbrt)
+
+
+def test_optimizer_dict_maps_to_the_step_hyperparameters():
+    pytest.importorskip("torch")
+    from dips_gb300 import _lib, trainer
+
+    custom = trainer.adam_state_from_dict(10, {"optimizer_name": "custom", "learning_rate": 1e-2,
+                                               "sched": {"scheduler_name": "polynomial", "decay_rate": 0.9}}, "cpu")
+    assert custom.hp.kind == _lib.OPT_ADAM and custom.hp.schedule == _lib.SCHED_POLYNOMIAL
+    assert custom.hp.max_norm == 1.0
+    rms = trainer.adam_state_from_dict(10, {"optimizer_name": "rmsprop", "learning_rate": 1e-2}, "cpu")
+    assert rms.hp.kind == _lib.OPT_RMSPROP and abs(rms.hp.b2 - 0.9) < 1e-7 and rms.hp.decay_rate == 1.0
+    assert rms.hp.max_norm == float("inf")
+    adam = trainer.adam_state_from_dict(10, {"optimizer_name": "adam", "learning_rate": 1e-2}, "cpu")
+    assert adam.hp.kind == _lib.OPT_ADAM and adam.hp.schedule == _lib.SCHED_EXPONENTIAL and adam.hp.decay_rate == 1.0
+    assert trainer.adam_state_from_dict(10, {"optimizer_name": "lbfgs"}, "cpu") is None
+    with pytest.raises(ValueError):
+        trainer.adam_state_from_dict(10, {"optimizer_name": "custom", "sched": {"scheduler_name": "cosine"}}, "cpu")
+    with pytest.raises(ValueError):
+        trainer.adam_state_from_dict(10, {"optimizer_name": "sgd"}, "cpu")
