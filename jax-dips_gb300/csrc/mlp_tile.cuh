@@ -2,8 +2,8 @@
 // layers of width 16 (nn/mlp/MLP.py:93-139): residual, adjoint and weight gradient of the NBM
 // loss (solvers/poisson/trainer.py:783-789, :892-912) for bulk points and for general jobs.
 //
-// Included by residual_arch.cuh inside the per-shape namespace (after Net, Workspace, the
-// constant bank and act_tanh are defined).
+// Included by residual_arch.cuh inside the per-shape namespace (after Net, Workspace and
+// act_tanh are defined).
 //
 // Work unit: one warp owns a tile of 32 jobs and runs it through the whole network with
 // __syncwarp only.  Every layer is a [32 jobs x W] x [W x W] product computed as 4 x NT

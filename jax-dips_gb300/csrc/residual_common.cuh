@@ -101,8 +101,7 @@ __device__ __forceinline__ void job_point(const PtsH& ph, const int32_t* ids, in
   job_coords(p, ph.h, code, x);
 }
 
-// Kernels and launches of one DoubleMLP shape (one translation unit per shape, each with
-// its own constant-bank copy of the weights).
+// Kernels and launches of one DoubleMLP shape (one translation unit per shape).
 // Optional CUDA events recorded on the launching stream at the step's phase boundaries
 // (slot numbers as in dips_train_step_profiled).  A null Marks pointer records nothing.
 struct Marks {
@@ -132,8 +131,9 @@ struct ArchOps {
   int m_layers, m_width, p_layers, p_width;
   int n_params;
   int bulk_ok;  // 0: no bulk-point kernel; every point is expanded into jobs
-  // makes params the operands of the kernels that follow on s; for_eval: also for mlp_eval (the
-  // constant-bank copy, which the tile engine's training launches do not read)
+  // hands params to the launches that follow on the calling thread, for a shape whose kernels do
+  // not take them from the Workspace (the tcgen05 engine records the pointer); for_eval: the call
+  // comes from mlp_eval.  The FP32 shapes read their own call's parameters and do nothing here.
   int (*load_params)(const float* params, int for_eval, cudaStream_t s);
   int (*job_forward)(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s);
   int (*job_adjoint)(const PtsH& ph, const int32_t* ids, const Workspace& w, const Marks* mk, cudaStream_t s);

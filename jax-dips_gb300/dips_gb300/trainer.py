@@ -11,7 +11,10 @@ Differences from the reference, all on purpose:
 * The training step is one CUDA graph: batch ids from the device step counter, residual
   forward, adjoint, gradient reduction, chained Adam.
 * ``model_dict["preconditioner"]`` may be absent (the reference requires it,
-  trainer.py:229); an enabled preconditioner is not supported.
+  trainer.py:229); an enabled one (uniform ``layer_widths``) is trained with the networks.
+* ``optimizer_name == "lbfgs"`` runs scipy's L-BFGS-B on the GPU loss and gradient instead of
+  jaxopt (solve_jaxopt, trainer.py:354-420).
+* Nonlinear operators are ``None`` or one of ``dips_gb300.nonlinear``'s kinds.
 """
 
 from __future__ import annotations
