@@ -37,7 +37,8 @@ enum {
   DIPS_E_ARG = 1,        /* invalid argument (null pointer, bad size, unsupported shape) */
   DIPS_E_CUDA = 2,       /* a CUDA call failed */
   DIPS_E_WORKSPACE = 3,  /* workspace too small */
-  DIPS_E_UNSUPPORTED = 4 /* network shape without a compiled kernel */
+  DIPS_E_UNSUPPORTED = 4 /* network shape without a compiled kernel, or a feature the entry
+                            point does not take (nonlinear records, the learned preconditioner) */
 };
 
 /* Level-set grid: ghosted samples and ghosted coordinates (n+2 each). */
