@@ -78,3 +78,55 @@ def test_noalloc_step_rejects_bad_sizes_on_the_host():
     assert need > 64 << 20
     st = lib.dips_train_step_noalloc(a, None, p, p, p, p, None, None, 4096, 10**8, p, None, None)
     assert st == 3 and b"built-in" in lib.dips_last_error()
+
+
+# entry points that return a size, a count, a string or a previous setting rather than a status
+_NOT_STATUS = {"dips_version", "dips_last_error", "dips_tc_set_wait_limit", "dips_num_params", "dips_arch_supported",
+               "dips_step_workspace_bytes", "dips_bicgstab_workspace_bytes", "dips_instances_table_bytes",
+               "dips_geometry_assemble_scratch_bytes", "dips_xla_workspace_bytes", "dips_xla_set_status_fn"}
+
+
+def _status_entry_points():
+    from dips_gb300 import _lib
+
+    return [n for n in sorted(_lib._SIGS) if n not in _NOT_STATUS]
+
+
+@pytest.mark.parametrize("name", _status_entry_points())
+def test_null_pointers_are_rejected_on_the_host(name):
+    """Every status-returning entry point, called with every pointer NULL and every size 1,
+    returns a non-zero status with a message (the XLA handlers, which return nothing, record
+    the message), before any CUDA call: no host dereference of a NULL struct pointer and no
+    launch on NULL device pointers."""
+    import ctypes
+
+    from dips_gb300 import _lib
+
+    lib = _lib.load()
+    res, args = _lib._SIGS[name]
+    vals = []
+    for a in args:
+        if a in (ctypes.c_float, ctypes.c_double):
+            vals.append(1.0)
+        elif a is ctypes.c_void_p or a is ctypes.c_char_p or issubclass(a, (ctypes._Pointer, ctypes._CFuncPtr)):
+            vals.append(None)
+        else:
+            vals.append(1)
+    lib.dips_last_error()
+    st = getattr(lib, name)(*vals)
+    msg = lib.dips_last_error().decode()
+    if res is None:  # XLA custom-call handlers
+        assert msg.startswith("dips_xla"), msg
+        return
+    assert st != 0, name
+    assert msg and msg != "no error", name
+
+
+def test_size_queries_without_a_shape_return_zero():
+    from dips_gb300 import _lib
+
+    lib = _lib.load()
+    assert lib.dips_num_params(None) == -1
+    assert lib.dips_arch_supported(None) == 0
+    assert lib.dips_step_workspace_bytes(None, 1, 1) == 0
+    assert lib.dips_xla_workspace_bytes(None, 1, 1) == 0
