@@ -466,6 +466,9 @@ def run_ours(args, rank, world):
                                     "residual, adjoint and dW of every job)"),
                          "achieved": dom_tflops, "peak": dom_peak, "unit": "TFLOP/s",
                          "frac": dom_tflops / dom_peak, "traffic": FUSED_TRAFFIC.get((args.n, B)),
+                         "traffic_source": ("dram__bytes_read.sum + dram__bytes_write.sum of one launch, ncu "
+                                            "capture of this workload (profiles/k_tile_engine_sphere_3x32_and_"
+                                            "lpbe_2x16.md)") if (args.n, B) in FUSED_TRAFFIC else None,
                          "algorithmic": f"3 x F per job, F = sum(2*in*out+out) + tanh count = "
                                         f"{dom_f}; {dom_jobs} jobs per launch (bulk points: {bulk_m} u-, {bulk_p} u+)",
                          "peak_source": peak_src, "fp32_peak_tflops": fp32_peak,
