@@ -199,9 +199,9 @@ def run_reference(args, rank, world):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"{args.problem} {args.n}^3, DoubleMLP {args.arch}/{args.arch} tanh, h=dx; each step a sample of "
-                               f"{sample} points (geometry + residual + gradient, recomputed per step as the "
-                               "reference does)", "global_batch": sample},
+        "config": {"workload": nbm_workload(args), "global_batch": min(args.batch, args.n ** 3) * args.gpus,
+                   "cpu_sample_per_step": f"{sample} points of the batch's distribution (geometry + residual + "
+                                          "gradient, recomputed per step as the reference does)"},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{steps} steps x {sample} points of the {args.n}^3 grid, {wall:.1f} s"},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -217,6 +217,14 @@ def run_reference(args, rank, world):
 def arch_tuple(args):
     L, W = (int(v) for v in args.arch.split("x"))
     return (L, W, L, W)
+
+
+def nbm_workload(args):
+    """The workload both arms report in ``config.workload`` (the metric's configuration)."""
+    tensor = arch_tuple(args)[1] == 64
+    return (f"NBM training step, {args.problem} {args.n}^3 (phi grid {args.n_ls or args.n}^3), "
+            f"DoubleMLP {args.arch}/{args.arch} tanh ({'TF32 tensor cores' if tensor else 'FP32'}), "
+            "h=dx, minibatch drawn uniformly")
 
 
 def run_ours(args, rank, world):
@@ -452,9 +460,7 @@ def run_ours(args, rank, world):
             "vs_baseline": None,
             "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": f"NBM training step, {args.problem} {args.n}^3 (phi grid {args.n_ls or args.n}^3), "
-                                   f"DoubleMLP {args.arch}/{args.arch} tanh ({'TF32 tensor cores' if tensor else 'FP32'}), "
-                                   "h=dx, minibatch drawn uniformly",
+            "config": {"workload": nbm_workload(args),
                        "global_batch": B * world, "points": int(lvl.n), "jobs_per_step": jobs_m + jobs_p,
                        "l2": "flushed (256 MB write) between timed steps", "cuda_graph": world == 1,
                        "autotuned_cta_warps": cta_warps,
