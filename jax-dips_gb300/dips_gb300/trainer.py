@@ -125,7 +125,7 @@ class Trainer:
     def __init__(self, lvl_gstate: GridState, tr_gstate: GridState, eval_gstate: GridState, sim_state_fn,
                  num_epochs=1000, batch_size=131072, optimizer_dict=None, model_dict=None, batching="sequential",
                  seed=0, checkpoint_dir=None, restart=False, restart_checkpoint_dir=None, use_graph=True,
-                 device="cuda", multi_gpu=False):
+                 device="cuda", multi_gpu=False, checkpoint_interval=None):
         if not torch.cuda.is_available():
             raise RuntimeError("dips_gb300 runs on a CUDA GPU; none is available")
         _lib.load()
@@ -141,6 +141,7 @@ class Trainer:
         self.batching = batching
         self.use_graph = use_graph
         self.checkpoint_dir = checkpoint_dir
+        self.checkpoint_interval = int(checkpoint_interval or 0)
         # ---- level set on the level-set grid (samples of the user's phi callable)
         self.ls = levelset.LevelSetGrid.from_callable(lvl_gstate, sim_state_fn.phi_fn, device)
         # ---- training points, batches (DatasetDict, data/data_management.py:79-159)
@@ -269,7 +270,7 @@ class Trainer:
         self.lbfgs_result = res
         self.epoch_store = np.arange(len(losses))
         self.loss_epochs = np.asarray(losses)
-        if self.checkpoint_dir:
+        if self.checkpoint_dir and self.rank == 0:
             self.save_checkpoint(self.checkpoint_dir, len(losses))
         return self.epoch_store, self.loss_epochs
 
@@ -295,9 +296,10 @@ class Trainer:
                 logger.info("epoch %d loss %.6e", epoch, loss_epochs[epoch - self.epoch_start])
             if callback is not None:
                 callback(epoch, loss_epochs[epoch - self.epoch_start])
+            self._interval_checkpoint(epoch)
         self.epoch_store = np.arange(self.epoch_start, self.num_epochs)
         self.loss_epochs = loss_epochs
-        if self.checkpoint_dir:
+        if self.checkpoint_dir and self.rank == 0:  # the ranks hold the same state: one writer
             self.save_checkpoint(self.checkpoint_dir, self.num_epochs)
         return self.epoch_store, loss_epochs
 
@@ -331,6 +333,15 @@ class Trainer:
         fields = {"solution": u.reshape(shape), "grad_solution": gu.reshape(shape + (3,)),
                   "grad_normal_solution": gn.reshape(shape), "phi": self.ls(R).reshape(shape)}
         return io.write_vtk_manual(gstate, fields, filename)
+
+    def _interval_checkpoint(self, epoch):
+        """multi_GPU_train's checkpoints (trainer.py:769-777): after every checkpoint_interval-th
+        epoch, written by rank 0.  The reference's single-GPU loop saves at the end only
+        (trainer.py:470-477), and so does this one."""
+        if (self.multi_gpu and self.rank == 0 and self.checkpoint_dir and self.checkpoint_interval > 0
+                and (epoch + 1) % self.checkpoint_interval == 0):
+            return self.save_checkpoint(self.checkpoint_dir, epoch + 1)
+        return None
 
     def save_checkpoint(self, checkpoint_dir, epoch):
         """pickle of {opt_state, params, epoch, batch_size, resolution} (trainer.py:340-351).
@@ -410,7 +421,7 @@ def setup(initial_value_fn, dirichlet_bc_fn, lvl_set_fn, mu_m_fn_, mu_p_fn_, k_m
             tr = Trainer(lvl_gstate, tr_gstate, eval_gstate, fn, num_epochs=num_epochs, batch_size=batch_size,
                          optimizer_dict=optimizer_dict, model_dict=model_dict, batching=batching, seed=seed,
                          checkpoint_dir=checkpoint_dir, restart=restart, restart_checkpoint_dir=restart_checkpoint_dir,
-                         use_graph=use_graph, multi_gpu=multi_gpu)
+                         use_graph=use_graph, multi_gpu=multi_gpu, checkpoint_interval=checkpoint_interval)
             epoch_store, loss_epochs = tr.solve(print_rate=print_rate)
             u, gu, gn = tr.evaluate_solution_and_gradients(eval_gstate)
             new = dataclasses.replace(sim_state, solution=u, grad_solution=gu, grad_normal_solution=gn)

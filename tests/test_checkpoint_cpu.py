@@ -83,3 +83,24 @@ def test_restore_skips_stray_files_and_refuses_another_batch_size(tmp_path):
     with pytest.raises(ValueError, match="batch_size 4096"):
         Trainer._restore(other, str(tmp_path))
     assert int(other.opt.count) == 0
+
+
+def test_interval_checkpoints_of_the_multi_gpu_loop(tmp_path):
+    """multi_GPU_train saves after every checkpoint_interval-th epoch (trainer.py:769-777); one
+    rank writes (the ranks hold the same state); the single-GPU loop saves at the end only."""
+    d = str(tmp_path)
+    t = _trainer(3, 5)
+    t.checkpoint_dir, t.checkpoint_interval = d, 4
+    t.save_checkpoint = lambda cdir, epoch: Trainer.save_checkpoint(t, cdir, epoch)
+    for multi, rank in ((False, 0), (True, 1)):
+        t.multi_gpu, t.rank = multi, rank
+        assert all(Trainer._interval_checkpoint(t, e) is None for e in range(12))
+    assert os.listdir(d) == []
+    t.multi_gpu, t.rank = True, 0
+    written = [Trainer._interval_checkpoint(t, e) for e in range(12)]
+    assert [os.path.basename(p) for p in written if p] == ["checkpoint_4", "checkpoint_8", "checkpoint_12"]
+    t.checkpoint_interval = 0
+    assert Trainer._interval_checkpoint(t, 15) is None
+    r = _trainer(0, 0)
+    Trainer._restore(r, d)
+    assert r.epoch_start == 12
