@@ -409,6 +409,12 @@ def setup(initial_value_fn, dirichlet_bc_fn, lvl_set_fn, mu_m_fn_, mu_p_fn_, k_m
                 optimizer_dict: dict = None, model_dict: dict = None, restart: bool = False,
                 restart_checkpoint_dir: str = "./checkpoints", print_rate: int = 1, batching: str = "sequential",
                 seed: int = 42, use_graph: bool = True):
+        """``init_fn`` (trainer.py:1035-1136): the initial state on ``eval_gstate`` and ``solve_fn``.
+
+        Accepted for the reference's signature and without effect here: ``results_dir`` and
+        ``loss_plot_name`` (the reference's matplotlib loss plot; ``solve_fn`` returns the losses)
+        and ``mgrad_over_pgrad_scalefactor``, which has no effect in the reference either (its one
+        use is in ``Trainer.__update``, trainer.py:792-815, which nothing calls)."""
         if algorithm != 0:
             raise NotImplementedError("algorithm 1 (network extrapolation) is unimplemented in the reference too")
         R = torch.as_tensor(eval_gstate.R, device="cuda")
