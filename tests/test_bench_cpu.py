@@ -71,3 +71,13 @@ def test_reference_arm_under_torchrun_prints_once():
     lines = _json_lines(p.stdout)
     assert len(lines) == 1, p.stdout[-2000:]
     _check_line(lines[0], 2)
+
+
+def test_algorithmic_flops_per_network_evaluation():
+    """The roofline's numerator: F(net) = sum over layers of 2 in out + out, plus one per tanh
+    (3 inputs, one output); the training launch counts 3 F per job."""
+    b = _bench_module()
+    assert b.net_flops(3, 32) == (2 * 3 * 32 + 32) + 2 * (2 * 32 * 32 + 32) + (2 * 32 + 1) + 3 * 32 == 4545
+    assert b.net_flops(2, 16) == (2 * 3 * 16 + 16) + (2 * 16 * 16 + 16) + (2 * 16 + 1) + 2 * 16
+    assert b.net_flops(4, 64) == (2 * 3 * 64 + 64) + 3 * (2 * 64 * 64 + 64) + (2 * 64 + 1) + 4 * 64
+    assert b.net_flops(1, 1) == (2 * 3 + 1) + (2 + 1) + 1
