@@ -54,6 +54,30 @@ def load(ref_root, x64=False):
     return mods
 
 
+def load_data_management(ref_root):
+    """Install the stand-in and import the reference's ``data/data_management.py`` (``DatasetDict``,
+    the batching of the training points).  That module also imports ``utils/conversions.py``
+    (dlpack converters between jax and torch, and NVIDIA warp helpers), which the batching code
+    does not use and which cannot be imported without jaxlib and warp: a module whose functions
+    raise stands in for it."""
+    import importlib
+    import types
+
+    refjax.install(x64=False)
+    if ref_root not in sys.path:
+        sys.path.insert(0, ref_root)
+    name = "jax_dips.utils.conversions"
+    if name not in sys.modules:
+        stub = types.ModuleType(name)
+
+        def _unavailable(*a, **k):
+            raise NotImplementedError(name + " is not available on the stand-in")
+
+        stub.jax_to_torch = stub.torch_to_jax = _unavailable
+        sys.modules[name] = stub
+    return importlib.import_module("jax_dips.data.data_management")
+
+
 def _key(*args):
     parts = []
     for a in args:

@@ -270,9 +270,40 @@ def run_fv_case(args):
         time.time() - t0
 
 
+# the per-device batch layout of DatasetDict(x, batch_size, num_gpus) (data_management.py:79-159):
+# (points, batch size, devices)
+DATA_CASES = ((1000, 128, 1), (1000, 128, 2), (1000, 100, 3), (1024, 256, 4), (999, 1000, 2),
+              (4096, 4096, 1), (37, 8, 3), (125, 7, 1), (50, 7, 4))
+PAD = -123.0  # stands for the padding points in ref_dataset_layout.npz
+
+
+def run_data_case(ref_root):
+    """``ref_dataset_layout.npz``: ``DatasetDict(x, batch_size, num_gpus).batched_data`` of the
+    reference for each of DATA_CASES, x[i] = (3i, 3i+1, 3i+2)/7 so that every point is
+    identifiable.  The padding points are drawn by ``generate_random_points_like`` with
+    ``jax.random.PRNGKey(0)``, which the stand-in cannot reproduce; that one function is replaced by
+    one returning rows of PAD, so the fixture records where the padding goes (its values are a
+    documented deviation: the product draws them with numpy)."""
+    import ref_harness as H
+    import refjax
+
+    dm = H.load_data_management(ref_root)
+    dm.generate_random_points_like = lambda x, k: refjax._wrap(np.full((k, 3), PAD, F32))
+    out = {"cases": np.array(DATA_CASES, np.int64), "pad": np.float32(PAD)}
+    for i, (n, bs, g) in enumerate(DATA_CASES):
+        x = np.arange(3 * n, dtype=F32).reshape(n, 3) / F32(7.0)
+        d = dm.DatasetDict(refjax._wrap(x), bs, num_gpus=g)
+        b = np.asarray(refjax._raw(d.batched_data), F32)
+        out[f"batched_{i}"] = b if g > 1 else b[None]
+    return out
+
+
 def main(argv):
     ref_root = argv[1] if len(argv) > 1 else DEFAULT_REFERENCE
-    names = argv[2:] or (list(CASES) + list(FV_CASES))
+    names = argv[2:] or (list(CASES) + list(FV_CASES) + ["dataset_layout"])
+    if "dataset_layout" in names:
+        np.savez_compressed(os.path.join(HERE, "ref_dataset_layout.npz"), **run_data_case(ref_root))
+        print("dataset_layout: %d cases" % len(DATA_CASES), flush=True)
     fv = [nm for nm in names if nm in FV_CASES]
     names = [nm for nm in names if nm in CASES]
     ctx = mp.get_context("spawn")
