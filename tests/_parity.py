@@ -134,9 +134,9 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 def reference_fixtures(kind="loss"):
     """Names of the fixtures written by the reference's own code (tests/golden/ref_*.npz):
     kind "loss" for the network residual cases, "fvop" for the discrete operator of a nodal vector
-    (the batch-layout fixture ``ref_dataset_layout`` is neither)."""
+    (the batch-layout and interpolant fixtures, ``ref_dataset_*`` and ``ref_interp_*``, are neither)."""
     names = sorted(f[4:-4] for f in os.listdir(GOLDEN) if f.startswith("ref_") and f.endswith(".npz"))
-    names = [k for k in names if not k.startswith("dataset_")]
+    names = [k for k in names if not k.startswith(("dataset_", "interp_"))]
     return [k for k in names if k.startswith("fvop_") == (kind == "fvop")]
 
 

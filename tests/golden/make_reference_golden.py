@@ -298,9 +298,38 @@ def run_data_case(ref_root):
     return out
 
 
+def run_interp_case(ref_root, n=16):
+    """``ref_interp_nodal16.npz``: the reference's ``multilinear_interpolation`` (interpolate.py:
+    906-1021) and ``nonoscillatory_quadratic_interpolation`` (:572-759) of a seeded nodal field on
+    the n^3 grid over [-1, 1]^3, at 650 seeded points: inside the box, in the first and last cells
+    of each axis (where both clamp their cell index and extrapolate), beyond the box, and on nodes."""
+    import ref_harness as H
+    import refjax
+
+    mods = H.load(ref_root, x64=False)
+    import jax.numpy as jnp
+
+    x = jnp.linspace(-1.0, 1.0, n, dtype=jnp.float32)
+    gs = mods["mesh"].construct(3)[0](x, x, x)
+    R = np.asarray(refjax._raw(gs.R), F32)
+    rng = np.random.default_rng(3)
+    u = (np.sin(3 * R[:, 0]) * np.cos(2 * R[:, 1]) + R[:, 2] ** 2 + 0.1 * rng.standard_normal(n ** 3)).astype(F32)
+    pts = np.concatenate([rng.uniform(-1, 1, (300, 3)), rng.uniform(-1.0, -0.8, (100, 3)),
+                          rng.uniform(0.8, 1.0, (100, 3)), rng.uniform(-1.2, 1.2, (100, 3)),
+                          R[rng.choice(n ** 3, 50)]]).astype(F32)
+    tri = mods["interpolate"].multilinear_interpolation(jnp.asarray(u), gs)
+    quad = mods["interpolate"].nonoscillatory_quadratic_interpolation(jnp.asarray(u), gs)
+    return {"n": np.int32(n), "u": u, "pts": pts,
+            "trilinear": np.asarray(refjax._raw(tri(jnp.asarray(pts))), F32).reshape(-1),
+            "quadratic": np.asarray(refjax._raw(quad(jnp.asarray(pts))), F32).reshape(-1)}
+
+
 def main(argv):
     ref_root = argv[1] if len(argv) > 1 else DEFAULT_REFERENCE
-    names = argv[2:] or (list(CASES) + list(FV_CASES) + ["dataset_layout"])
+    names = argv[2:] or (list(CASES) + list(FV_CASES) + ["dataset_layout", "interp_nodal16"])
+    if "interp_nodal16" in names:
+        np.savez_compressed(os.path.join(HERE, "ref_interp_nodal16.npz"), **run_interp_case(ref_root))
+        print("interp_nodal16", flush=True)
     if "dataset_layout" in names:
         np.savez_compressed(os.path.join(HERE, "ref_dataset_layout.npz"), **run_data_case(ref_root))
         print("dataset_layout: %d cases" % len(DATA_CASES), flush=True)
