@@ -305,7 +305,9 @@ class Trainer:
 
     # ------------------------------------------------------------------ evaluation
     def evaluate_solution_and_gradients(self, gstate: GridState):
-        """u, grad u and d_n u on a grid (trainer.py:929-977)."""
+        """u, grad u and d_n u on a grid (trainer.py:929-977): d_n u = n . grad u with n the
+        normalised central difference of the interpolated phi at spacing (dx, dy, dz)
+        (``normal_point_fn``, discretization.py:199-218)."""
         R = torch.as_tensor(gstate.R, device=self.device)
         phi = self.ls(R)
         u, gu = nn.mlp_eval(self.arch, self.params, R, phi, want_grad=True)
@@ -317,7 +319,8 @@ class Trainer:
             rm[:, a] -= float(h[a])
             d.append((self.ls(rp) - self.ls(rm)) / (2.0 * float(h[a])))
         nrm = torch.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
-        gn = (gu[:, 0] * d[0] + gu[:, 1] * d[1] + gu[:, 2] * d[2]) / nrm
+        nx, ny, nz = d[0] / nrm, d[1] / nrm, d[2] / nrm
+        gn = nx * gu[:, 0] + ny * gu[:, 1] + nz * gu[:, 2]
         return u, gu, gn
 
     # ------------------------------------------------------------------ checkpoints
